@@ -1,0 +1,321 @@
+// extern "C" entry points declared in include/combustion_gb300.h.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/combustion_gb300.h"
+#include "kernels.h"
+#include "mechanism.hpp"
+
+struct cb_mech {
+    cbg::HostMechanism host;
+    int device = 0;
+    int kmax = 0;
+    uint8_t* d_rates = nullptr;      // rates table blob
+    uint8_t* d_transport = nullptr;  // transport table blob
+    int* d_status = nullptr;         // kernel status bits
+    // Device staging for CB_HOST_MEMORY calls: two slots, each holding one chunk of inputs and outputs.
+    double* d_stage = nullptr;
+    size_t stage_doubles = 0;
+    cudaStream_t copy_stream[2] = {nullptr, nullptr};
+    cudaEvent_t slot_free[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(CB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CB_CUDA(call)                                  \
+    do {                                               \
+        cudaError_t e_ = (call);                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+int check_status(cb_mech* m) {
+    int st = 0;
+    CB_CUDA(cudaMemcpy(&st, m->d_status, sizeof st, cudaMemcpyDeviceToHost));
+    if (st) {
+        cudaMemset(m->d_status, 0, sizeof(int));
+        return fail(CB_ERR_DEVICE, "a kernel reported status " + std::to_string(st) + " (table staging wait ran out)");
+    }
+    return CB_OK;
+}
+
+enum class Path { Rates, ReactionRates, Transport };
+
+// Arguments of one launch: pointer arrays already resolved to device memory.
+int launch_path(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags,
+                cudaStream_t st) {
+    const int K = m->host.K, A = m->host.A;
+    if (n == 0) return CB_OK;
+    if (path == Path::Rates) {
+        cudaError_t e;
+        switch (m->kmax) {
+#define CB_RATES(KM)                                                                 \
+    case KM: {                                                                       \
+        cbg::RatesArgs<KM> a;                                                        \
+        std::memset(&a, 0, sizeof a);                                                \
+        for (int q = 0; q < K + 3; q++) a.in[q] = in[q];                             \
+        for (int q = 0; q < A + 2; q++) a.out[q] = out[q];                           \
+        a.flags = flags;                                                             \
+        e = cbg::launch_rates(KM, m->d_rates, (uint32_t)m->host.rates_blob.size(), &a, n, st, m->d_status); \
+        break;                                                                       \
+    }
+            CB_RATES(16) CB_RATES(64) CB_RATES(256)
+#undef CB_RATES
+        default: return fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
+        return CB_OK;
+    }
+    if (path == Path::Transport) {
+        cudaError_t e;
+        switch (m->kmax) {
+#define CB_TRANSPORT(KM)                                                             \
+    case KM: {                                                                       \
+        cbg::TransportArgs<KM> a;                                                    \
+        std::memset(&a, 0, sizeof a);                                                \
+        for (int q = 0; q < K + 1; q++) a.in[q] = in[q];                             \
+        for (int q = 0; q < K + 2; q++) a.out[q] = out[q];                           \
+        a.flags = flags;                                                             \
+        e = cbg::launch_transport(KM, m->d_transport, (uint32_t)m->host.transport_blob.size(), &a, n, st, m->d_status); \
+        break;                                                                       \
+    }
+            CB_TRANSPORT(16) CB_TRANSPORT(64) CB_TRANSPORT(256)
+#undef CB_TRANSPORT
+        default: return fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "transport kernel launch");
+        return CB_OK;
+    }
+    return fail(CB_ERR_UNSUPPORTED, "per-reaction rates are not built yet");
+}
+
+int n_inputs(const cb_mech* m, Path p) {
+    return p == Path::Rates ? m->host.K + 3 : p == Path::ReactionRates ? m->host.K + 2 : m->host.K + 1;
+}
+int n_outputs(const cb_mech* m, Path p) {
+    return p == Path::Rates ? m->host.A + 2 : p == Path::ReactionRates ? m->host.R : m->host.K + 2;
+}
+
+// Host arrays: copy chunks through two device staging slots so that the copies of one chunk overlap
+// the kernel of the other (one cudaMemcpyAsync per array per chunk).
+int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags) {
+    const int ni = n_inputs(m, path), no = n_outputs(m, path);
+    const bool uniform = path == Path::Rates && (flags & CB_UNIFORM_PRESSURE);
+    size_t chunk = (size_t)1 << 20;
+    if (chunk > n) chunk = n;
+    const size_t per_slot = (size_t)(ni + no) * chunk + 2;
+    if (m->stage_doubles < 2 * per_slot) {
+        if (m->d_stage) cudaFree(m->d_stage);
+        m->d_stage = nullptr;
+        m->stage_doubles = 0;
+        CB_CUDA(cudaMalloc(&m->d_stage, 2 * per_slot * sizeof(double)));
+        m->stage_doubles = 2 * per_slot;
+    }
+    for (int s = 0; s < 2; s++) {
+        if (!m->copy_stream[s]) CB_CUDA(cudaStreamCreateWithFlags(&m->copy_stream[s], cudaStreamNonBlocking));
+        if (!m->slot_free[s]) CB_CUDA(cudaEventCreateWithFlags(&m->slot_free[s], cudaEventDisableTiming));
+    }
+    std::vector<const double*> din(ni);
+    std::vector<double*> dout(no);
+    size_t c = 0;
+    for (size_t lo = 0; lo < n; lo += chunk, c++) {
+        const size_t len = n - lo < chunk ? n - lo : chunk;
+        const int s = (int)(c & 1);
+        cudaStream_t st = m->copy_stream[s];
+        double* base = m->d_stage + s * per_slot;
+        for (int q = 0; q < ni; q++) {
+            double* dst = base + (size_t)q * chunk;
+            if (uniform && q < 2) {
+                CB_CUDA(cudaMemcpyAsync(dst, in[q], sizeof(double), cudaMemcpyHostToDevice, st));
+            } else {
+                CB_CUDA(cudaMemcpyAsync(dst, in[q] + lo, len * sizeof(double), cudaMemcpyHostToDevice, st));
+            }
+            din[q] = dst;
+        }
+        for (int q = 0; q < no; q++) dout[q] = base + (size_t)(ni + q) * chunk;
+        int rc = launch_path(m, path, len, din.data(), dout.data(), flags & ~CB_HOST_MEMORY, st);
+        if (rc) return rc;
+        for (int q = 0; q < no; q++)
+            CB_CUDA(cudaMemcpyAsync(out[q] + lo, dout[q], len * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    for (int s = 0; s < 2; s++) CB_CUDA(cudaStreamSynchronize(m->copy_stream[s]));
+    return check_status(m);
+}
+
+int call(cb_mech* m, Path path, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+         void* stream) {
+    if (!m || !inputs || !outputs) return fail(CB_ERR_INVALID, "null argument");
+    if (flags & ~(CB_HOST_MEMORY | CB_UNIFORM_PRESSURE)) return fail(CB_ERR_INVALID, "unknown flag");
+    if ((flags & CB_UNIFORM_PRESSURE) && path != Path::Rates) return fail(CB_ERR_INVALID, "CB_UNIFORM_PRESSURE applies to rates only");
+    if (path == Path::Transport && !m->host.transport_ready) return fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
+    const int ni = n_inputs(m, path), no = n_outputs(m, path);
+    if (n == 0) return CB_OK;
+    for (int q = 0; q < ni; q++) if (!inputs[q]) return fail(CB_ERR_INVALID, "null input array");
+    for (int q = 0; q < no; q++) if (!outputs[q]) return fail(CB_ERR_INVALID, "null output array");
+    CB_CUDA(cudaSetDevice(m->device));
+    if (flags & CB_HOST_MEMORY) return call_host(m, path, n, inputs, outputs, flags);
+    return launch_path(m, path, n, inputs, outputs, flags, static_cast<cudaStream_t>(stream));
+}
+
+void to_work(const cbg::Work& w, cb_work* o) {
+    o->flops = w.flops; o->exps = w.exps; o->logs = w.logs; o->divs = w.divs; o->sqrts = w.sqrts;
+    o->bytes_in = w.bytes_in; o->bytes_out = w.bytes_out;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cb_last_error(void) { return g_error.c_str(); }
+const char* cb_version(void) { return "combustion_gb300 0.1 (sm_103a)"; }
+
+int cb_mech_create(const cb_mech_desc* desc, cb_mech** out) {
+    if (!out) return fail(CB_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    cb_mech* m = new cb_mech();
+    std::string err;
+    int rc = cbg::build_mechanism(desc, m->host, err);
+    if (rc) { delete m; return fail(rc, err); }
+    m->kmax = cbg::kmax_for(m->host.K);
+    if (!m->kmax) { delete m; return fail(CB_ERR_UNSUPPORTED, "more than 256 species"); }
+    cudaError_t e = cudaGetDevice(&m->device);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_rates, m->host.rates_blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(m->d_rates, m->host.rates_blob.data(), m->host.rates_blob.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) { cb_mech_destroy(m); return cuda_fail(e, "mechanism upload"); }
+    *out = m;
+    return CB_OK;
+}
+
+int cb_mech_validate(const cb_mech_desc* desc, cb_mech_info* info) {
+    cbg::HostMechanism h;
+    std::string err;
+    int rc = cbg::build_mechanism(desc, h, err);
+    if (rc) return fail(rc, err);
+    if (!cbg::kmax_for(h.K)) return fail(CB_ERR_UNSUPPORTED, "more than 256 species");
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->n_species = h.K; info->n_active = h.A; info->n_reactions = h.R;
+        info->rates_inputs = h.K + 3; info->rates_outputs = h.A + 2;
+        info->transport_inputs = h.K + 1; info->transport_outputs = h.K + 2;
+        info->device_table_bytes = h.rates_blob.size();
+    }
+    return CB_OK;
+}
+
+int cb_transport_fit(const cb_mech_desc* desc, double T0, double* cond, double* visc, double* diff) {
+    cbg::HostMechanism h;
+    std::string err;
+    int rc = cbg::build_mechanism(desc, h, err);
+    if (rc) return fail(rc, err);
+    rc = cbg::build_transport(h, T0, 1.0, 1.0, err);
+    if (rc) return fail(rc, err);
+    if (cond) std::memcpy(cond, h.fit_cond.data(), h.fit_cond.size() * sizeof(double));
+    if (visc) std::memcpy(visc, h.fit_visc.data(), h.fit_visc.size() * sizeof(double));
+    if (diff) std::memcpy(diff, h.fit_diff.data(), h.fit_diff.size() * sizeof(double));
+    return CB_OK;
+}
+
+int cb_mech_destroy(cb_mech* m) {
+    if (!m) return CB_OK;
+    cudaSetDevice(m->device);
+    for (int s = 0; s < 2; s++) {
+        if (m->copy_stream[s]) { cudaStreamSynchronize(m->copy_stream[s]); cudaStreamDestroy(m->copy_stream[s]); }
+        if (m->slot_free[s]) cudaEventDestroy(m->slot_free[s]);
+    }
+    cudaFree(m->d_rates);
+    cudaFree(m->d_transport);
+    cudaFree(m->d_status);
+    cudaFree(m->d_stage);
+    delete m;
+    return CB_OK;
+}
+
+int cb_mech_query(const cb_mech* m, cb_mech_info* info) {
+    if (!m || !info) return fail(CB_ERR_INVALID, "null argument");
+    std::memset(info, 0, sizeof *info);
+    info->n_species = m->host.K;
+    info->n_active = m->host.A;
+    info->n_reactions = m->host.R;
+    info->transport_ready = m->host.transport_ready;
+    info->T0 = m->host.T0;
+    info->viscosity0 = m->host.mu0;
+    info->conductivity0 = m->host.lambda0;
+    info->rates_inputs = m->host.K + 3;
+    info->rates_outputs = m->host.A + 2;
+    info->transport_inputs = m->host.K + 1;
+    info->transport_outputs = m->host.K + 2;
+    info->device_table_bytes = m->host.rates_blob.size() + m->host.transport_blob.size();
+    return CB_OK;
+}
+
+int cb_transport_setup(cb_mech* m, double T0, double viscosity0, double conductivity0) {
+    if (!m) return fail(CB_ERR_INVALID, "null mechanism");
+    std::string err;
+    int rc = cbg::build_transport(m->host, T0, viscosity0, conductivity0, err);
+    if (rc) return fail(rc, err);
+    CB_CUDA(cudaSetDevice(m->device));
+    if (m->d_transport) { CB_CUDA(cudaDeviceSynchronize()); cudaFree(m->d_transport); m->d_transport = nullptr; }
+    CB_CUDA(cudaMalloc(&m->d_transport, m->host.transport_blob.size()));
+    CB_CUDA(cudaMemcpy(m->d_transport, m->host.transport_blob.data(), m->host.transport_blob.size(), cudaMemcpyHostToDevice));
+    return CB_OK;
+}
+
+int cb_transport_coefficients(const cb_mech* m, double* cond, double* visc, double* diff) {
+    if (!m) return fail(CB_ERR_INVALID, "null mechanism");
+    if (!m->host.transport_ready) return fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
+    if (cond) std::memcpy(cond, m->host.fit_cond.data(), m->host.fit_cond.size() * sizeof(double));
+    if (visc) std::memcpy(visc, m->host.fit_visc.data(), m->host.fit_visc.size() * sizeof(double));
+    if (diff) std::memcpy(diff, m->host.fit_diff.data(), m->host.fit_diff.size() * sizeof(double));
+    return CB_OK;
+}
+
+int cb_rates_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+                 void* stream) {
+    return call(m, Path::Rates, n, inputs, outputs, flags, stream);
+}
+
+int cb_reaction_rates_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+                          void* stream) {
+    return call(m, Path::ReactionRates, n, inputs, outputs, flags, stream);
+}
+
+int cb_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+                     void* stream) {
+    return call(m, Path::Transport, n, inputs, outputs, flags, stream);
+}
+
+int cb_rates_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* rates_out,
+                           double* const* transport_out, uint32_t flags, void* stream) {
+    (void)m; (void)n; (void)inputs; (void)rates_out; (void)transport_out; (void)flags; (void)stream;
+    return fail(CB_ERR_UNSUPPORTED, "the fused entry point is not built yet");
+}
+
+int cb_work_model(const cb_mech* m, cb_work* rates, cb_work* transport) {
+    if (!m) return fail(CB_ERR_INVALID, "null mechanism");
+    if (rates) to_work(m->host.rates_work, rates);
+    if (transport) to_work(m->host.transport_work, transport);
+    return CB_OK;
+}
+
+int cb_synchronize(cb_mech* m, void* stream) {
+    if (!m) return fail(CB_ERR_INVALID, "null mechanism");
+    CB_CUDA(cudaSetDevice(m->device));
+    CB_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    return check_status(m);
+}
+
+}  // extern "C"

@@ -1,0 +1,34 @@
+// Kernel arguments and launchers shared by the C ABI (capi.cu) and the kernels (kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cbg {
+
+constexpr int kBlock = 128;  // threads per block: one warp per SM sub-partition fills the FP64 pipe
+
+// One pointer per input / output array (struct of arrays), passed by value as a kernel parameter.
+template <int KMAX>
+struct RatesArgs {
+    const double* in[KMAX + 3];  // P/R, R/P, T, V, n_0 .. n_{K-2}
+    double* out[KMAX + 2];       // dT/dt, dV/dt, wdot_0 .. wdot_{A-1}
+    uint32_t flags;              // bit 1: P/R and R/P are single values
+};
+
+template <int KMAX>
+struct TransportArgs {
+    const double* in[KMAX + 1];  // sum n, T/T0, n_0 .. n_{K-2}
+    double* out[KMAX + 2];       // lambda/lambda0, mu/mu0, rhoD_k/mu0
+    uint32_t flags;
+};
+
+// Smallest compiled capacity holding K species (0 if none).
+inline int kmax_for(int K) { return K <= 16 ? 16 : K <= 64 ? 64 : K <= 256 ? 256 : 0; }
+
+int max_table_smem();
+cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                         cudaStream_t st, int* status);
+cudaError_t launch_transport(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                             cudaStream_t st, int* status);
+
+}  // namespace cbg

@@ -1,0 +1,151 @@
+/* combustion_gb300: GB300 (sm_103a) per-cell chemistry kernels behind a C ABI.
+ *
+ * Drop-in for the per-cell path of Matthias-Fauconneau/combustion: the reference builds one
+ * straight-line program per mechanism (reaction::rates, reaction.rs:356-391; reaction::reactions_rates,
+ * reaction.rs:329-354; transport::properties, transport.rs:179-214) and runs it once per cell through
+ * device::assemble (device.rs:25-49 on the CPU, device.rs:59-96 on a GPU), whose call takes uniform
+ * constants plus one struct-of-arrays slice per input and returns one array per output. Here a
+ * mechanism handle holds the same mechanism as tables on the GPU, and each cb_*_f64 call is that
+ * assembled function's call: same inputs, same outputs, same order.
+ *
+ * Conventions
+ *  - Every function returns CB_OK (0) or a CB_ERR_* code; cb_last_error() describes the last failure
+ *    of the calling thread. Nothing aborts, traps or prints.
+ *  - Arrays are caller-owned. Pointer arrays (inputs/outputs) are read on the host during the call.
+ *  - Device-memory calls are asynchronous on the given CUDA stream (cudaStream_t passed as void*,
+ *    NULL = legacy default stream). With CB_HOST_MEMORY the call copies host arrays through
+ *    library-owned device buffers and returns when the outputs are on the host.
+ *  - A mechanism handle may be used from one host thread at a time.
+ */
+#ifndef COMBUSTION_GB300_H
+#define COMBUSTION_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum cb_status {
+    CB_OK = 0,
+    CB_ERR_INVALID = 1,    /* null pointer, bad size or flag */
+    CB_ERR_MECHANISM = 2,  /* mechanism rejected (the reference's loader or builder would panic) */
+    CB_ERR_CUDA = 3,       /* CUDA runtime error */
+    CB_ERR_NOT_READY = 4,  /* transport requested before cb_transport_setup */
+    CB_ERR_UNSUPPORTED = 5,/* feature outside this build (e.g. SRI falloff, more species than supported) */
+    CB_ERR_DEVICE = 6      /* a kernel reported a failure (e.g. a bounded wait ran out) */
+};
+
+/* Reaction models (lib.rs:238-245). */
+enum cb_reaction_model {
+    CB_ELEMENTARY = 0, CB_IRREVERSIBLE = 1, CB_THREE_BODY = 2, CB_LINDEMANN = 3, CB_TROE = 4, CB_SRI = 5
+};
+/* Species geometry (model.rs:15-19). */
+enum cb_geometry { CB_ATOM = 0, CB_LINEAR = 1, CB_NONLINEAR = 2 };
+
+/* Call flags. */
+#define CB_HOST_MEMORY 1u       /* inputs/outputs are host arrays (copied through device buffers) */
+#define CB_UNIFORM_PRESSURE 2u  /* rates: inputs[0] (P/R) and inputs[1] (R/P) each point to ONE value,
+                                   the reference's uniform "constants" (device.rs:31-32) */
+
+/* A mechanism in SI units, species ordered active first and the inert bulk species last: the output
+ * of the reference's loader (yaml.rs:54-171) and of combustion::new (lib.rs:127-140).
+ * Row-major arrays: nasa7 [K][2][7] (piece 0 for T <= split), reactants/products/efficiencies [R][K],
+ * rate and k0 [R][3] = (A [SI], temperature exponent b, activation temperature Ea/R [K]),
+ * troe [R][4] = (A, T3, T1, T2; T2 = +inf when absent), sri [R][5] (may be NULL without SRI).
+ * Transport: diameter [m], well_depth [J], polarizability [m^3], dipole [C.m] (lib.rs:40-59). */
+typedef struct cb_mech_desc {
+    int32_t n_species;
+    int32_t n_reactions;
+    const double* molar_mass;            /* [K] kg/mol */
+    const double* nasa7_split;           /* [K] K; NaN: one piece */
+    const double* nasa7;                 /* [K][2][7] */
+    const int32_t* geometry;             /* [K] cb_geometry */
+    const double* diameter;              /* [K] */
+    const double* well_depth;            /* [K] */
+    const double* polarizability;        /* [K] */
+    const double* dipole;                /* [K] */
+    const double* rotational_relaxation; /* [K] */
+    const uint8_t* reactants;            /* [R][K] */
+    const uint8_t* products;             /* [R][K] */
+    const int32_t* model;                /* [R] cb_reaction_model */
+    const double* rate;                  /* [R][3] */
+    const double* k0;                    /* [R][3] (falloff models; may be NULL otherwise) */
+    const double* troe;                  /* [R][4] (may be NULL without Troe reactions) */
+    const double* sri;                   /* [R][5] (may be NULL) */
+    const double* efficiencies;          /* [R][K] (may be NULL: all 1) */
+} cb_mech_desc;
+
+typedef struct cb_mech cb_mech;
+
+typedef struct cb_mech_info {
+    int32_t n_species;        /* K */
+    int32_t n_active;         /* A: species whose amount some reaction changes (lib.rs:130-135) */
+    int32_t n_reactions;      /* R */
+    int32_t transport_ready;  /* cb_transport_setup done */
+    double T0, viscosity0, conductivity0; /* transport normalisation (transport.rs:180-182) */
+    int32_t rates_inputs;     /* K+3 */
+    int32_t rates_outputs;    /* A+2 */
+    int32_t transport_inputs; /* K+1 */
+    int32_t transport_outputs;/* K+2 */
+    size_t device_table_bytes;
+} cb_mech_info;
+
+/* Algorithmic work per cell (the roofline numerator): FP64 flops counted with FMA = 2, plus the number
+ * of exp, log, division/reciprocal and sqrt evaluations, and DRAM bytes in/out (per-cell pressure). */
+typedef struct cb_work {
+    double flops;
+    double exps, logs, divs, sqrts;
+    double bytes_in, bytes_out;
+} cb_work;
+
+/* Replaces combustion::new (lib.rs:127-140) plus the table-building half of reaction::rates
+ * (reaction.rs:356-391): validates the mechanism exactly as the reference's builder would (active
+ * species prefix, net order, unimplemented SRI) and uploads its tables to the current CUDA device. */
+int cb_mech_create(const cb_mech_desc* desc, cb_mech** out);
+/* Host only, no device needed: the validation of cb_mech_create (combustion::new, lib.rs:127-140),
+ * filling info (species, active species, reactions, table size) without uploading anything. */
+int cb_mech_validate(const cb_mech_desc* desc, cb_mech_info* info);
+int cb_mech_destroy(cb_mech* mech);
+int cb_mech_query(const cb_mech* mech, cb_mech_info* info);
+
+/* Replaces transport::properties::<5> (transport.rs:212-214): fits the 50-point collision-integral
+ * species properties (transport.rs:119-138) and uploads the scaled polynomials (transport.rs:180-182)
+ * for a normalisation (T0, viscosity0, conductivity0) chosen by the caller (cantera.rs:60-76). */
+int cb_transport_setup(cb_mech* mech, double T0, double viscosity0, double conductivity0);
+/* Host only: the fits of transport::Polynomials::new (transport.rs:125-136) for temperature
+ * normalisation T0, without a device: cond [K][5], visc [K][5], diff [K*K][5] (any may be NULL). */
+int cb_transport_fit(const cb_mech_desc* desc, double T0, double* cond, double* visc, double* diff);
+/* Raw fitted coefficients (before the transport.rs:180-182 scaling): cond [K][5], visc [K][5],
+ * diff [K*K][5] (every ordered pair; only j < k is used). Any pointer may be NULL. */
+int cb_transport_coefficients(const cb_mech* mech, double* cond, double* visc, double* diff);
+
+/* Replaces device::assemble(reaction::rates(...)) called as f(constants, inputs) (device.rs:30-47).
+ * inputs  [K+3]: P/R, R/P, T [K], V [m^3], n_0 .. n_{K-2} [mol] (n arrays of length n)
+ * outputs [A+2]: dT/dt [K/s], dV/dt [m^3/s], wdot_0 .. wdot_{A-1} [mol/m^3/s] */
+int cb_rates_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* outputs,
+                 uint32_t flags, void* stream);
+/* Replaces reaction::reactions_rates (reaction.rs:329-354):
+ * inputs [K+2]: P/R, T, V, n_0 .. n_{K-2};  outputs [R]: rate of progress of each reaction. */
+int cb_reaction_rates_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* outputs,
+                          uint32_t flags, void* stream);
+/* Replaces device::assemble(transport::properties::<5>(...)) (transport.rs:179-214):
+ * inputs  [K+1]: sum of amounts n [mol], T/T0, n_0 .. n_{K-2}
+ * outputs [K+2]: lambda/lambda0, mu/mu0, rhoD_0/mu0 .. rhoD_{K-1}/mu0 */
+int cb_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* outputs,
+                     uint32_t flags, void* stream);
+/* Both on the same cells: rates inputs as cb_rates_f64, and transport evaluated at
+ * sum n = (P/R * V) / T and T/T0 (the ideal-gas total of the same cell). */
+int cb_rates_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* rates_out,
+                           double* const* transport_out, uint32_t flags, void* stream);
+
+int cb_work_model(const cb_mech* mech, cb_work* rates, cb_work* transport);
+
+/* Blocks until the mechanism's work on `stream` is done and reports any kernel-side failure. */
+int cb_synchronize(cb_mech* mech, void* stream);
+const char* cb_last_error(void);
+const char* cb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

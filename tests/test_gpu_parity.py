@@ -1,0 +1,168 @@
+"""GPU parity of the plain FP64 path against the FP64 oracle, through the C ABI.
+
+Plain FP64 must match the oracle to a relative error of 1e-12 per output (util.PLAIN_TOL), measured
+against each output's condition scale. Every case runs the same seeded cells through the GPU and through
+the oracle on the host cores.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import util
+from mechanisms import branch_mechanism, cells_for
+
+pytestmark = pytest.mark.gpu
+NTHREADS = os.cpu_count() or 4
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _mech(m):
+    import combustion_gb300 as cb
+    mech = cb.Mechanism(m)
+    from combustion_gb300 import synthetic
+    mech.transport_setup(*synthetic.transport_scales(m))
+    return mech
+
+
+def _oracle_for(m, mech):
+    import oracle
+    from combustion_gb300 import synthetic
+    o = oracle.Oracle(m)
+    o.set_transport(*synthetic.transport_scales(m), *mech.transport_coefficients())
+    return o
+
+
+def _dev(rows):
+    torch = _torch()
+    return torch.tensor(np.array(rows), dtype=torch.float64, device="cuda")
+
+
+def _run_rates(mech, o, cells):
+    torch = _torch()
+    ins = o.rates_inputs(cells)
+    out = torch.empty((mech.A + 2, cells.n), dtype=torch.float64, device="cuda")
+    mech.rates(_dev(ins), out)
+    torch.cuda.synchronize()
+    mech.synchronize()
+    ref, scale = o.rates(ins, nthreads=NTHREADS, scale=True)
+    return out.cpu().numpy(), ref, scale
+
+
+def _run_transport(mech, o, cells):
+    torch = _torch()
+    ins = o.transport_inputs(cells)
+    out = torch.empty((mech.K + 2, cells.n), dtype=torch.float64, device="cuda")
+    mech.transport(_dev(ins), out)
+    torch.cuda.synchronize()
+    mech.synchronize()
+    ref, scale = o.transport(ins, nthreads=NTHREADS, scale=True)
+    return out.cpu().numpy(), ref, scale
+
+
+def _report(name, x, ref, scale):
+    ce = util.cond_err(x, ref, scale)
+    re = util.rel_err(x, ref)
+    print(f"{name}: max cond err {ce.max():.3e}, median rel err {np.median(re):.3e}, "
+          f"99.9% rel err {np.quantile(re, 0.999):.3e}, finite {np.isfinite(x).all()}")
+    return ce
+
+
+@pytest.mark.parametrize("config,n", [("k10", 65536), ("k53", 8192)])
+def test_rates_parity(config, n):
+    from combustion_gb300 import synthetic
+    m = util.mechanism(config)
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, n, config)
+    x, ref, scale = _run_rates(mech, o, cells)
+    ce = _report(f"rates {config}", x, ref, scale)
+    assert np.isfinite(x).all()
+    assert ce.max() <= util.PLAIN_TOL
+
+
+@pytest.mark.parametrize("config,n", [("k10", 65536), ("k53", 8192)])
+def test_transport_parity(config, n):
+    from combustion_gb300 import synthetic
+    m = util.mechanism(config)
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, n, config)
+    x, ref, scale = _run_transport(mech, o, cells)
+    ce = _report(f"transport {config}", x, ref, scale)
+    assert np.isfinite(x).all()
+    assert ce.max() <= util.PLAIN_TOL
+
+
+def test_branch_mechanism_parity():
+    m = branch_mechanism()
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = cells_for(m, 4096)
+    x, ref, scale = _run_rates(mech, o, cells)
+    assert _report("rates branches", x, ref, scale).max() <= util.PLAIN_TOL
+    x, ref, scale = _run_transport(mech, o, cells)
+    assert _report("transport branches", x, ref, scale).max() <= util.PLAIN_TOL
+
+
+@pytest.mark.parametrize("n", [0, 1, 31, 127, 129, 1000])
+def test_ragged_sizes(n):
+    from combustion_gb300 import synthetic
+    torch = _torch()
+    m = util.mechanism("k10")
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, max(n, 1), "k10", offset=12345)
+    ins = [a[:n] for a in o.rates_inputs(cells)]
+    guard = 4
+    out = torch.full((mech.A + 2, n + guard), 7.0, dtype=torch.float64, device="cuda")
+    mech.rates(_dev(ins) if n else [torch.empty(0, dtype=torch.float64, device="cuda")] * (m.K + 3),
+               [out[q, :n] for q in range(mech.A + 2)] if n else [out[q, :0] for q in range(mech.A + 2)])
+    torch.cuda.synchronize()
+    mech.synchronize()
+    res = out.cpu().numpy()
+    assert (res[:, n:] == 7.0).all(), "kernel wrote past the end of its outputs"
+    if n:
+        ref, scale = o.rates(ins, scale=True)
+        assert util.cond_err(res[:, :n], ref, scale).max() <= util.PLAIN_TOL
+
+
+def test_host_memory_path_and_uniform_pressure():
+    """CB_HOST_MEMORY with more cells than one staging chunk, and the uniform-pressure constants."""
+    from combustion_gb300 import synthetic
+    m = util.mechanism("k10")
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    n = (1 << 20) + 4321
+    cells = synthetic.generate_cells(m.K, n, "k10")  # fixed 1 atm: P/R is uniform
+    ins = o.rates_inputs(cells)
+    out = np.zeros((mech.A + 2, n))
+    mech.rates(np.array(ins), out)
+    ref, scale = o.rates(ins, nthreads=NTHREADS, scale=True)
+    assert util.cond_err(out, ref, scale).max() <= util.PLAIN_TOL
+    uni = [np.array([ins[0][0]]), np.array([ins[1][0]])] + [np.ascontiguousarray(a) for a in ins[2:]]
+    assert (ins[0] == ins[0][0]).all()
+    out2 = np.zeros_like(out)
+    mech.rates(uni, list(out2), uniform_pressure=True)
+    assert np.array_equal(out2, out)
+    tin = o.transport_inputs(cells)
+    tout = np.zeros((mech.K + 2, n))
+    mech.transport(np.array(tin), tout)
+    tref, tscale = o.transport(tin, nthreads=NTHREADS, scale=True)
+    assert util.cond_err(tout, tref, tscale).max() <= util.PLAIN_TOL
+
+
+def test_errors_are_reported_not_raised_on_device():
+    import combustion_gb300 as cb
+    m = util.mechanism("k10")
+    mech = cb.Mechanism(m)
+    torch = _torch()
+    ins = torch.zeros((m.K + 1, 4), dtype=torch.float64, device="cuda")
+    out = torch.zeros((m.K + 2, 4), dtype=torch.float64, device="cuda")
+    with pytest.raises(cb.CombustionError) as e:
+        mech.transport(ins, out)
+    assert e.value.code == cb.CB_ERR_NOT_READY
