@@ -1,0 +1,319 @@
+"""Benchmark: cells/s of species rates + mixture-averaged transport, 53-species mechanism, 2^22 cells.
+
+One step = one pass of the hot path (rates then transport, plain FP64) over the 2^22-cell batch.
+  value : inputs resident in HBM, device-timed with CUDA events on the launching stream (max over ranks)
+  e2e   : the public fused call cb_rates_transport_f64 on pinned HOST buffers; host->device copies of the
+          inputs and device->host copies of all outputs are inside the timed region
+  --impl reference : the CPU FP64 restatement of the reference's path (oracle/, the reference's own
+          Rust code cannot be built here) on all host cores, on bounded samples of the same workload
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--cells N]
+Multi-GPU (torchrun): every rank runs its own 2^22 cells (weak scaling, replicas, no collective on the
+data path); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cells/s rates+transport (53 sp) plain FP64 vs mixed/surrogate at stated error"
+CONFIG = "k53"
+WORKLOAD = ("rates+transport, synthetic K=53 species / R=325 reactions (250 reversible, 45 three-body, "
+            "30 Troe), 2^22 cells, T~U[300,3000] K, P log-uniform [0.1,40] atm, X~Dirichlet(0.3)")
+# Ideal FP64-pipe cost (FMA slots) of one evaluation in a table-driven implementation, used to convert
+# the algorithmic exp/log/div/sqrt counts into flops (FMA = 2 flops): exp 10, log 12, div 4, sqrt 4.
+SLOT_COST = {"exps": 10.0, "logs": 12.0, "divs": 4.0, "sqrts": 4.0}
+
+
+def algorithmic_flops(work: dict) -> float:
+    return work["flops"] + 2.0 * sum(SLOT_COST[k] * work[k] for k in SLOT_COST)
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(backend: str):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def run_reference(args):
+    """The reference arm: the CPU FP64 path on all host cores (rank 0 only)."""
+    world, rank, _ = dist_setup("gloo")
+    if rank != 0:
+        return
+    import oracle
+    from combustion_gb300 import synthetic
+    import combustion_gb300 as cb
+    m = synthetic.generate_mechanism(CONFIG)
+    scales = synthetic.transport_scales(m)
+    o = oracle.Oracle(m)
+    o.set_transport(*scales, *cb.transport_fit(m, scales[0]))
+    threads = os.cpu_count() or 1
+    n = args.ref_cells
+    rates = []
+    for step in range(args.warmup + args.steps):
+        cells = synthetic.generate_cells_parallel(m.K, n, CONFIG, seed=1, workers=threads)
+        ins = o.rates_inputs(cells)
+        t = time.perf_counter()
+        o.fused(ins, nthreads=threads)
+        dt = time.perf_counter() - t
+        if step >= args.warmup:
+            rates.append(n / dt)
+    value = float(np.median(rates))
+    sample = f"{n} cells of the same seeded workload per step, {args.steps} steps, median"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells_per_step": n, "form": "plain_f64",
+                   "implementation": "oracle/oracle.c: C restatement of the reference interpreter (Rust not buildable here)"},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args):
+    world, rank, local = dist_setup("nccl")
+    from combustion_gb300 import synthetic
+    m = synthetic.generate_mechanism(CONFIG)
+    scales = synthetic.transport_scales(m)
+    n = args.cells
+    threads = os.cpu_count() or 1
+    # Seeded cells, generated before any CUDA call; rank r draws its own window of the cell sequence.
+    import torch
+    K = m.K
+    pin = torch.empty((K + 3, n), dtype=torch.float64).pin_memory()
+    host_in = pin.numpy()
+    cells = synthetic.generate_cells_parallel(K, n, CONFIG, seed=1 + rank, workers=threads,
+                                              out_amounts=host_in[4:])
+    host_in[0], host_in[1], host_in[2], host_in[3] = cells.pressure_R, 1.0 / cells.pressure_R, cells.temperature, cells.volume
+
+    torch.cuda.set_device(local)
+    import combustion_gb300 as cb
+    mech = cb.Mechanism(m)
+    mech.transport_setup(*scales)
+    A = mech.A
+    stream = torch.cuda.current_stream()
+    d_in = torch.empty((K + 3, n), dtype=torch.float64, device="cuda")
+    d_in.copy_(pin)
+    # Transport inputs (sum n, T/T0) as two extra rows; the amounts rows are shared with the rates inputs.
+    d_tn = torch.empty((2, n), dtype=torch.float64, device="cuda")
+    d_tn[0] = (d_in[0] * d_in[3]) / d_in[2]
+    d_tn[1] = d_in[2] / scales[0]
+    t_in = [d_tn[0], d_tn[1]] + [d_in[4 + k] for k in range(K - 1)]
+    r_out = torch.empty((A + 2, n), dtype=torch.float64, device="cuda")
+    t_out = torch.empty((K + 2, n), dtype=torch.float64, device="cuda")
+
+    def step(ev=None):
+        mech.rates(d_in, r_out)
+        if ev is not None:
+            ev.record(stream)
+        mech.transport(t_in, t_out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    mech.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_mid = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        for s in range(args.steps):
+            ev_start[s].record(stream)
+            step(ev_mid[s])
+            ev_end[s].record(stream)
+        torch.cuda.synchronize()
+    mech.synchronize()
+    rates_ms = [a.elapsed_time(b) for a, b in zip(ev_start, ev_mid)]
+    transport_ms = [a.elapsed_time(b) for a, b in zip(ev_mid, ev_end)]
+    total_ms = ev_start[0].elapsed_time(ev_end[-1])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step * 1e-3)
+
+    # Roofline of the dominant kernel (FP64 pipe bound): algorithmic flops per launch / mean duration.
+    work_r, work_t = mech.work_model()
+    peak = 2.0 * cb.device_fp64_peak() / 1e12
+    kern = {"rates_f64": (float(np.mean(rates_ms)), work_r), "transport_f64": (float(np.mean(transport_ms)), work_t)}
+    dom = max(kern, key=lambda k: kern[k][0])
+    ms, work = kern[dom]
+    achieved = algorithmic_flops(work) * n / (ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        per_cell = json.load(open(tpath)).get(dom, {}).get("dram_bytes_per_cell")
+        traffic = per_cell * n if per_cell else None
+
+    # Parity of this run's outputs on a sample of cells against the FP64 oracle.
+    parity = None
+    if rank == 0 and not args.no_parity:
+        import oracle
+        o = oracle.Oracle(m)
+        o.set_transport(*scales, *mech.transport_coefficients())
+        idx = np.linspace(0, n - 1, 2048).astype(np.int64)
+        ins = [np.ascontiguousarray(host_in[q, idx]) for q in range(K + 3)]
+        rref, rsc = o.rates(ins, nthreads=threads, scale=True)
+        tin = [(ins[0] * ins[3]) / ins[2], ins[2] / scales[0]] + ins[4:]
+        tref, tsc = o.transport(tin, nthreads=threads, scale=True)
+        ridx = torch.from_numpy(idx).cuda()
+        gr = r_out.index_select(1, ridx).cpu().numpy()
+        gt = t_out.index_select(1, ridx).cpu().numpy()
+        parity = {"cells_checked": int(len(idx)),
+                  "rates_max_err": float((np.abs(gr - rref) / np.maximum(rsc, 1e-300)).max()),
+                  "transport_max_err": float((np.abs(gt - tref) / np.maximum(tsc, 1e-300)).max()),
+                  "tolerance": 1e-12, "metric": "|gpu - oracle| / condition scale of the output"}
+
+    # End to end through the public fused call with host buffers.
+    h_ro = torch.empty((A + 2, n), dtype=torch.float64).pin_memory().numpy()
+    h_to = torch.empty((K + 2, n), dtype=torch.float64).pin_memory().numpy()
+    mech.rates_transport(host_in, h_ro, h_to)  # warm-up (staging buffers)
+    e2e_steps = max(1, min(args.steps, 3))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        mech.rates_transport(host_in, h_ro, h_to)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    # CPU baseline: the oracle (port of the reference's FP64 path) on a bounded sample, all host cores.
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        o = oracle.Oracle(m)
+        o.set_transport(*scales, *mech.transport_coefficients())
+        ns = args.ref_cells
+        ins = [np.ascontiguousarray(host_in[q, :ns]) for q in range(K + 3)]
+        o.fused([a[:1024] for a in ins], nthreads=threads)
+        t = time.perf_counter()
+        o.fused(ins, nthreads=threads)
+        cpu = {"value": ns / (time.perf_counter() - t), "unit": "cells/s", "cores": threads, "kind": "port",
+               "sample": f"first {ns} cells of the benchmark batch, fused rates+transport, {threads} threads"}
+
+    if rank == 0:
+        clk = clocks.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, no public dataset)",
+            "config": {"workload": WORKLOAD, "cells": n, "species": K, "reactions": mech.R, "form": "plain_f64",
+                       "pressure": "per cell", "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (%.1f GB per step), no flush needed" % ((K + 3 + A + 2 + K + 2) * 8 * n / 1e9)},
+            "kernels_ms": {"rates_f64": float(np.mean(rates_ms)), "transport_f64": float(np.mean(transport_ms))},
+            "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "measured FP64 FMA rate of this GPU (cb_device_fp64_peak), FMA = 2 flops",
+                         "flops_per_cell": algorithmic_flops(work),
+                         "flop_model": "reference program ops (+-x min max = 1) plus exp/log/div/sqrt at "
+                                       "2 x {10,12,4,4} FMA slots"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": (K + 3) * 8 * n,
+                    "d2h_bytes_per_step": (A + 2 + K + 2) * 8 * n, "api": "cb_rates_transport_f64, CB_HOST_MEMORY"},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk,
+            "parity": parity,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=1 << 22)
+    ap.add_argument("--ref-cells", type=int, default=1 << 18)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ CB_UNIFORM_PRESSURE = 2
 EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_query", "cb_transport_setup",
            "cb_transport_fit", "cb_transport_coefficients", "cb_rates_f64", "cb_reaction_rates_f64",
            "cb_transport_f64", "cb_rates_transport_f64", "cb_work_model", "cb_synchronize", "cb_last_error",
-           "cb_version"]
+           "cb_version", "cb_device_fp64_peak"]
 
 
 class CombustionError(RuntimeError):
@@ -90,6 +90,7 @@ def lib():
         L.cb_synchronize.argtypes = [vp, vp]
         L.cb_last_error.restype = C.c_char_p
         L.cb_version.restype = C.c_char_p
+        L.cb_device_fp64_peak.argtypes = [C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -256,6 +257,13 @@ class Mechanism:
         _check(lib().cb_rates_transport_f64(self.h, n, _ptr_array(ins), _ptr_array(ro), _ptr_array(to), flags,
                                             None if flags else self._stream(stream)))
         return rates_out, transport_out
+
+
+def device_fp64_peak() -> float:
+    """FP64 FMAs per second of the current GPU (measured)."""
+    v = C.c_double()
+    _check(lib().cb_device_fp64_peak(C.byref(v)))
+    return v.value
 
 
 def version() -> str:

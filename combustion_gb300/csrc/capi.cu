@@ -21,7 +21,6 @@ struct cb_mech {
     double* d_stage = nullptr;
     size_t stage_doubles = 0;
     cudaStream_t copy_stream[2] = {nullptr, nullptr};
-    cudaEvent_t slot_free[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -51,68 +50,84 @@ int check_status(cb_mech* m) {
     return CB_OK;
 }
 
-enum class Path { Rates, ReactionRates, Transport };
+enum class Path { Rates, ReactionRates, Transport, Fused };
 
-// Arguments of one launch: pointer arrays already resolved to device memory.
+template <template <int> class Args, int KM>
+int fill_and_launch(cb_mech* m, size_t n, const double* const* in, int ni, double* const* out, int no,
+                    uint32_t flags, cudaStream_t st,
+                    cudaError_t (*launch)(int, const uint8_t*, uint32_t, const void*, size_t, cudaStream_t, int*),
+                    const uint8_t* tab, size_t tab_bytes, const char* what) {
+    Args<KM> a;
+    std::memset(&a, 0, sizeof a);
+    for (int q = 0; q < ni; q++) a.in[q] = in[q];
+    for (int q = 0; q < no; q++) a.out[q] = out[q];
+    a.flags = flags;
+    cudaError_t e = launch(KM, tab, (uint32_t)tab_bytes, &a, n, st, m->d_status);
+    return e == cudaSuccess ? CB_OK : cuda_fail(e, what);
+}
+
+template <template <int> class Args>
+int dispatch(cb_mech* m, size_t n, const double* const* in, int ni, double* const* out, int no, uint32_t flags,
+             cudaStream_t st,
+             cudaError_t (*launch)(int, const uint8_t*, uint32_t, const void*, size_t, cudaStream_t, int*),
+             const uint8_t* tab, size_t tab_bytes, const char* what) {
+    switch (m->kmax) {
+    case 16: return fill_and_launch<Args, 16>(m, n, in, ni, out, no, flags, st, launch, tab, tab_bytes, what);
+    case 64: return fill_and_launch<Args, 64>(m, n, in, ni, out, no, flags, st, launch, tab, tab_bytes, what);
+    case 256: return fill_and_launch<Args, 256>(m, n, in, ni, out, no, flags, st, launch, tab, tab_bytes, what);
+    default: return fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
+    }
+}
+
+// One call on device pointers (pointer arrays already resolved).
 int launch_path(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags,
                 cudaStream_t st) {
-    const int K = m->host.K, A = m->host.A;
+    const int K = m->host.K, A = m->host.A, R = m->host.R;
     if (n == 0) return CB_OK;
-    if (path == Path::Rates) {
-        cudaError_t e;
-        switch (m->kmax) {
-#define CB_RATES(KM)                                                                 \
-    case KM: {                                                                       \
-        cbg::RatesArgs<KM> a;                                                        \
-        std::memset(&a, 0, sizeof a);                                                \
-        for (int q = 0; q < K + 3; q++) a.in[q] = in[q];                             \
-        for (int q = 0; q < A + 2; q++) a.out[q] = out[q];                           \
-        a.flags = flags;                                                             \
-        e = cbg::launch_rates(KM, m->d_rates, (uint32_t)m->host.rates_blob.size(), &a, n, st, m->d_status); \
-        break;                                                                       \
+    const size_t rb = m->host.rates_blob.size(), tb = m->host.transport_blob.size();
+    switch (path) {
+    case Path::Rates:
+        return dispatch<cbg::RatesArgs>(m, n, in, K + 3, out, A + 2, flags, st, cbg::launch_rates, m->d_rates, rb,
+                                        "rates kernel");
+    case Path::ReactionRates:
+        if (R > cbg::kMaxReactions) return fail(CB_ERR_UNSUPPORTED, "more reactions than per-reaction outputs support");
+        return dispatch<cbg::ReactionRatesArgs>(m, n, in, K + 2, out, R, flags, st, cbg::launch_reaction_rates,
+                                                m->d_rates, rb, "reaction rates kernel");
+    case Path::Transport:
+        return dispatch<cbg::TransportArgs>(m, n, in, K + 1, out, K + 2, flags, st, cbg::launch_transport,
+                                            m->d_transport, tb, "transport kernel");
+    case Path::Fused: {
+        int rc = dispatch<cbg::RatesArgs>(m, n, in, K + 3, out, A + 2, flags, st, cbg::launch_rates, m->d_rates, rb,
+                                          "rates kernel");
+        if (rc) return rc;
+        return dispatch<cbg::TransportArgs>(m, n, in, K + 3, out + (A + 2), K + 2, flags | cbg::kFromRates, st,
+                                            cbg::launch_transport, m->d_transport, tb, "transport kernel");
     }
-            CB_RATES(16) CB_RATES(64) CB_RATES(256)
-#undef CB_RATES
-        default: return fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
-        }
-        if (e != cudaSuccess) return cuda_fail(e, "rates kernel launch");
-        return CB_OK;
     }
-    if (path == Path::Transport) {
-        cudaError_t e;
-        switch (m->kmax) {
-#define CB_TRANSPORT(KM)                                                             \
-    case KM: {                                                                       \
-        cbg::TransportArgs<KM> a;                                                    \
-        std::memset(&a, 0, sizeof a);                                                \
-        for (int q = 0; q < K + 1; q++) a.in[q] = in[q];                             \
-        for (int q = 0; q < K + 2; q++) a.out[q] = out[q];                           \
-        a.flags = flags;                                                             \
-        e = cbg::launch_transport(KM, m->d_transport, (uint32_t)m->host.transport_blob.size(), &a, n, st, m->d_status); \
-        break;                                                                       \
-    }
-            CB_TRANSPORT(16) CB_TRANSPORT(64) CB_TRANSPORT(256)
-#undef CB_TRANSPORT
-        default: return fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
-        }
-        if (e != cudaSuccess) return cuda_fail(e, "transport kernel launch");
-        return CB_OK;
-    }
-    return fail(CB_ERR_UNSUPPORTED, "per-reaction rates are not built yet");
+    return fail(CB_ERR_INVALID, "unknown path");
 }
 
 int n_inputs(const cb_mech* m, Path p) {
-    return p == Path::Rates ? m->host.K + 3 : p == Path::ReactionRates ? m->host.K + 2 : m->host.K + 1;
+    switch (p) {
+    case Path::Rates: case Path::Fused: return m->host.K + 3;
+    case Path::ReactionRates: return m->host.K + 2;
+    default: return m->host.K + 1;
+    }
 }
 int n_outputs(const cb_mech* m, Path p) {
-    return p == Path::Rates ? m->host.A + 2 : p == Path::ReactionRates ? m->host.R : m->host.K + 2;
+    switch (p) {
+    case Path::Rates: return m->host.A + 2;
+    case Path::ReactionRates: return m->host.R;
+    case Path::Fused: return m->host.A + 2 + m->host.K + 2;
+    default: return m->host.K + 2;
+    }
 }
 
 // Host arrays: copy chunks through two device staging slots so that the copies of one chunk overlap
 // the kernel of the other (one cudaMemcpyAsync per array per chunk).
 int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags) {
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
-    const bool uniform = path == Path::Rates && (flags & CB_UNIFORM_PRESSURE);
+    const bool uniform = (path == Path::Rates || path == Path::Fused) && (flags & CB_UNIFORM_PRESSURE);
     size_t chunk = (size_t)1 << 20;
     if (chunk > n) chunk = n;
     const size_t per_slot = (size_t)(ni + no) * chunk + 2;
@@ -125,7 +140,6 @@ int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* 
     }
     for (int s = 0; s < 2; s++) {
         if (!m->copy_stream[s]) CB_CUDA(cudaStreamCreateWithFlags(&m->copy_stream[s], cudaStreamNonBlocking));
-        if (!m->slot_free[s]) CB_CUDA(cudaEventCreateWithFlags(&m->slot_free[s], cudaEventDisableTiming));
     }
     std::vector<const double*> din(ni);
     std::vector<double*> dout(no);
@@ -158,8 +172,10 @@ int call(cb_mech* m, Path path, size_t n, const double* const* inputs, double* c
          void* stream) {
     if (!m || !inputs || !outputs) return fail(CB_ERR_INVALID, "null argument");
     if (flags & ~(CB_HOST_MEMORY | CB_UNIFORM_PRESSURE)) return fail(CB_ERR_INVALID, "unknown flag");
-    if ((flags & CB_UNIFORM_PRESSURE) && path != Path::Rates) return fail(CB_ERR_INVALID, "CB_UNIFORM_PRESSURE applies to rates only");
-    if (path == Path::Transport && !m->host.transport_ready) return fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
+    if ((flags & CB_UNIFORM_PRESSURE) && path != Path::Rates && path != Path::Fused)
+        return fail(CB_ERR_INVALID, "CB_UNIFORM_PRESSURE applies to the rates inputs only");
+    if ((path == Path::Transport || path == Path::Fused) && !m->host.transport_ready)
+        return fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
     if (n == 0) return CB_OK;
     for (int q = 0; q < ni; q++) if (!inputs[q]) return fail(CB_ERR_INVALID, "null input array");
@@ -234,7 +250,6 @@ int cb_mech_destroy(cb_mech* m) {
     cudaSetDevice(m->device);
     for (int s = 0; s < 2; s++) {
         if (m->copy_stream[s]) { cudaStreamSynchronize(m->copy_stream[s]); cudaStreamDestroy(m->copy_stream[s]); }
-        if (m->slot_free[s]) cudaEventDestroy(m->slot_free[s]);
     }
     cudaFree(m->d_rates);
     cudaFree(m->d_transport);
@@ -300,8 +315,10 @@ int cb_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* 
 
 int cb_rates_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* rates_out,
                            double* const* transport_out, uint32_t flags, void* stream) {
-    (void)m; (void)n; (void)inputs; (void)rates_out; (void)transport_out; (void)flags; (void)stream;
-    return fail(CB_ERR_UNSUPPORTED, "the fused entry point is not built yet");
+    if (!m || !rates_out || !transport_out) return fail(CB_ERR_INVALID, "null argument");
+    std::vector<double*> outs(rates_out, rates_out + m->host.A + 2);
+    outs.insert(outs.end(), transport_out, transport_out + m->host.K + 2);
+    return call(m, Path::Fused, n, inputs, outs.data(), flags, stream);
 }
 
 int cb_work_model(const cb_mech* m, cb_work* rates, cb_work* transport) {

@@ -1,5 +1,5 @@
-// Plain FP64 kernels: species production rates (reaction.rs:207-391) and mixture-averaged transport
-// (transport.rs:141-210), one cell per thread.
+// Plain FP64 kernels: species production rates (reaction.rs:207-391), per-reaction rates of progress
+// (reaction.rs:329-354) and mixture-averaged transport (transport.rs:141-210), one cell per thread.
 //
 // Every thread of a warp walks the same reaction / species / pair at the same time, so each table read
 // is a broadcast; the per-cell working arrays (concentrations, Gibbs exponentials, accumulators) live in
@@ -14,8 +14,8 @@
 
 namespace cbg {
 
-constexpr double kF32Max = 3.4028234663852886e+38;       // f32::MAX as f64
-constexpr double kF32MinPos = 1.1754943508222875e-38;    // f32::MIN_POSITIVE as f64
+constexpr double kF32Max = 3.4028234663852886e+38;     // f32::MAX as f64
+constexpr double kF32MinPos = 1.1754943508222875e-38;  // f32::MIN_POSITIVE as f64
 
 struct Temps {
     double lnT, T, T2, T3, T4, rcpT, rcpT2;
@@ -49,153 +49,191 @@ __device__ __forceinline__ double arrhenius(const Arrhenius& a, const Temps& t) 
 // Piece 0 for T <= split (lib.rs:15); NaN splits (one piece) select piece 0 as well.
 __device__ __forceinline__ int piece_of(double split, double T) { return bits(T) <= bits(split) ? 0 : 1; }
 
+struct RatesTables {
+    const RatesHeader* H;
+    const Species* species;
+    const Reaction* reactions;
+    const Falloff* falloff;
+    const double* eff;
+    __device__ explicit RatesTables(const uint8_t* tab)
+        : H(reinterpret_cast<const RatesHeader*>(tab)),
+          species(reinterpret_cast<const Species*>(tab + H->off_species)),
+          reactions(reinterpret_cast<const Reaction*>(tab + H->off_reactions)),
+          falloff(reinterpret_cast<const Falloff*>(tab + H->off_falloff)),
+          eff(reinterpret_cast<const double*>(tab + H->off_eff)) {}
+};
+
 template <int KMAX>
-__device__ void rates_cell(const uint8_t* tab, const RatesArgs<KMAX>& io, size_t i) {
-    const RatesHeader& H = *reinterpret_cast<const RatesHeader*>(tab);
-    const Species* species = reinterpret_cast<const Species*>(tab + H.off_species);
-    const Reaction* reactions = reinterpret_cast<const Reaction*>(tab + H.off_reactions);
-    const Falloff* falloff = reinterpret_cast<const Falloff*>(tab + H.off_falloff);
-    const double* eff = reinterpret_cast<const double*>(tab + H.off_eff);
+struct Cell {
+    Temps t;
+    double Ctot, C0, rcpC0;
+    double C[KMAX];              // concentrations, bulk last
+    double ex[KMAX], exn[KMAX];  // min(M3, exp(g_k)), min(cbrt(f32::MAX), exp(-g_k))
+};
+
+// Prologue of reaction.rs:362-373 and the Gibbs exponentials of reaction.rs:234-263.
+template <int KMAX>
+__device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressure_R, double T, double V,
+                                           const double* const* amounts, size_t i, Cell<KMAX>& c) {
+    const RatesHeader& H = *tb.H;
     const int K = H.K, A = H.A;
-    const bool uniform = io.flags & 2u;
+    const double md = rcp64(V);
+    c.t.T = T;
+    c.t.rcpT = rcp64(T);
+    c.t.lnT = log64(T);
+    c.t.T2 = T * T;
+    c.t.T3 = T * c.t.T2;
+    c.t.T4 = c.t.T2 * c.t.T2;
+    c.t.rcpT2 = c.t.rcpT * c.t.rcpT;
+    double sum = 0.0;
+    for (int k = 0; k < K - 1; k++) {
+        c.C[k] = md * max0(amounts[k][i]);
+        sum += c.C[k];
+    }
+    c.Ctot = pressure_R * c.t.rcpT;
+    c.C[K - 1] = c.Ctot - sum;
+    c.C0 = H.C0 * c.t.rcpT;
+    c.rcpC0 = H.rcp_C0 * T;
+    for (int k = 0; k < A; k++) {
+        const Species& s = tb.species[k];
+        if (!(s.need_exp | s.need_exp_neg)) continue;
+        const double* g = s.g[piece_of(s.split, T)];
+        const double x = fma(g[6], c.t.rcpT, fma(g[5], c.t.T4, fma(g[4], c.t.T3, fma(g[3], c.t.T2,
+                         fma(g[2], T, fma(g[1], c.t.lnT, g[0]))))));
+        if (s.need_exp) c.ex[k] = min_pos(H.M3, exp64(x));
+        if (s.need_exp_neg) c.exn[k] = min_pos(H.cbrt_max, exp64(-x));
+    }
+}
+
+// cR of one reaction (reaction.rs:149-309): forward rate constant (with third-body efficiency and
+// falloff), rate of progress against the equilibrium constant, and their product.
+template <int KMAX>
+__device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const Cell<KMAX>& c) {
+    const RatesHeader& H = *tb.H;
+    const int K = H.K;
+    const Temps& t = c.t;
+    double M = c.Ctot;
+    if (x.eff_row >= 0) {  // efficiency() (reaction.rs:141-145)
+        const double* e = tb.eff + (size_t)x.eff_row * K;
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s = fma(e[k], c.C[k], s);
+        M = c.Ctot + s;
+    }
+    double num, den = 1.0;
+    bool ratio = false;
+    if (x.model == 4) {  // Troe (reaction.rs:160-193)
+        const Falloff& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius(f.k0, t);
+        double Pr, kinf;
+        if (f.flags & kKinfConst) {
+            Pr = M * k0;
+            kinf = f.ainf;
+        } else {
+            const double ki = arrhenius(x.k, t);
+            Pr = div64(M * k0, ki + kF32MinPos);
+            kinf = f.ainf * ki;
+        }
+        double lnF;
+        if (f.flags & kFcentConst) {
+            lnF = f.ln_fcent;
+        } else {
+            double F = 0.0;
+            if (f.flags & kTermT3) F = f.c1mA * exp64(t.T * f.c3);
+            if (f.flags & kTermT1) F += f.cA * exp64(t.T * f.c1);
+            if (f.flags & kTermAConst) F += f.cA;
+            if (f.flags & kTermT2) F += exp64(f.cmT2 * t.rcpT);
+            lnF = log64(F);
+        }
+        const double Cc = fma(-0.67, lnF, -H.ln10_04);
+        const double Nn = fma(-1.27, lnF, H.ln10_075);
+        const double lnPrC = log64(Pr + kF32MinPos) + Cc;
+        const double f1 = div64(lnPrC, fma(-0.14, lnPrC, Nn));
+        const double Fb = exp64(div64(lnF, fma(f1, f1, 1.0)));
+        num = (Fb * kinf) * Pr;
+        den = Pr + 1.0;
+        ratio = true;
+    } else if (x.model == 3) {  // Lindemann (reaction.rs:153-159)
+        const Falloff& f = tb.falloff[x.falloff];
+        const double Ck0 = M * arrhenius(f.k0, t);
+        const double ki = arrhenius(x.k, t);
+        num = Ck0 * ki;
+        den = (Ck0 + ki) + kF32MinPos;
+        ratio = true;
+    } else {
+        num = arrhenius(x.k, t);
+        if (x.model == 2) num *= M;  // three-body (reaction.rs:152)
+    }
+    // Rate of progress (reaction.rs:269-306).
+    double Rf = 1.0;
+    for (int q = 0; q < x.n_r; q++)
+        for (int n = 0; n < x.r_n[q]; n++) Rf *= c.C[x.r_k[q]];
+    double Rnet = Rf;
+    if (x.model != 1) {
+        double p = 1.0;
+        for (int q = 0; q < x.n_net; q++) {
+            const int nu = x.net_n[q], k = x.net_k[q];
+            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
+        }
+        switch (x.minus_sigma_net) {
+        case 1: p = c.C0 * p; break;
+        case -1: p = c.rcpC0 * p; break;
+        case -2: p = (c.rcpC0 * c.rcpC0) * p; break;
+        default: break;
+        }
+        double Rr = 1.0;
+        for (int q = 0; q < x.n_p; q++)
+            for (int n = 0; n < x.p_n[q]; n++) Rr *= c.C[x.p_k[q]];
+        Rnet = Rf - p * Rr;
+    }
+    return ratio ? div64(Rnet * num, den) : Rnet * num;
+}
+
+template <int KMAX>
+__device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, size_t i) {
+    const RatesHeader& H = *tb.H;
+    const int K = H.K, A = H.A;
+    const bool uniform = io.flags & kUniformPressure;
     const double pressure_R = uniform ? io.in[0][0] : io.in[0][i];
     const double rcp_pressure_R = uniform ? io.in[1][0] : io.in[1][i];
     const double T = io.in[2][i], V = io.in[3][i];
-
-    // Prologue (reaction.rs:362-373).
-    double C[KMAX];
-    Temps t;
-    const double md = rcp64(V);
-    t.T = T;
-    t.rcpT = rcp64(T);
-    t.lnT = log64(T);
-    t.T2 = T * T;
-    t.T3 = T * t.T2;
-    t.T4 = t.T2 * t.T2;
-    t.rcpT2 = t.rcpT * t.rcpT;
-    double sum = 0.0;
-    for (int k = 0; k < K - 1; k++) {
-        C[k] = md * max0(io.in[4 + k][i]);
-        sum += C[k];
-    }
-    const double Ctot = pressure_R * t.rcpT;
-    C[K - 1] = Ctot - sum;
-
-    // Gibbs exponentials of the active species (reaction.rs:234-263).
-    double ex[KMAX], exn[KMAX];
-    for (int k = 0; k < A; k++) {
-        const Species& s = species[k];
-        if (!(s.need_exp | s.need_exp_neg)) continue;
-        const double* g = s.g[piece_of(s.split, T)];
-        double x = fma(g[6], t.rcpT, fma(g[5], t.T4, fma(g[4], t.T3, fma(g[3], t.T2, fma(g[2], T, fma(g[1], t.lnT, g[0]))))));
-        if (s.need_exp) ex[k] = min_pos(H.M3, exp64(x));
-        if (s.need_exp_neg) exn[k] = min_pos(H.cbrt_max, exp64(-x));
-    }
-
+    Cell<KMAX> c;
+    cell_setup<KMAX>(tb, pressure_R, T, V, io.in + 4, i, c);
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
-    const double C0 = H.C0 * t.rcpT, rcpC0 = H.rcp_C0 * T;
-
-    for (int r = 0; r < H.R; r++) {
-        const Reaction& x = reactions[r];
-        double M = Ctot;
-        if (x.eff_row >= 0) {  // efficiency() (reaction.rs:141-145)
-            const double* e = eff + (size_t)x.eff_row * K;
-            double s = 0.0;
-            for (int k = 0; k < K; k++) s = fma(e[k], C[k], s);
-            M = Ctot + s;
-        }
-        double num, den = 1.0;
-        bool ratio = false;
-        if (x.model == 4) {  // Troe (reaction.rs:160-193)
-            const Falloff& f = falloff[x.falloff];
-            const double k0 = arrhenius(f.k0, t);
-            double Pr, kinf;
-            if (f.flags & kKinfConst) {
-                Pr = M * k0;
-                kinf = f.ainf;
-            } else {
-                const double ki = arrhenius(x.k, t);
-                Pr = div64(M * k0, ki + kF32MinPos);
-                kinf = f.ainf * ki;
-            }
-            double lnF;
-            if (f.flags & kFcentConst) lnF = f.ln_fcent;
-            else {
-                double F = 0.0;
-                if (f.flags & kTermT3) F = f.c1mA * exp64(T * f.c3);
-                if (f.flags & kTermT1) F += f.cA * exp64(T * f.c1);
-                if (f.flags & kTermAConst) F += f.cA;
-                if (f.flags & kTermT2) F += exp64(f.cmT2 * t.rcpT);
-                lnF = log64(F);
-            }
-            const double Cc = fma(-0.67, lnF, -H.ln10_04);
-            const double Nn = fma(-1.27, lnF, H.ln10_075);
-            const double lnPrC = log64(Pr + kF32MinPos) + Cc;
-            const double f1 = div64(lnPrC, fma(-0.14, lnPrC, Nn));
-            const double Fb = exp64(div64(lnF, fma(f1, f1, 1.0)));
-            num = (Fb * kinf) * Pr;
-            den = Pr + 1.0;
-            ratio = true;
-        } else if (x.model == 3) {  // Lindemann (reaction.rs:153-159)
-            const Falloff& f = falloff[x.falloff];
-            const double Ck0 = M * arrhenius(f.k0, t);
-            const double ki = arrhenius(x.k, t);
-            num = Ck0 * ki;
-            den = (Ck0 + ki) + kF32MinPos;
-            ratio = true;
-        } else {
-            num = arrhenius(x.k, t);
-            if (x.model == 2) num *= M;  // three-body (reaction.rs:152)
-        }
-        // Rate of progress (reaction.rs:269-306).
-        double Rf = 1.0;
-        for (int q = 0; q < x.n_r; q++)
-            for (int n = 0; n < x.r_n[q]; n++) Rf *= C[x.r_k[q]];
-        double Rnet = Rf;
-        if (x.model != 1) {
-            double p = 1.0;
-            for (int q = 0; q < x.n_net; q++) {
-                const int nu = x.net_n[q], k = x.net_k[q];
-                const double tt = nu > 0 ? ex[k] : exn[k];
-                for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
-            }
-            switch (x.minus_sigma_net) {
-            case 1: p = C0 * p; break;
-            case -1: p = rcpC0 * p; break;
-            case -2: p = (rcpC0 * rcpC0) * p; break;
-            default: break;
-            }
-            double Rr = 1.0;
-            for (int q = 0; q < x.n_p; q++)
-                for (int n = 0; n < x.p_n[q]; n++) Rr *= C[x.p_k[q]];
-            Rnet = Rf - p * Rr;
-        }
-        const double cR = ratio ? div64(Rnet * num, den) : Rnet * num;
+    for (int r = 0; r < H.R; r++) {  // species_rates (reaction.rs:312-327)
+        const Reaction& x = tb.reactions[r];
+        const double cR = reaction_rate<KMAX>(tb, x, c);
         for (int q = 0; q < x.n_net; q++) wdot[x.net_k[q]] = fma((double)x.net_n[q], cR, wdot[x.net_k[q]]);
     }
-
     // Energy and volume (reaction.rs:375-384).
     double E = 0.0;
     for (int k = 0; k < A; k++) {
-        const Species& s = species[k];
+        const Species& s = tb.species[k];
         const double* h = s.h[piece_of(s.split, T)];
-        const double hk = fma(h[5], t.rcpT, fma(h[4], t.T4, fma(h[3], t.T3, fma(h[2], t.T2, fma(h[1], T, h[0])))));
+        const double hk = fma(h[5], c.t.rcpT, fma(h[4], c.t.T4, fma(h[3], c.t.T3, fma(h[2], c.t.T2, fma(h[1], T, h[0])))));
         E = fma(wdot[k], hk, E);
     }
     double Cp = 0.0;
     for (int k = 0; k < K; k++) {
-        const Species& s = species[k];
-        const double* c = s.cp[piece_of(s.split, T)];
-        const double ck = fma(c[4], t.T4, fma(c[3], t.T3, fma(c[2], t.T2, fma(c[1], T, c[0]))));
-        Cp = fma(ck, C[k], Cp);
+        const Species& s = tb.species[k];
+        const double* cp = s.cp[piece_of(s.split, T)];
+        const double ck = fma(cp[4], c.t.T4, fma(cp[3], c.t.T3, fma(cp[2], c.t.T2, fma(cp[1], T, cp[0]))));
+        Cp = fma(ck, c.C[k], Cp);
     }
     const double dtT_T = div64(-E, Cp);
     double dtE = 0.0;
-    for (int k = 0; k < A; k++) dtE = fma(species[k].dtE, wdot[k], dtE);
+    for (int k = 0; k < A; k++) dtE = fma(tb.species[k].dtE, wdot[k], dtE);
     io.out[0][i] = T * dtT_T;
     io.out[1][i] = V * fma(rcp_pressure_R * T, dtE, dtT_T);
     for (int k = 0; k < A; k++) io.out[2 + k][i] = wdot[k];
+}
+
+template <int KMAX>
+__device__ void reaction_rates_cell(const RatesTables& tb, const ReactionRatesArgs<KMAX>& io, size_t i) {
+    Cell<KMAX> c;
+    cell_setup<KMAX>(tb, io.in[0][i], io.in[1][i], io.in[2][i], io.in + 3, i, c);
+    for (int r = 0; r < tb.H->R; r++) io.out[r][i] = reaction_rate<KMAX>(tb, tb.reactions[r], c);
 }
 
 template <int KMAX, bool SMEM>
@@ -209,8 +247,25 @@ __global__ void __launch_bounds__(kBlock) rates_kernel(const uint8_t* __restrict
         if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
         tab = smem;
     }
+    const RatesTables tb(tab);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        rates_cell<KMAX>(tab, io, i);
+        rates_cell<KMAX>(tb, io, i);
+}
+
+template <int KMAX, bool SMEM>
+__global__ void __launch_bounds__(kBlock) reaction_rates_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
+                                                               const __grid_constant__ ReactionRatesArgs<KMAX> io,
+                                                               size_t n, int* status) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint64_t bar;
+    const uint8_t* tab = gtab;
+    if (SMEM) {
+        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
+        tab = smem;
+    }
+    const RatesTables tb(tab);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        reaction_rates_cell<KMAX>(tb, io, i);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -225,14 +280,26 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
     const double* AB = reinterpret_cast<const double*>(tab + H.off_AB);
     const double* B2 = reinterpret_cast<const double*>(tab + H.off_B2);
     const int K = H.K;
-    const double N = io.in[0][i], Tn = io.in[1][i];
+    double N, Tn;
+    const double* const* amounts;
+    if (io.flags & kFromRates) {  // sum n = (P/R V) / T and T/T0 of a rates-layout cell
+        const double pressure_R = (io.flags & kUniformPressure) ? io.in[0][0] : io.in[0][i];
+        const double T = io.in[2][i];
+        N = div64(pressure_R * io.in[3][i], T);
+        Tn = div64(T, H.T0);
+        amounts = io.in + 4;
+    } else {
+        N = io.in[0][i];
+        Tn = io.in[1][i];
+        amounts = io.in + 2;
+    }
     const double L1 = log64(Tn), L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
     auto poly = [&](const double* P) { return fma(P[4], L4, fma(P[3], L3, fma(P[2], L2, fma(P[1], L1, P[0])))); };
 
     double X[KMAX], v[KMAX], Y[KMAX], Z[KMAX];
     double s = 0.0;
     for (int k = 0; k < K - 1; k++) {
-        X[k] = io.in[2 + k][i];
+        X[k] = amounts[k][i];
         s += X[k];
     }
     X[K - 1] = N - s;
@@ -308,95 +375,68 @@ __global__ void __launch_bounds__(kBlock) transport_kernel(const uint8_t* __rest
 
 // ---------------------------------------------------------------------------------------------------
 namespace {
-int g_sms = 0;
 int sm_count() {
-    if (!g_sms) {
+    static int sms = 0;
+    if (!sms) {
         int dev = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
     }
-    return g_sms;
+    return sms;
 }
 
-template <int KMAX>
-cudaError_t launch_rates_k(const uint8_t* tab, uint32_t tab_bytes, const RatesArgs<KMAX>& io, size_t n,
-                           cudaStream_t st, int* status, int max_smem) {
-    const bool smem = (int)tab_bytes <= max_smem;
-    int blocks_per_sm = 1;
+// Persistent grid: as many blocks as fit on the GPU at once (each stages the tables once), never more
+// than the cells need. Tables go to shared memory when they fit, else they are read through L1/L2.
+template <class Args, class KS, class KG>
+cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io,
+                                size_t n, cudaStream_t st, int* status) {
+    const bool smem = (int)tab_bytes <= max_table_smem();
+    int per_sm = 1;
+    const size_t want = (n + kBlock - 1) / kBlock;
     if (smem) {
-        auto k = rates_kernel<KMAX, true>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
+        cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
         if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k, kBlock, tab_bytes);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-        size_t want = (n + kBlock - 1) / kBlock, grid = (size_t)sm_count() * blocks_per_sm;
-        if (want < grid) grid = want ? want : 1;
-        k<<<(unsigned)grid, kBlock, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, kBlock, tab_bytes);
     } else {
-        auto k = rates_kernel<KMAX, false>;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k, kBlock, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-        size_t want = (n + kBlock - 1) / kBlock, grid = (size_t)sm_count() * blocks_per_sm;
-        if (want < grid) grid = want ? want : 1;
-        k<<<(unsigned)grid, kBlock, 0, st>>>(tab, tab_bytes, io, n, status);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, kBlock, 0);
     }
-    return cudaGetLastError();
-}
-
-template <int KMAX>
-cudaError_t launch_transport_k(const uint8_t* tab, uint32_t tab_bytes, const TransportArgs<KMAX>& io, size_t n,
-                               cudaStream_t st, int* status, int max_smem) {
-    const bool smem = (int)tab_bytes <= max_smem;
-    int blocks_per_sm = 1;
-    if (smem) {
-        auto k = transport_kernel<KMAX, true>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k, kBlock, tab_bytes);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-        size_t want = (n + kBlock - 1) / kBlock, grid = (size_t)sm_count() * blocks_per_sm;
-        if (want < grid) grid = want ? want : 1;
-        k<<<(unsigned)grid, kBlock, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    } else {
-        auto k = transport_kernel<KMAX, false>;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k, kBlock, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
-        size_t want = (n + kBlock - 1) / kBlock, grid = (size_t)sm_count() * blocks_per_sm;
-        if (want < grid) grid = want ? want : 1;
-        k<<<(unsigned)grid, kBlock, 0, st>>>(tab, tab_bytes, io, n, status);
-    }
+    if (per_sm < 1) per_sm = 1;
+    size_t grid = (size_t)sm_count() * per_sm;
+    if (want < grid) grid = want ? want : 1;
+    if (smem) ksmem<<<(unsigned)grid, kBlock, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, kBlock, 0, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace
 
 int max_table_smem() {
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return optin - 1024;  // leave room for the static shared variables
+    static int v = -1;
+    if (v < 0) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        v = optin - 1024;  // room for the static shared variables
+    }
+    return v;
 }
 
-cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
-                         cudaStream_t st, int* status) {
-    const int ms = max_table_smem();
-    switch (kmax) {
-    case 16: return launch_rates_k<16>(tab, tab_bytes, *static_cast<const RatesArgs<16>*>(args), n, st, status, ms);
-    case 64: return launch_rates_k<64>(tab, tab_bytes, *static_cast<const RatesArgs<64>*>(args), n, st, status, ms);
-    case 256: return launch_rates_k<256>(tab, tab_bytes, *static_cast<const RatesArgs<256>*>(args), n, st, status, ms);
-    default: return cudaErrorInvalidValue;
+#define CB_DISPATCH(FN, KERNEL, ARGS)                                                                      \
+    cudaError_t FN(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,            \
+                   cudaStream_t st, int* status) {                                                         \
+        switch (kmax) {                                                                                    \
+        case 16: return launch_table_kernel(KERNEL<16, true>, KERNEL<16, false>, tab, tab_bytes,           \
+                                            *static_cast<const ARGS<16>*>(args), n, st, status);           \
+        case 64: return launch_table_kernel(KERNEL<64, true>, KERNEL<64, false>, tab, tab_bytes,           \
+                                            *static_cast<const ARGS<64>*>(args), n, st, status);           \
+        case 256: return launch_table_kernel(KERNEL<256, true>, KERNEL<256, false>, tab, tab_bytes,        \
+                                             *static_cast<const ARGS<256>*>(args), n, st, status);         \
+        default: return cudaErrorInvalidValue;                                                             \
+        }                                                                                                  \
     }
-}
-
-cudaError_t launch_transport(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
-                             cudaStream_t st, int* status) {
-    const int ms = max_table_smem();
-    switch (kmax) {
-    case 16: return launch_transport_k<16>(tab, tab_bytes, *static_cast<const TransportArgs<16>*>(args), n, st, status, ms);
-    case 64: return launch_transport_k<64>(tab, tab_bytes, *static_cast<const TransportArgs<64>*>(args), n, st, status, ms);
-    case 256: return launch_transport_k<256>(tab, tab_bytes, *static_cast<const TransportArgs<256>*>(args), n, st, status, ms);
-    default: return cudaErrorInvalidValue;
-    }
-}
+CB_DISPATCH(launch_rates, rates_kernel, RatesArgs)
+CB_DISPATCH(launch_reaction_rates, reaction_rates_kernel, ReactionRatesArgs)
+CB_DISPATCH(launch_transport, transport_kernel, TransportArgs)
+#undef CB_DISPATCH
 
 }  // namespace cbg

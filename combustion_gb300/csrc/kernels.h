@@ -15,9 +15,23 @@ struct RatesArgs {
     uint32_t flags;              // bit 1: P/R and R/P are single values
 };
 
+// Per-reaction rates of progress: inputs P/R, T, V, n_0 .. n_{K-2}; one output per reaction.
+constexpr int kMaxReactions = 2048;
+template <int KMAX>
+struct ReactionRatesArgs {
+    const double* in[KMAX + 2];
+    double* out[kMaxReactions];
+    uint32_t flags;
+};
+
+// Transport input layouts: the reference's (sum n, T/T0, n...) or, with kFromRates, the rates inputs
+// (P/R, R/P, T, V, n...) from which sum n = (P/R * V) / T and T/T0 are derived per cell.
+constexpr uint32_t kUniformPressure = 2u;
+constexpr uint32_t kFromRates = 4u;
+
 template <int KMAX>
 struct TransportArgs {
-    const double* in[KMAX + 1];  // sum n, T/T0, n_0 .. n_{K-2}
+    const double* in[KMAX + 3];  // sum n, T/T0, n_0 .. n_{K-2} (or the rates inputs with kFromRates)
     double* out[KMAX + 2];       // lambda/lambda0, mu/mu0, rhoD_k/mu0
     uint32_t flags;
 };
@@ -28,6 +42,8 @@ inline int kmax_for(int K) { return K <= 16 ? 16 : K <= 64 ? 64 : K <= 256 ? 256
 int max_table_smem();
 cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
                          cudaStream_t st, int* status);
+cudaError_t launch_reaction_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                                  cudaStream_t st, int* status);
 cudaError_t launch_transport(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
                              cudaStream_t st, int* status);
 

@@ -533,7 +533,7 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
         }
     TransportHeader h;
     std::memset(&h, 0, sizeof h);
-    h.K = K; h.n_pairs = n_pairs;
+    h.K = K; h.n_pairs = n_pairs; h.T0 = T0;
     std::vector<uint8_t>& blob = m.transport_blob;
     blob.clear();
     append(blob, &h, 1);

@@ -69,6 +69,7 @@ struct RatesHeader {
 struct TransportHeader {
     int32_t K, n_pairs, total_bytes, pad;
     int32_t off_cond, off_visc, off_W, off_diff, off_A2, off_AB, off_B2, pad2;
+    double T0, pad3;  // temperature normalisation (inputs from the rates layout are divided by it)
 };
 
 }  // namespace cbg

@@ -357,3 +357,33 @@ def generate_cells(K: int, n: int, config: str = "k53", seed: int = 1, offset: i
     amounts = X[:K - 1] * total
     return Cells(pressure_R=pressure_R, temperature=T, volume=V, amounts=np.ascontiguousarray(amounts),
                  total_amount=total)
+
+
+def _cells_window(args):
+    K, n, config, seed, offset = args
+    c = generate_cells(K, n, config, seed, offset)
+    return c.pressure_R, c.temperature, c.volume, c.amounts, c.total_amount
+
+
+def generate_cells_parallel(K: int, n: int, config: str = "k53", seed: int = 1, workers: int = 0,
+                            out_amounts: np.ndarray = None) -> Cells:
+    """generate_cells over ``workers`` spawned processes (identical result: draws are counter-based).
+    ``out_amounts`` ([K-1, n] float64, e.g. pinned host memory) receives the amounts in place."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os as _os
+    workers = workers or min(16, _os.cpu_count() or 1)
+    if n < 65536 or workers == 1:
+        c = generate_cells(K, n, config, seed)
+        if out_amounts is not None:
+            out_amounts[:] = c.amounts
+            c.amounts = out_amounts
+        return c
+    bounds = [n * w // workers for w in range(workers + 1)]
+    jobs = [(K, bounds[w + 1] - bounds[w], config, seed, bounds[w]) for w in range(workers)]
+    P, T, V, N = (np.empty(n) for _ in range(4))
+    amounts = out_amounts if out_amounts is not None else np.empty((K - 1, n))
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        for (lo, hi), (p, t, v, a, tot) in zip(zip(bounds[:-1], bounds[1:]), ex.map(_cells_window, jobs)):
+            P[lo:hi], T[lo:hi], V[lo:hi], amounts[:, lo:hi], N[lo:hi] = p, t, v, a, tot
+    return Cells(pressure_R=P, temperature=T, volume=V, amounts=amounts, total_amount=N)

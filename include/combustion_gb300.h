@@ -140,6 +140,10 @@ int cb_rates_transport_f64(cb_mech* mech, size_t n, const double* const* inputs,
 
 int cb_work_model(const cb_mech* mech, cb_work* rates, cb_work* transport);
 
+/* Diagnostic: FP64 fused multiply-adds per second the current GPU issues (8 independent chains per
+ * thread, 8 blocks of 256 threads per SM, best of 3): the peak of the FP64-bound kernels' roofline. */
+int cb_device_fp64_peak(double* fma_per_second);
+
 /* Blocks until the mechanism's work on `stream` is done and reports any kernel-side failure. */
 int cb_synchronize(cb_mech* mech, void* stream);
 const char* cb_last_error(void);

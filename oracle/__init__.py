@@ -57,7 +57,7 @@ def lib():
         L.or_reaction_rates.argtypes = [vp, vp, vp]
         L.or_transport.argtypes = [vp, vp, vp, vp]
         L.or_rates_batch.argtypes = [vp, C.c_size_t, vp, vp, vp, C.c_int]
-        L.or_reaction_rates_batch.argtypes = [vp, C.c_size_t, vp, vp, C.c_int]
+        L.or_reaction_rates_batch.argtypes = [vp, C.c_size_t, vp, vp, vp, C.c_int]
         L.or_transport_batch.argtypes = [vp, C.c_size_t, vp, vp, vp, C.c_int]
         L.or_fused_batch.argtypes = [vp, C.c_size_t, vp, vp, vp, C.c_int]
         _lib = L
@@ -166,11 +166,21 @@ class Oracle:
         assert rc == 0, rc
         return (out, sc) if scale else out
 
-    def reaction_rates(self, inputs, nthreads=1):
+    @staticmethod
+    def reaction_rates_inputs(cells):
+        rows = [cells.pressure_R, cells.temperature, cells.volume] + list(cells.amounts)
+        return [np.ascontiguousarray(r, dtype=np.float64) for r in rows]
+
+    def fused_inputs(self, cells):
+        return self.rates_inputs(cells)
+
+    def reaction_rates(self, inputs, nthreads=1, scale=False):
         n = len(inputs[0])
         out = np.zeros((self.R, n))
-        assert lib().or_reaction_rates_batch(self.h, n, _ptrs(inputs), _ptrs(list(out)), nthreads) == 0
-        return out
+        sc = np.zeros((self.R, n)) if scale else None
+        assert lib().or_reaction_rates_batch(self.h, n, _ptrs(inputs), _ptrs(list(out)),
+                                             _ptrs(list(sc)) if scale else None, nthreads) == 0
+        return (out, sc) if scale else out
 
     def transport(self, inputs, nthreads=1, scale=False):
         n = len(inputs[0])

@@ -541,15 +541,19 @@ void or_rates(const or_mech* m, const double* in, double* out, double* scale) {
     work_free(&w);
 }
 
-static void reaction_rates_cell(const or_mech* m, const double* in, double* out, work_t* w) {
+static void reaction_rates_cell(const or_mech* m, const double* in, double* out, double* scale, work_t* w) {
     cell_t c = {.Ck = w->Ck, .ex = w->ex, .exn = w->exn, .has_ex = w->has_ex, .has_exn = w->has_exn};
     cell_prologue(m, in[0], in[1], in[2], in + 3, &c);
-    for (int r = 0; r < m->R; r++) { double mag; out[r] = reaction_cR(m, &m->rx[r], &c, &mag); }
+    for (int r = 0; r < m->R; r++) {
+        double mag;
+        out[r] = reaction_cR(m, &m->rx[r], &c, &mag);
+        if (scale) scale[r] = mag;
+    }
 }
 
 void or_reaction_rates(const or_mech* m, const double* in, double* out) {
     work_t w; work_alloc(m, &w);
-    reaction_rates_cell(m, in, out, &w);
+    reaction_rates_cell(m, in, out, NULL, &w);
     work_free(&w);
 }
 
@@ -862,8 +866,10 @@ static void* run_job(void* p) {
             for (int q = 0; q < A + 2; q++) { j->out[q][i] = tout[q]; if (j->scale) j->scale[q][i] = tsc[q]; }
         } else if (j->kind == 1) { /* reaction rates */
             for (int q = 0; q < K + 2; q++) tin[q] = j->in[q][i];
-            reaction_rates_cell(m, tin, tout, &w);
-            for (int q = 0; q < R; q++) j->out[q][i] = tout[q];
+            double* rsc = j->scale ? malloc(sizeof(double) * R) : NULL;
+            reaction_rates_cell(m, tin, tout, rsc, &w);
+            for (int q = 0; q < R; q++) { j->out[q][i] = tout[q]; if (rsc) j->scale[q][i] = rsc[q]; }
+            free(rsc);
         } else if (j->kind == 2) { /* transport */
             for (int q = 0; q < K + 1; q++) tin[q] = j->in[q][i];
             transport_cell(m, tin, tout, j->scale ? tsc : NULL, X, X + K, X + 2 * K, X + 3 * K, Si);
@@ -909,8 +915,9 @@ int or_rates_batch(const or_mech* m, size_t n, const double* const* in, double* 
                    int nthreads) {
     return run_batch(m, n, 0, in, out, scale, NULL, nthreads);
 }
-int or_reaction_rates_batch(const or_mech* m, size_t n, const double* const* in, double* const* out, int nthreads) {
-    return run_batch(m, n, 1, in, out, NULL, NULL, nthreads);
+int or_reaction_rates_batch(const or_mech* m, size_t n, const double* const* in, double* const* out,
+                            double* const* scale, int nthreads) {
+    return run_batch(m, n, 1, in, out, scale, NULL, nthreads);
 }
 int or_transport_batch(const or_mech* m, size_t n, const double* const* in, double* const* out, double* const* scale,
                        int nthreads) {

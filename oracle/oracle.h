@@ -66,7 +66,8 @@ void or_transport(const or_mech* m, const double* in, double* out, double* scale
  * pointers, one per input/output (scale may be NULL). Returns 0. */
 int or_rates_batch(const or_mech* m, size_t n, const double* const* in, double* const* out,
                    double* const* scale, int nthreads);
-int or_reaction_rates_batch(const or_mech* m, size_t n, const double* const* in, double* const* out, int nthreads);
+int or_reaction_rates_batch(const or_mech* m, size_t n, const double* const* in, double* const* out,
+                            double* const* scale, int nthreads);
 int or_transport_batch(const or_mech* m, size_t n, const double* const* in, double* const* out,
                        double* const* scale, int nthreads);
 /* Rates + transport of the same cells, transport inputs derived as sum n = (P/R * V) / T, T' = T / T0. */

@@ -166,3 +166,48 @@ def test_errors_are_reported_not_raised_on_device():
     with pytest.raises(cb.CombustionError) as e:
         mech.transport(ins, out)
     assert e.value.code == cb.CB_ERR_NOT_READY
+
+
+@pytest.mark.parametrize("config,n", [("k10", 16384), ("k53", 4096)])
+def test_reaction_rates_parity(config, n):
+    from combustion_gb300 import synthetic
+    torch = _torch()
+    m = util.mechanism(config)
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, n, config)
+    ins = o.reaction_rates_inputs(cells)
+    out = torch.empty((mech.R, n), dtype=torch.float64, device="cuda")
+    mech.reaction_rates(_dev(ins), out)
+    torch.cuda.synchronize()
+    mech.synchronize()
+    ref, scale = o.reaction_rates(ins, nthreads=NTHREADS, scale=True)
+    assert _report(f"reaction rates {config}", out.cpu().numpy(), ref, scale).max() <= util.PLAIN_TOL
+
+
+@pytest.mark.parametrize("config,n", [("k10", 16384), ("k53", 4096)])
+def test_fused_parity(config, n):
+    """cb_rates_transport_f64: rates plus transport at sum n = (P/R V)/T, T/T0, device and host memory."""
+    from combustion_gb300 import synthetic
+    torch = _torch()
+    m = util.mechanism(config)
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, n, config)
+    ins = o.rates_inputs(cells)
+    ro = torch.empty((mech.A + 2, n), dtype=torch.float64, device="cuda")
+    to = torch.empty((mech.K + 2, n), dtype=torch.float64, device="cuda")
+    mech.rates_transport(_dev(ins), ro, to)
+    torch.cuda.synchronize()
+    mech.synchronize()
+    rref, tref = o.fused(ins, nthreads=NTHREADS)
+    # condition scales from the separate oracle paths on the same derived inputs
+    _, rsc = o.rates(ins, nthreads=NTHREADS, scale=True)
+    tin = [(ins[0] * ins[3]) / ins[2], ins[2] / o.T0] + ins[4:]
+    tref2, tsc = o.transport(tin, nthreads=NTHREADS, scale=True)
+    assert np.array_equal(tref, tref2)
+    assert _report(f"fused rates {config}", ro.cpu().numpy(), rref, rsc).max() <= util.PLAIN_TOL
+    assert _report(f"fused transport {config}", to.cpu().numpy(), tref, tsc).max() <= util.PLAIN_TOL
+    hro, hto = np.zeros((mech.A + 2, n)), np.zeros((mech.K + 2, n))
+    mech.rates_transport(np.array(ins), hro, hto)
+    assert np.array_equal(hro, ro.cpu().numpy()) and np.array_equal(hto, to.cpu().numpy())
