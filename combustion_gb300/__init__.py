@@ -34,7 +34,7 @@ CB_UNIFORM_PRESSURE = 2
 EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_query", "cb_transport_setup",
            "cb_transport_fit", "cb_transport_coefficients", "cb_rates_f64", "cb_reaction_rates_f64",
            "cb_transport_f64", "cb_rates_transport_f64", "cb_work_model", "cb_synchronize", "cb_last_error",
-           "cb_version", "cb_device_fp64_peak"]
+           "cb_version", "cb_device_fp64_peak", "cb_fp64_math"]
 
 
 class CombustionError(RuntimeError):
@@ -91,6 +91,7 @@ def lib():
         L.cb_last_error.restype = C.c_char_p
         L.cb_version.restype = C.c_char_p
         L.cb_device_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+        L.cb_fp64_math.argtypes = [C.c_int, vp, vp, sz, vp]
         _lib = L
     return _lib
 
@@ -264,6 +265,16 @@ def device_fp64_peak() -> float:
     v = C.c_double()
     _check(lib().cb_device_fp64_peak(C.byref(v)))
     return v.value
+
+
+def fp64_math(which: str, x):
+    """The kernels' FP64 exp/log/reciprocal on a CUDA float64 tensor (which: "exp", "log", "rcp")."""
+    import torch
+    code = {"exp": 0, "log": 1, "rcp": 2}[which]
+    x = x.contiguous()
+    y = torch.empty_like(x)
+    _check(lib().cb_fp64_math(code, x.data_ptr(), y.data_ptr(), x.numel(), torch.cuda.current_stream().cuda_stream))
+    return y
 
 
 def version() -> str:

@@ -9,6 +9,7 @@
 #include "../../include/combustion_gb300.h"
 #include "kernels.h"
 #include "mechanism.hpp"
+#include "tables.h"
 
 struct cb_mech {
     cbg::HostMechanism host;
@@ -326,6 +327,19 @@ int cb_work_model(const cb_mech* m, cb_work* rates, cb_work* transport) {
     if (rates) to_work(m->host.rates_work, rates);
     if (transport) to_work(m->host.transport_work, transport);
     return CB_OK;
+}
+
+int cb_fp64_math(int which, const double* x, double* y, size_t n, void* stream) {
+    if (which < 0 || which > 2 || (n && (!x || !y))) return fail(CB_ERR_INVALID, "bad arguments");
+    cbg::MathTables t = cbg::make_math_tables();
+    uint8_t* d = nullptr;
+    CB_CUDA(cudaMalloc(&d, sizeof t));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(d, &t, sizeof t, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cbg::launch_math_check(d, which, x, y, n, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    return e == cudaSuccess ? CB_OK : cuda_fail(e, "math check");
 }
 
 int cb_synchronize(cb_mech* m, void* stream) {

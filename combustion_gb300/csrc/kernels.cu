@@ -17,6 +17,22 @@ namespace cbg {
 constexpr double kF32Max = 3.4028234663852886e+38;     // f32::MAX as f64
 constexpr double kF32MinPos = 1.1754943508222875e-38;  // f32::MIN_POSITIVE as f64
 
+// Per-block copy of the elementary-function tables (lane-divergent lookups).
+__shared__ MathTables s_math;
+
+__device__ __forceinline__ double exp64(double x) { return exp_fast(x, s_math.exp2j); }
+__device__ __forceinline__ double log64(double x) { return log_fast(x, s_math); }
+__device__ __forceinline__ double rcp64(double x) { return rcp_fast(x); }
+__device__ __forceinline__ double div64(double a, double b) { return div_fast(a, b); }
+
+// Copies the math tables of a blob (byte offset off_math) into s_math; call before any use.
+__device__ __forceinline__ void load_math(const uint8_t* gtab, int off_math) {
+    const double* src = reinterpret_cast<const double*>(gtab + off_math);
+    double* dst = reinterpret_cast<double*>(&s_math);
+    for (int q = threadIdx.x; q < (int)(sizeof(MathTables) / sizeof(double)); q += blockDim.x) dst[q] = src[q];
+    __syncthreads();
+}
+
 struct Temps {
     double lnT, T, T2, T3, T4, rcpT, rcpT2;
 };
@@ -115,9 +131,16 @@ __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Rea
     double M = c.Ctot;
     if (x.eff_row >= 0) {  // efficiency() (reaction.rs:141-145)
         const double* e = tb.eff + (size_t)x.eff_row * K;
-        double s = 0.0;
-        for (int k = 0; k < K; k++) s = fma(e[k], c.C[k], s);
-        M = c.Ctot + s;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // four independent chains
+        int k = 0;
+        for (; k + 3 < K; k += 4) {
+            s0 = fma(e[k], c.C[k], s0);
+            s1 = fma(e[k + 1], c.C[k + 1], s1);
+            s2 = fma(e[k + 2], c.C[k + 2], s2);
+            s3 = fma(e[k + 3], c.C[k + 3], s3);
+        }
+        for (; k < K; k++) s0 = fma(e[k], c.C[k], s0);
+        M = c.Ctot + ((s0 + s1) + (s2 + s3));
     }
     double num, den = 1.0;
     bool ratio = false;
@@ -242,6 +265,7 @@ __global__ void __launch_bounds__(kBlock) rates_kernel(const uint8_t* __restrict
                                                       int* status) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
+    load_math(gtab, reinterpret_cast<const RatesHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
     if (SMEM) {
         if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
@@ -258,6 +282,7 @@ __global__ void __launch_bounds__(kBlock) reaction_rates_kernel(const uint8_t* _
                                                                size_t n, int* status) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
+    load_math(gtab, reinterpret_cast<const RatesHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
     if (SMEM) {
         if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
@@ -325,45 +350,68 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         Y[k] = X[k] * r;
         Z[k] = Y[k] * r;
     }
+    // Four rows per pass over j (rows padded with zeros to a multiple of 4): 12 independent FMA chains
+    // per thread and one load of X_j, Y_j, Z_j per 12 FMAs.
     double mu = 0.0;
-    for (int k = 0; k < K; k++) {
-        const double* a2 = A2 + (size_t)k * K;
-        const double* ab = AB + (size_t)k * K;
-        const double* b2 = B2 + (size_t)k * K;
-        double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int k0 = 0; k0 < K; k0 += 4) {
+        const double* a2 = A2 + (size_t)k0 * K;
+        const double* ab = AB + (size_t)k0 * K;
+        const double* b2 = B2 + (size_t)k0 * K;
+        double s1[4] = {0.0, 0.0, 0.0, 0.0}, s2[4] = {0.0, 0.0, 0.0, 0.0}, s3[4] = {0.0, 0.0, 0.0, 0.0};
         for (int j = 0; j < K; j++) {
-            s1 = fma(a2[j], X[j], s1);
-            s2 = fma(ab[j], Y[j], s2);
-            s3 = fma(b2[j], Z[j], s3);
+            const double xj = X[j], yj = Y[j], zj = Z[j];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                s1[q] = fma(a2[q * K + j], xj, s1[q]);
+                s2[q] = fma(ab[q * K + j], yj, s2[q]);
+                s3[q] = fma(b2[q * K + j], zj, s3[q]);
+            }
         }
-        const double den = fma(v[k], fma(v[k], s3, s2), s1);
-        mu = fma(X[k] * (v[k] * v[k]), rcp64(den), mu);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = k0 + q;
+            if (k < K) {
+                const double den = fma(v[k], fma(v[k], s3[q], s2[q]), s1[q]);
+                mu = fma(X[k] * (v[k] * v[k]), rcp64(den), mu);
+            }
+        }
     }
     io.out[1][i] = VT * mu;
 
     // Mixture-averaged diffusion (transport.rs:162-177); S reuses Y.
     double* S = Y;
     for (int k = 0; k < K; k++) S[k] = 0.0;
+    // Two pairs per iteration: two independent polynomial + reciprocal chains.
     const double* P = diff;
     for (int k = 1; k < K; k++) {
         const double xk = X[k];
-        double sk = 0.0;
-        for (int j = 0; j < k; j++, P += 5) {
-            const double R = rcp64(poly(P));
-            sk = fma(X[j], R, sk);
-            S[j] = fma(xk, R, S[j]);
+        double sa = 0.0, sb = 0.0;
+        int j = 0;
+        for (; j + 1 < k; j += 2, P += 10) {
+            const double Ra = rcp64(poly(P)), Rb = rcp64(poly(P + 5));
+            sa = fma(X[j], Ra, sa);
+            sb = fma(X[j + 1], Rb, sb);
+            S[j] = fma(xk, Ra, S[j]);
+            S[j + 1] = fma(xk, Rb, S[j + 1]);
         }
-        S[k] += sk;
+        if (j < k) {
+            const double R = rcp64(poly(P));
+            sa = fma(X[j], R, sa);
+            S[j] = fma(xk, R, S[j]);
+            P += 5;
+        }
+        S[k] += sa + sb;
     }
     for (int k = 0; k < K; k++) io.out[2 + k][i] = div64(MVTN - (VT * W[k]) * X[k], S[k]);
 }
 
 template <int KMAX, bool SMEM>
-__global__ void __launch_bounds__(kBlock) transport_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
+__global__ void __launch_bounds__(kTransportBlock) transport_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                           const __grid_constant__ TransportArgs<KMAX> io,
                                                           size_t n, int* status) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
+    load_math(gtab, reinterpret_cast<const TransportHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
     if (SMEM) {
         if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
@@ -388,27 +436,46 @@ int sm_count() {
 
 // Persistent grid: as many blocks as fit on the GPU at once (each stages the tables once), never more
 // than the cells need. Tables go to shared memory when they fit, else they are read through L1/L2.
-template <class Args, class KS, class KG>
+template <int BLOCK, class Args, class KS, class KG>
 cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io,
                                 size_t n, cudaStream_t st, int* status) {
     const bool smem = (int)tab_bytes <= max_table_smem();
     int per_sm = 1;
-    const size_t want = (n + kBlock - 1) / kBlock;
+    const size_t want = (n + BLOCK - 1) / BLOCK;
     if (smem) {
         cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
         if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, kBlock, tab_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, kBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, 0);
     }
     if (per_sm < 1) per_sm = 1;
     size_t grid = (size_t)sm_count() * per_sm;
     if (want < grid) grid = want ? want : 1;
-    if (smem) ksmem<<<(unsigned)grid, kBlock, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    else kglobal<<<(unsigned)grid, kBlock, 0, st>>>(tab, tab_bytes, io, n, status);
+    if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, BLOCK, 0, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace
+
+// The elementary functions of the plain path on device arrays (which: 0 exp, 1 log, 2 reciprocal), for
+// accuracy checks against CUDA's own functions.
+__global__ void math_check_kernel(const uint8_t* math, int which, const double* x, double* y, size_t n) {
+    load_math(math, 0);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        y[i] = which == 0 ? exp64(v) : which == 1 ? log64(v) : rcp64(v);
+    }
+}
+
+cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, double* y, size_t n,
+                              cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    size_t grid = (n + 255) / 256;
+    if (grid > 4096) grid = 4096;
+    math_check_kernel<<<(unsigned)grid, 256, 0, st>>>(math, which, x, y, n);
+    return cudaGetLastError();
+}
 
 int max_table_smem() {
     static int v = -1;
@@ -416,27 +483,27 @@ int max_table_smem() {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        v = optin - 1024;  // room for the static shared variables
+        v = optin - (int)sizeof(MathTables) - 1024;  // room for the static shared variables
     }
     return v;
 }
 
-#define CB_DISPATCH(FN, KERNEL, ARGS)                                                                      \
+#define CB_DISPATCH(FN, KERNEL, ARGS, BLOCK)                                                               \
     cudaError_t FN(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,            \
                    cudaStream_t st, int* status) {                                                         \
         switch (kmax) {                                                                                    \
-        case 16: return launch_table_kernel(KERNEL<16, true>, KERNEL<16, false>, tab, tab_bytes,           \
-                                            *static_cast<const ARGS<16>*>(args), n, st, status);           \
-        case 64: return launch_table_kernel(KERNEL<64, true>, KERNEL<64, false>, tab, tab_bytes,           \
-                                            *static_cast<const ARGS<64>*>(args), n, st, status);           \
-        case 256: return launch_table_kernel(KERNEL<256, true>, KERNEL<256, false>, tab, tab_bytes,        \
-                                             *static_cast<const ARGS<256>*>(args), n, st, status);         \
+        case 16: return launch_table_kernel<BLOCK>(KERNEL<16, true>, KERNEL<16, false>, tab, tab_bytes,    \
+                                                   *static_cast<const ARGS<16>*>(args), n, st, status);    \
+        case 64: return launch_table_kernel<BLOCK>(KERNEL<64, true>, KERNEL<64, false>, tab, tab_bytes,    \
+                                                   *static_cast<const ARGS<64>*>(args), n, st, status);    \
+        case 256: return launch_table_kernel<BLOCK>(KERNEL<256, true>, KERNEL<256, false>, tab, tab_bytes, \
+                                                    *static_cast<const ARGS<256>*>(args), n, st, status);  \
         default: return cudaErrorInvalidValue;                                                             \
         }                                                                                                  \
     }
-CB_DISPATCH(launch_rates, rates_kernel, RatesArgs)
-CB_DISPATCH(launch_reaction_rates, reaction_rates_kernel, ReactionRatesArgs)
-CB_DISPATCH(launch_transport, transport_kernel, TransportArgs)
+CB_DISPATCH(launch_rates, rates_kernel, RatesArgs, kBlock)
+CB_DISPATCH(launch_reaction_rates, reaction_rates_kernel, ReactionRatesArgs, kBlock)
+CB_DISPATCH(launch_transport, transport_kernel, TransportArgs, kTransportBlock)
 #undef CB_DISPATCH
 
 }  // namespace cbg

@@ -5,7 +5,10 @@
 
 namespace cbg {
 
-constexpr int kBlock = 128;  // threads per block: one warp per SM sub-partition fills the FP64 pipe
+// Threads per block. The rates tables (94 KB at K = 53) fit twice per SM: 2 x 128 threads give two warps
+// per SM sub-partition. The transport tables (135 KB) fit once, so that kernel runs 256-thread blocks.
+constexpr int kBlock = 128;
+constexpr int kTransportBlock = 256;
 
 // One pointer per input / output array (struct of arrays), passed by value as a kernel parameter.
 template <int KMAX>
@@ -40,6 +43,8 @@ struct TransportArgs {
 inline int kmax_for(int K) { return K <= 16 ? 16 : K <= 64 ? 64 : K <= 256 ? 256 : 0; }
 
 int max_table_smem();
+cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, double* y, size_t n,
+                              cudaStream_t st);
 cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
                          cudaStream_t st, int* status);
 cudaError_t launch_reaction_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,

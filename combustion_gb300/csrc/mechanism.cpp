@@ -200,6 +200,30 @@ double rotational_scaling(double Ts) {  // fz of transport.rs:109
     return 1. + std::pow(PI, 3. / 2.) / std::sqrt(Ts) * (1. / 2. + 1. / Ts) + (1. / 4. * (PI * PI) + 2.) / Ts;
 }
 
+}  // namespace
+
+// Tables of fp64_math.cuh, computed in long double and rounded once.
+MathTables make_math_tables() {
+    MathTables t;
+    std::memset(&t, 0, sizeof t);
+    for (int j = 0; j < 256; j++) t.exp2j[j] = (double)std::exp2((long double)j / 256.0L);
+    for (int j = 0; j <= 256; j++) {
+        long double c = 1.0L + (long double)j / 256.0L;
+        long double l = std::log(c);
+        t.log_hi[j] = (double)l;
+        t.log_lo[j] = (double)(l - (long double)t.log_hi[j]);
+        t.rcp[j] = (double)(1.0L / c);
+    }
+    // ln 2 split exactly as in log_fast so that e ln2 + ln c cancels exactly just below x = 1.
+    t.log_hi[256] = 0x1.62e42fefa4000p-1;
+    t.log_lo[256] = -0x1.8432a1b0e2634p-43;
+    t.log_hi[0] = 0.0;
+    t.log_lo[0] = 0.0;
+    return t;
+}
+
+namespace {
+
 void add_work(Work& w, double flops, double exps = 0, double logs = 0, double divs = 0, double sqrts = 0) {
     w.flops += flops; w.exps += exps; w.logs += logs; w.divs += divs; w.sqrts += sqrts;
 }
@@ -413,6 +437,10 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     h.off_reactions = align_blob(blob); append(blob, reactions.data(), reactions.size());
     h.off_falloff = align_blob(blob); append(blob, falloff.data(), falloff.size());
     h.off_eff = align_blob(blob); append(blob, eff_rows.data(), eff_rows.size());
+    {
+        MathTables mt = make_math_tables();
+        h.off_math = align_blob(blob); append(blob, &mt, 1);
+    }
     h.total_bytes = align_blob(blob);
     std::memcpy(blob.data(), &h, sizeof h);
 
@@ -522,7 +550,9 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
     for (int k = 0, p = 0; k < K; k++)
         for (int j = 0; j < k; j++, p++) scaled(&m.fit_diff[((size_t)k * K + j) * 5], sd, &diff[(size_t)p * 5]);
     // Wilke: phi_kj = (a_kj + b_kj v_k / v_j)^2 = a^2 + 2ab (v_k/v_j) + b^2 (v_k/v_j)^2 (transport.rs:152-157)
-    std::vector<double> A2((size_t)K * K), AB((size_t)K * K), B2((size_t)K * K);
+    // Rows padded with zeros to a multiple of 4: the kernel evaluates four rows per pass over j.
+    const int K4 = (K + 3) / 4 * 4;
+    std::vector<double> A2((size_t)K4 * K, 0.), AB((size_t)K4 * K, 0.), B2((size_t)K4 * K, 0.);
     for (int k = 0; k < K; k++)
         for (int j = 0; j < K; j++) {
             double Va = std::sqrt(1. / std::sqrt(8.) * 1. / std::sqrt(1. + m.W[k] / m.W[j]));
@@ -544,6 +574,10 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
     h.off_A2 = align_blob(blob); append(blob, A2.data(), A2.size());
     h.off_AB = align_blob(blob); append(blob, AB.data(), AB.size());
     h.off_B2 = align_blob(blob); append(blob, B2.data(), B2.size());
+    {
+        MathTables mt = make_math_tables();
+        h.off_math = align_blob(blob); append(blob, &mt, 1);
+    }
     h.total_bytes = align_blob(blob);
     std::memcpy(blob.data(), &h, sizeof h);
 

@@ -37,6 +37,9 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err);
 // Fits the species properties and packs the transport tables for the given normalisation.
 int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std::string& err);
 
+struct MathTables;
+MathTables make_math_tables();
+
 // Transport physics of one species or pair at temperature T (SI), used by the fits.
 double species_viscosity(const HostMechanism& m, int k, double T);
 double species_conductivity(const HostMechanism& m, int k, double T);

@@ -60,14 +60,24 @@ struct Species {
     int32_t pad[2];
 };
 
+// Tables of the FP64 elementary functions (fp64_math.cuh), staged with every blob: lookups use a
+// different index in every lane, which shared memory serves and the constant cache would serialise.
+struct MathTables {
+    double exp2j[256];   // 2^(j/256), correctly rounded
+    double log_hi[257];  // ln(1 + j/256) as a double-double (log_hi[256] + log_lo[256] = ln 2 split
+    double log_lo[257];  //   exactly like the ln 2 constant of log_fast)
+    double rcp[257];     // 1 / (1 + j/256), rounded
+    double pad;
+};
+
 struct RatesHeader {
     int32_t K, A, R, n_eff, n_falloff, total_bytes;
-    int32_t off_species, off_reactions, off_falloff, off_eff, pad[2];
+    int32_t off_species, off_reactions, off_falloff, off_eff, off_math, pad;
     double M3, cbrt_max, C0, rcp_C0, ln10_04, ln10_075, pad2[2];
 };
 
 struct TransportHeader {
-    int32_t K, n_pairs, total_bytes, pad;
+    int32_t K, n_pairs, total_bytes, off_math;
     int32_t off_cond, off_visc, off_W, off_diff, off_A2, off_AB, off_B2, pad2;
     double T0, pad3;  // temperature normalisation (inputs from the rates layout are divided by it)
 };

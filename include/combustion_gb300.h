@@ -144,6 +144,10 @@ int cb_work_model(const cb_mech* mech, cb_work* rates, cb_work* transport);
  * thread, 8 blocks of 256 threads per SM, best of 3): the peak of the FP64-bound kernels' roofline. */
 int cb_device_fp64_peak(double* fma_per_second);
 
+/* Diagnostic: the FP64 elementary functions the kernels use (which: 0 exp, 1 natural log, 2 reciprocal)
+ * evaluated on n device doubles, synchronously on `stream`. */
+int cb_fp64_math(int which, const double* x, double* y, size_t n, void* stream);
+
 /* Blocks until the mechanism's work on `stream` is done and reports any kernel-side failure. */
 int cb_synchronize(cb_mech* mech, void* stream);
 const char* cb_last_error(void);
