@@ -187,6 +187,17 @@ def run_ours(args):
     ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev_mid = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # The mixed-precision form on the same inputs (reported under "forms", not in "value").
+    m_r_out = torch.empty_like(r_out)
+    m_t_out = torch.empty_like(t_out)
+
+    def step_mixed():
+        mech.rates(d_in, m_r_out, mixed=True)
+        mech.transport(t_in, m_t_out, mixed=True)
+
+    for _ in range(args.warmup):
+        step_mixed()
+    mix_start, mix_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         time.sleep(0.3)
         torch.cuda.synchronize()
@@ -195,7 +206,13 @@ def run_ours(args):
             step(ev_mid[s])
             ev_end[s].record(stream)
         torch.cuda.synchronize()
+        mix_start.record(stream)
+        for s in range(args.steps):
+            step_mixed()
+        mix_end.record(stream)
+        torch.cuda.synchronize()
     mech.synchronize()
+    mixed_ms = mix_start.elapsed_time(mix_end) / args.steps
     rates_ms = [a.elapsed_time(b) for a, b in zip(ev_start, ev_mid)]
     transport_ms = [a.elapsed_time(b) for a, b in zip(ev_mid, ev_end)]
     total_ms = ev_start[0].elapsed_time(ev_end[-1])
@@ -221,6 +238,7 @@ def run_ours(args):
 
     # Parity of this run's outputs on a sample of cells against the FP64 oracle.
     parity = None
+    mixed_err = None
     if rank == 0 and not args.no_parity:
         import oracle
         o = oracle.Oracle(m)
@@ -237,6 +255,13 @@ def run_ours(args):
                   "rates_max_err": float((np.abs(gr - rref) / np.maximum(rsc, 1e-300)).max()),
                   "transport_max_err": float((np.abs(gt - tref) / np.maximum(tsc, 1e-300)).max()),
                   "tolerance": 1e-12, "metric": "|gpu - oracle| / condition scale of the output"}
+        mr = m_r_out.index_select(1, ridx).cpu().numpy()
+        mt = m_t_out.index_select(1, ridx).cpu().numpy()
+        er = np.abs(mr - rref) / np.maximum(rsc, 1e-300)
+        et = np.abs(mt - tref) / np.maximum(tsc, 1e-300)
+        mixed_err = {"rates_max_err": float(er.max()), "rates_rms_err": float(np.sqrt((er ** 2).mean())),
+                     "transport_max_err": float(et.max()), "transport_rms_err": float(np.sqrt((et ** 2).mean())),
+                     "tolerance": 1e-4}
 
     # End to end through the public fused call with host buffers.
     h_ro = torch.empty((A + 2, n), dtype=torch.float64).pin_memory().numpy()
@@ -290,6 +315,12 @@ def run_ours(args):
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
             "parity": parity,
+            "forms": {
+                "plain_f64": {"cells_per_s": value, "ms_per_step": ms_per_step,
+                              "max_err": None if parity is None else max(parity["rates_max_err"], parity["transport_max_err"])},
+                "mixed": {"cells_per_s": world * n / (mixed_ms * 1e-3), "ms_per_step": mixed_ms, "error": mixed_err,
+                          "api": "cb_rates_mixed + cb_transport_mixed"},
+            },
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -34,7 +34,8 @@ CB_UNIFORM_PRESSURE = 2
 EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_query", "cb_transport_setup",
            "cb_transport_fit", "cb_transport_coefficients", "cb_rates_f64", "cb_reaction_rates_f64",
            "cb_transport_f64", "cb_rates_transport_f64", "cb_work_model", "cb_synchronize", "cb_last_error",
-           "cb_version", "cb_device_fp64_peak", "cb_fp64_math"]
+           "cb_version", "cb_device_fp64_peak", "cb_fp64_math", "cb_rates_mixed", "cb_transport_mixed",
+           "cb_rates_transport_mixed"]
 
 
 class CombustionError(RuntimeError):
@@ -83,9 +84,10 @@ def lib():
         L.cb_transport_setup.argtypes = [vp, C.c_double, C.c_double, C.c_double]
         L.cb_transport_fit.argtypes = [C.POINTER(cb_mech_desc), C.c_double, vp, vp, vp]
         L.cb_transport_coefficients.argtypes = [vp, vp, vp, vp]
-        for f in ("cb_rates_f64", "cb_reaction_rates_f64", "cb_transport_f64"):
+        for f in ("cb_rates_f64", "cb_reaction_rates_f64", "cb_transport_f64", "cb_rates_mixed", "cb_transport_mixed"):
             getattr(L, f).argtypes = [vp, sz, vp, vp, C.c_uint32, vp]
         L.cb_rates_transport_f64.argtypes = [vp, sz, vp, vp, vp, C.c_uint32, vp]
+        L.cb_rates_transport_mixed.argtypes = [vp, sz, vp, vp, vp, C.c_uint32, vp]
         L.cb_work_model.argtypes = [vp, C.POINTER(cb_work), C.POINTER(cb_work)]
         L.cb_synchronize.argtypes = [vp, vp]
         L.cb_last_error.restype = C.c_char_p
@@ -237,26 +239,30 @@ class Mechanism:
         _check(fn(self.h, n, _ptr_array(ins), _ptr_array(outs), flags, None if flags & CB_HOST_MEMORY else self._stream(stream)))
         return outputs
 
-    def rates(self, inputs, outputs, uniform_pressure=False, stream=None):
-        """inputs [K+3]: P/R, R/P, T, V, n_0..n_{K-2}; outputs [A+2]: dT/dt, dV/dt, wdot_0..wdot_{A-1}."""
-        return self._call(lib().cb_rates_f64, inputs, outputs, CB_UNIFORM_PRESSURE if uniform_pressure else 0, stream)
+    def rates(self, inputs, outputs, uniform_pressure=False, stream=None, mixed=False):
+        """inputs [K+3]: P/R, R/P, T, V, n_0..n_{K-2}; outputs [A+2]: dT/dt, dV/dt, wdot_0..wdot_{A-1}.
+        mixed=True: the mixed-precision form (cb_rates_mixed)."""
+        fn = lib().cb_rates_mixed if mixed else lib().cb_rates_f64
+        return self._call(fn, inputs, outputs, CB_UNIFORM_PRESSURE if uniform_pressure else 0, stream)
 
     def reaction_rates(self, inputs, outputs, stream=None):
         """inputs [K+2]: P/R, T, V, n_0..n_{K-2}; outputs [R]: rate of progress of each reaction."""
         return self._call(lib().cb_reaction_rates_f64, inputs, outputs, 0, stream)
 
-    def transport(self, inputs, outputs, stream=None):
+    def transport(self, inputs, outputs, stream=None, mixed=False):
         """inputs [K+1]: sum n, T/T0, n_0..n_{K-2}; outputs [K+2]: lambda/lambda0, mu/mu0, rhoD_k/mu0."""
-        return self._call(lib().cb_transport_f64, inputs, outputs, 0, stream)
+        fn = lib().cb_transport_mixed if mixed else lib().cb_transport_f64
+        return self._call(fn, inputs, outputs, 0, stream)
 
-    def rates_transport(self, inputs, rates_out, transport_out, stream=None):
+    def rates_transport(self, inputs, rates_out, transport_out, stream=None, mixed=False):
         """Both paths on the same cells (transport at sum n = P/R V / T, T/T0)."""
         ins, _ = self._rows(inputs)
         ro, n = self._rows(rates_out)
         to, _ = self._rows(transport_out)
         flags = CB_HOST_MEMORY if self._is_host(rates_out) else 0
-        _check(lib().cb_rates_transport_f64(self.h, n, _ptr_array(ins), _ptr_array(ro), _ptr_array(to), flags,
-                                            None if flags else self._stream(stream)))
+        fn = lib().cb_rates_transport_mixed if mixed else lib().cb_rates_transport_f64
+        _check(fn(self.h, n, _ptr_array(ins), _ptr_array(ro), _ptr_array(to), flags,
+                  None if flags else self._stream(stream)))
         return rates_out, transport_out
 
 

@@ -17,6 +17,8 @@ struct cb_mech {
     int kmax = 0;
     uint8_t* d_rates = nullptr;      // rates table blob
     uint8_t* d_transport = nullptr;  // transport table blob
+    uint8_t* d_rates_mixed = nullptr;      // tables of the mixed-precision form
+    uint8_t* d_transport_mixed = nullptr;
     int* d_status = nullptr;         // kernel status bits
     // Device staging for CB_HOST_MEMORY calls: two slots, each holding one chunk of inputs and outputs.
     double* d_stage = nullptr;
@@ -51,7 +53,7 @@ int check_status(cb_mech* m) {
     return CB_OK;
 }
 
-enum class Path { Rates, ReactionRates, Transport, Fused };
+enum class Path { Rates, ReactionRates, Transport, Fused, RatesMixed, TransportMixed, FusedMixed };
 
 template <template <int> class Args, int KM>
 int fill_and_launch(cb_mech* m, size_t n, const double* const* in, int ni, double* const* out, int no,
@@ -104,31 +106,52 @@ int launch_path(cb_mech* m, Path path, size_t n, const double* const* in, double
         return dispatch<cbg::TransportArgs>(m, n, in, K + 3, out + (A + 2), K + 2, flags | cbg::kFromRates, st,
                                             cbg::launch_transport, m->d_transport, tb, "transport kernel");
     }
+    case Path::RatesMixed:
+        return dispatch<cbg::RatesArgs>(m, n, in, K + 3, out, A + 2, flags, st, cbg::launch_rates_mixed,
+                                        m->d_rates_mixed, m->host.rates_mixed_blob.size(), "mixed rates kernel");
+    case Path::TransportMixed:
+        return dispatch<cbg::TransportArgs>(m, n, in, K + 1, out, K + 2, flags, st, cbg::launch_transport_mixed,
+                                            m->d_transport_mixed, m->host.transport_mixed_blob.size(),
+                                            "mixed transport kernel");
+    case Path::FusedMixed: {
+        int rc = dispatch<cbg::RatesArgs>(m, n, in, K + 3, out, A + 2, flags, st, cbg::launch_rates_mixed,
+                                          m->d_rates_mixed, m->host.rates_mixed_blob.size(), "mixed rates kernel");
+        if (rc) return rc;
+        return dispatch<cbg::TransportArgs>(m, n, in, K + 3, out + (A + 2), K + 2, flags | cbg::kFromRates, st,
+                                            cbg::launch_transport_mixed, m->d_transport_mixed,
+                                            m->host.transport_mixed_blob.size(), "mixed transport kernel");
+    }
     }
     return fail(CB_ERR_INVALID, "unknown path");
 }
 
 int n_inputs(const cb_mech* m, Path p) {
     switch (p) {
-    case Path::Rates: case Path::Fused: return m->host.K + 3;
+    case Path::Rates: case Path::Fused: case Path::RatesMixed: case Path::FusedMixed: return m->host.K + 3;
     case Path::ReactionRates: return m->host.K + 2;
     default: return m->host.K + 1;
     }
 }
 int n_outputs(const cb_mech* m, Path p) {
     switch (p) {
-    case Path::Rates: return m->host.A + 2;
+    case Path::Rates: case Path::RatesMixed: return m->host.A + 2;
     case Path::ReactionRates: return m->host.R;
-    case Path::Fused: return m->host.A + 2 + m->host.K + 2;
+    case Path::Fused: case Path::FusedMixed: return m->host.A + 2 + m->host.K + 2;
     default: return m->host.K + 2;
     }
+}
+bool rates_layout(Path p) {
+    return p == Path::Rates || p == Path::Fused || p == Path::RatesMixed || p == Path::FusedMixed;
+}
+bool needs_transport(Path p) {
+    return p == Path::Transport || p == Path::Fused || p == Path::TransportMixed || p == Path::FusedMixed;
 }
 
 // Host arrays: copy chunks through two device staging slots so that the copies of one chunk overlap
 // the kernel of the other (one cudaMemcpyAsync per array per chunk).
 int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags) {
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
-    const bool uniform = (path == Path::Rates || path == Path::Fused) && (flags & CB_UNIFORM_PRESSURE);
+    const bool uniform = rates_layout(path) && (flags & CB_UNIFORM_PRESSURE);
     size_t chunk = (size_t)1 << 20;
     if (chunk > n) chunk = n;
     const size_t per_slot = (size_t)(ni + no) * chunk + 2;
@@ -173,9 +196,9 @@ int call(cb_mech* m, Path path, size_t n, const double* const* inputs, double* c
          void* stream) {
     if (!m || !inputs || !outputs) return fail(CB_ERR_INVALID, "null argument");
     if (flags & ~(CB_HOST_MEMORY | CB_UNIFORM_PRESSURE)) return fail(CB_ERR_INVALID, "unknown flag");
-    if ((flags & CB_UNIFORM_PRESSURE) && path != Path::Rates && path != Path::Fused)
+    if ((flags & CB_UNIFORM_PRESSURE) && !rates_layout(path))
         return fail(CB_ERR_INVALID, "CB_UNIFORM_PRESSURE applies to the rates inputs only");
-    if ((path == Path::Transport || path == Path::Fused) && !m->host.transport_ready)
+    if (needs_transport(path) && !m->host.transport_ready)
         return fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
     if (n == 0) return CB_OK;
@@ -205,11 +228,15 @@ int cb_mech_create(const cb_mech_desc* desc, cb_mech** out) {
     std::string err;
     int rc = cbg::build_mechanism(desc, m->host, err);
     if (rc) { delete m; return fail(rc, err); }
-    m->kmax = cbg::kmax_for(m->host.K);
-    if (!m->kmax) { delete m; return fail(CB_ERR_UNSUPPORTED, "more than 256 species"); }
+    m->kmax = cbg::kmax_for(m->host.K, m->host.n_eff);
+    if (!m->kmax) { delete m; return fail(CB_ERR_UNSUPPORTED, "more than 256 species or 1024 third-body reactions"); }
     cudaError_t e = cudaGetDevice(&m->device);
     if (e == cudaSuccess) e = cudaMalloc(&m->d_rates, m->host.rates_blob.size());
     if (e == cudaSuccess) e = cudaMemcpy(m->d_rates, m->host.rates_blob.data(), m->host.rates_blob.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_rates_mixed, m->host.rates_mixed_blob.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(m->d_rates_mixed, m->host.rates_mixed_blob.data(), m->host.rates_mixed_blob.size(),
+                       cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, sizeof(int));
     if (e != cudaSuccess) { cb_mech_destroy(m); return cuda_fail(e, "mechanism upload"); }
@@ -222,7 +249,7 @@ int cb_mech_validate(const cb_mech_desc* desc, cb_mech_info* info) {
     std::string err;
     int rc = cbg::build_mechanism(desc, h, err);
     if (rc) return fail(rc, err);
-    if (!cbg::kmax_for(h.K)) return fail(CB_ERR_UNSUPPORTED, "more than 256 species");
+    if (!cbg::kmax_for(h.K, h.n_eff)) return fail(CB_ERR_UNSUPPORTED, "more than 256 species or 1024 third-body reactions");
     if (info) {
         std::memset(info, 0, sizeof *info);
         info->n_species = h.K; info->n_active = h.A; info->n_reactions = h.R;
@@ -254,6 +281,8 @@ int cb_mech_destroy(cb_mech* m) {
     }
     cudaFree(m->d_rates);
     cudaFree(m->d_transport);
+    cudaFree(m->d_rates_mixed);
+    cudaFree(m->d_transport_mixed);
     cudaFree(m->d_status);
     cudaFree(m->d_stage);
     delete m;
@@ -284,9 +313,17 @@ int cb_transport_setup(cb_mech* m, double T0, double viscosity0, double conducti
     int rc = cbg::build_transport(m->host, T0, viscosity0, conductivity0, err);
     if (rc) return fail(rc, err);
     CB_CUDA(cudaSetDevice(m->device));
-    if (m->d_transport) { CB_CUDA(cudaDeviceSynchronize()); cudaFree(m->d_transport); m->d_transport = nullptr; }
+    if (m->d_transport || m->d_transport_mixed) {
+        CB_CUDA(cudaDeviceSynchronize());
+        cudaFree(m->d_transport);
+        cudaFree(m->d_transport_mixed);
+        m->d_transport = m->d_transport_mixed = nullptr;
+    }
     CB_CUDA(cudaMalloc(&m->d_transport, m->host.transport_blob.size()));
     CB_CUDA(cudaMemcpy(m->d_transport, m->host.transport_blob.data(), m->host.transport_blob.size(), cudaMemcpyHostToDevice));
+    CB_CUDA(cudaMalloc(&m->d_transport_mixed, m->host.transport_mixed_blob.size()));
+    CB_CUDA(cudaMemcpy(m->d_transport_mixed, m->host.transport_mixed_blob.data(), m->host.transport_mixed_blob.size(),
+                       cudaMemcpyHostToDevice));
     return CB_OK;
 }
 
@@ -312,6 +349,24 @@ int cb_reaction_rates_f64(cb_mech* m, size_t n, const double* const* inputs, dou
 int cb_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
                      void* stream) {
     return call(m, Path::Transport, n, inputs, outputs, flags, stream);
+}
+
+int cb_rates_mixed(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+                   void* stream) {
+    return call(m, Path::RatesMixed, n, inputs, outputs, flags, stream);
+}
+
+int cb_transport_mixed(cb_mech* m, size_t n, const double* const* inputs, double* const* outputs, uint32_t flags,
+                       void* stream) {
+    return call(m, Path::TransportMixed, n, inputs, outputs, flags, stream);
+}
+
+int cb_rates_transport_mixed(cb_mech* m, size_t n, const double* const* inputs, double* const* rates_out,
+                             double* const* transport_out, uint32_t flags, void* stream) {
+    if (!m || !rates_out || !transport_out) return fail(CB_ERR_INVALID, "null argument");
+    std::vector<double*> outs(rates_out, rates_out + m->host.A + 2);
+    outs.insert(outs.end(), transport_out, transport_out + m->host.K + 2);
+    return call(m, Path::FusedMixed, n, inputs, outs.data(), flags, stream);
 }
 
 int cb_rates_transport_f64(cb_mech* m, size_t n, const double* const* inputs, double* const* rates_out,

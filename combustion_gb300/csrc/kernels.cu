@@ -8,30 +8,12 @@
 #include <stdint.h>
 
 #include "device_common.cuh"
-#include "fp64_math.cuh"
+#include "device_math.cuh"
 #include "kernels.h"
 #include "tables.h"
 
 namespace cbg {
 
-constexpr double kF32Max = 3.4028234663852886e+38;     // f32::MAX as f64
-constexpr double kF32MinPos = 1.1754943508222875e-38;  // f32::MIN_POSITIVE as f64
-
-// Per-block copy of the elementary-function tables (lane-divergent lookups).
-__shared__ MathTables s_math;
-
-__device__ __forceinline__ double exp64(double x) { return exp_fast(x, s_math.exp2j); }
-__device__ __forceinline__ double log64(double x) { return log_fast(x, s_math); }
-__device__ __forceinline__ double rcp64(double x) { return rcp_fast(x); }
-__device__ __forceinline__ double div64(double a, double b) { return div_fast(a, b); }
-
-// Copies the math tables of a blob (byte offset off_math) into s_math; call before any use.
-__device__ __forceinline__ void load_math(const uint8_t* gtab, int off_math) {
-    const double* src = reinterpret_cast<const double*>(gtab + off_math);
-    double* dst = reinterpret_cast<double*>(&s_math);
-    for (int q = threadIdx.x; q < (int)(sizeof(MathTables) / sizeof(double)); q += blockDim.x) dst[q] = src[q];
-    __syncthreads();
-}
 
 struct Temps {
     double lnT, T, T2, T3, T4, rcpT, rcpT2;
@@ -85,7 +67,18 @@ struct Cell {
     double Ctot, C0, rcpC0;
     double C[KMAX];              // concentrations, bulk last
     double ex[KMAX], exn[KMAX];  // min(M3, exp(g_k)), min(cbrt(f32::MAX), exp(-g_k))
+    double M[4 * KMAX];          // third-body concentrations C + sum (e_k - 1) C_k, one per efficiency row
 };
+
+// (double)v for a small integer with integer instructions only (no FP64 conversion on the FP64 pipe).
+__device__ __forceinline__ double small_int_to_double(int v) {
+    if (v == 0) return 0.0;
+    const unsigned a = v < 0 ? (unsigned)(-v) : (unsigned)v;
+    const int e = 31 - __clz(a);
+    const unsigned long long mant = (unsigned long long)(a ^ (1u << e)) << (52 - e);
+    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
+}
 
 // Prologue of reaction.rs:362-373 and the Gibbs exponentials of reaction.rs:234-263.
 template <int KMAX>
@@ -119,6 +112,30 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
         if (s.need_exp) c.ex[k] = min_pos(H.M3, exp64(x));
         if (s.need_exp_neg) c.exn[k] = min_pos(H.cbrt_max, exp64(-x));
     }
+    // efficiency() of every third-body / falloff reaction (reaction.rs:141-145), four rows per pass over
+    // the concentrations (rows padded to a multiple of 4): one local load of C_k per four FMAs.
+    for (int e0 = 0; e0 < H.n_eff; e0 += 4) {
+        const double* E = tb.eff + (size_t)e0 * K;
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = 0; k < K; k++) {
+            const double ck = c.C[k];
+#pragma unroll
+            for (int q = 0; q < 4; q++) s[q] = fma(E[q * K + k], ck, s[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e0 + q < H.n_eff) c.M[e0 + q] = c.Ctot + s[q];
+    }
+}
+
+// Product of concentrations with multiplicities (product_of_exponentiations, reaction.rs:53-63),
+// seeded with the first factor.
+__device__ __forceinline__ double conc_product(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
+    double p = C[ks[0]];
+    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+    for (int q = 1; q < n; q++)
+        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
+    return p;
 }
 
 // cR of one reaction (reaction.rs:149-309): forward rate constant (with third-body efficiency and
@@ -126,22 +143,8 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
 template <int KMAX>
 __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const Cell<KMAX>& c) {
     const RatesHeader& H = *tb.H;
-    const int K = H.K;
     const Temps& t = c.t;
-    double M = c.Ctot;
-    if (x.eff_row >= 0) {  // efficiency() (reaction.rs:141-145)
-        const double* e = tb.eff + (size_t)x.eff_row * K;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // four independent chains
-        int k = 0;
-        for (; k + 3 < K; k += 4) {
-            s0 = fma(e[k], c.C[k], s0);
-            s1 = fma(e[k + 1], c.C[k + 1], s1);
-            s2 = fma(e[k + 2], c.C[k + 2], s2);
-            s3 = fma(e[k + 3], c.C[k + 3], s3);
-        }
-        for (; k < K; k++) s0 = fma(e[k], c.C[k], s0);
-        M = c.Ctot + ((s0 + s1) + (s2 + s3));
-    }
+    const double M = x.eff_row >= 0 ? c.M[x.eff_row] : c.Ctot;
     double num, den = 1.0;
     bool ratio = false;
     if (x.model == 4) {  // Troe (reaction.rs:160-193)
@@ -187,16 +190,19 @@ __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Rea
         if (x.model == 2) num *= M;  // three-body (reaction.rs:152)
     }
     // Rate of progress (reaction.rs:269-306).
-    double Rf = 1.0;
-    for (int q = 0; q < x.n_r; q++)
-        for (int n = 0; n < x.r_n[q]; n++) Rf *= c.C[x.r_k[q]];
+    const double Rf = conc_product(c.C, x.r_k, x.r_n, x.n_r);
     double Rnet = Rf;
     if (x.model != 1) {
-        double p = 1.0;
+        // 1/Kc: product of the cached Gibbs exponentials, repeated |nu| times, in species order.
+        double p = 0.0;
+        bool first = true;
         for (int q = 0; q < x.n_net; q++) {
             const int nu = x.net_n[q], k = x.net_k[q];
             const double tt = nu > 0 ? c.ex[k] : c.exn[k];
-            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) {
+                p = first ? tt : p * tt;
+                first = false;
+            }
         }
         switch (x.minus_sigma_net) {
         case 1: p = c.C0 * p; break;
@@ -204,10 +210,7 @@ __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Rea
         case -2: p = (c.rcpC0 * c.rcpC0) * p; break;
         default: break;
         }
-        double Rr = 1.0;
-        for (int q = 0; q < x.n_p; q++)
-            for (int n = 0; n < x.p_n[q]; n++) Rr *= c.C[x.p_k[q]];
-        Rnet = Rf - p * Rr;
+        Rnet = fma(-p, conc_product(c.C, x.p_k, x.p_n, x.n_p), Rf);
     }
     return ratio ? div64(Rnet * num, den) : Rnet * num;
 }
@@ -227,7 +230,8 @@ __device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, siz
     for (int r = 0; r < H.R; r++) {  // species_rates (reaction.rs:312-327)
         const Reaction& x = tb.reactions[r];
         const double cR = reaction_rate<KMAX>(tb, x, c);
-        for (int q = 0; q < x.n_net; q++) wdot[x.net_k[q]] = fma((double)x.net_n[q], cR, wdot[x.net_k[q]]);
+        for (int q = 0; q < x.n_net; q++)
+            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
     }
     // Energy and volume (reaction.rs:375-384).
     double E = 0.0;

@@ -40,7 +40,12 @@ struct TransportArgs {
 };
 
 // Smallest compiled capacity holding K species (0 if none).
-inline int kmax_for(int K) { return K <= 16 ? 16 : K <= 64 ? 64 : K <= 256 ? 256 : 0; }
+// (The per-cell efficiency sums of up to 4 * KMAX third-body / falloff reactions are kept per thread.)
+inline int kmax_for(int K, int n_eff) {
+    for (int km : {16, 64, 256})
+        if (K <= km && n_eff <= 4 * km) return km;
+    return 0;
+}
 
 int max_table_smem();
 cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, double* y, size_t n,
@@ -49,6 +54,10 @@ cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const
                          cudaStream_t st, int* status);
 cudaError_t launch_reaction_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
                                   cudaStream_t st, int* status);
+cudaError_t launch_rates_mixed(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                               cudaStream_t st, int* status);
+cudaError_t launch_transport_mixed(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                                   cudaStream_t st, int* status);
 cudaError_t launch_transport(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
                              cudaStream_t st, int* status);
 

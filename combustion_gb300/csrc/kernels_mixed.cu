@@ -1,0 +1,386 @@
+// Mixed-precision kernels: the same programs as kernels.cu (reaction.rs:207-391, transport.rs:141-210)
+// with FP64 kept only where the reference's values cancel:
+//   FP64  Gibbs polynomials and exponentials of the equilibrium constant, the forward-minus-reverse rate
+//         of progress, the accumulation into species rates (and the energy dot products over them)
+//   FP32  Arrhenius exponentials (argument and exponential; the result stored as a double so that it
+//         keeps the full range), third-body sums, falloff blending, h/RT and cp/R polynomials, and all of
+//         transport (polynomial fits, Wilke mixing, conductivity, mixture diffusion)
+// Conversions between the two formats use integer instructions (device_math.cuh): the FP64 pipe is the
+// bottleneck of the rates kernel and the FP32 pipe that of transport.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "device_math.cuh"
+#include "kernels.h"
+#include "tables_mixed.h"
+
+namespace cbg {
+
+struct RatesMixedTables {
+    const RatesMixedHeader* H;
+    const SpeciesF* species;
+    const ReactionF* reactions;
+    const FalloffF* falloff;
+    const float* eff;
+    __device__ explicit RatesMixedTables(const uint8_t* tab)
+        : H(reinterpret_cast<const RatesMixedHeader*>(tab)),
+          species(reinterpret_cast<const SpeciesF*>(tab + H->off_species)),
+          reactions(reinterpret_cast<const ReactionF*>(tab + H->off_reactions)),
+          falloff(reinterpret_cast<const FalloffF*>(tab + H->off_falloff)),
+          eff(reinterpret_cast<const float*>(tab + H->off_eff)) {}
+};
+
+__device__ __forceinline__ int piece_of_m(double split, double T) {
+    return __double_as_longlong(T) <= __double_as_longlong(split) ? 0 : 1;
+}
+
+// min(f32::MAX, k) of reaction.rs:138 with k = exp(b lnT - Ea/T + ln A) evaluated in FP32.
+__device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, float rcpT) {
+    if (!a.has_x) return min_pos(kF32Max, a.A);
+    return min_pos(kF32Max, exp_f32x(fmaf(a.b, lnT, fmaf(a.mEa, rcpT, a.lnA))));
+}
+
+__device__ __forceinline__ double conc_product_m(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
+    double p = C[ks[0]];
+    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+    for (int q = 1; q < n; q++)
+        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
+    return p;
+}
+
+__device__ __forceinline__ double int_to_double_small(int v) {
+    if (v == 0) return 0.0;
+    const unsigned a = v < 0 ? (unsigned)(-v) : (unsigned)v;
+    const int e = 31 - __clz(a);
+    const unsigned long long mant = (unsigned long long)(a ^ (1u << e)) << (52 - e);
+    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
+}
+
+template <int KMAX>
+__device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMAX>& io, size_t i) {
+    const RatesMixedHeader& H = *tb.H;
+    const int K = H.K, A = H.A;
+    const bool uniform = io.flags & kUniformPressure;
+    const double pressure_R = uniform ? io.in[0][0] : io.in[0][i];
+    const double rcp_pressure_R = uniform ? io.in[1][0] : io.in[1][i];
+    const double T = io.in[2][i], V = io.in[3][i];
+    // FP64 prologue (reaction.rs:362-373): temperatures for the Gibbs polynomials, concentrations for
+    // the rates of progress.
+    const double md = rcp64(V), rcpT = rcp64(T), lnT = log64(T);
+    const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
+    double C[KMAX];
+    float Cf[KMAX];
+    double sum = 0.0;
+    for (int k = 0; k < K - 1; k++) {
+        C[k] = md * max0(io.in[4 + k][i]);
+        sum += C[k];
+        Cf[k] = dbl_to_flt(C[k]);
+    }
+    const double Ctot = pressure_R * rcpT;
+    C[K - 1] = Ctot - sum;
+    Cf[K - 1] = dbl_to_flt(C[K - 1]);
+    const float Ctotf = dbl_to_flt(Ctot), Tf = dbl_to_flt(T), lnTf = dbl_to_flt(lnT), rcpTf = dbl_to_flt(rcpT);
+    const double C0 = H.C0 * rcpT, rcpC0 = H.rcp_C0 * T;
+
+    // FP64 Gibbs exponentials (reaction.rs:234-263).
+    double ex[KMAX], exn[KMAX];
+    for (int k = 0; k < A; k++) {
+        const SpeciesF& s = tb.species[k];
+        if (!(s.need_exp | s.need_exp_neg)) continue;
+        const double* g = s.g[piece_of_m(s.split, T)];
+        const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
+        if (s.need_exp) ex[k] = min_pos(H.M3, exp64(x));
+        if (s.need_exp_neg) exn[k] = min_pos(H.cbrt_max, exp64(-x));
+    }
+    // FP32 third-body sums, four rows per pass.
+    float Mf[4 * KMAX];
+    for (int e0 = 0; e0 < H.n_eff; e0 += 4) {
+        const float* E = tb.eff + (size_t)e0 * K;
+        float s[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < K; k++) {
+            const float ck = Cf[k];
+#pragma unroll
+            for (int q = 0; q < 4; q++) s[q] = fmaf(E[q * K + k], ck, s[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (e0 + q < H.n_eff) Mf[e0 + q] = Ctotf + s[q];
+    }
+
+    double wdot[KMAX];
+    for (int k = 0; k < A; k++) wdot[k] = 0.0;
+    for (int r = 0; r < H.R; r++) {
+        const ReactionF& x = tb.reactions[r];
+        const float Mr = x.eff_row >= 0 ? Mf[x.eff_row] : Ctotf;
+        double kf;  // forward rate coefficient including third body and falloff
+        if (x.model == 4) {  // Troe, blending in FP32 (reaction.rs:160-193)
+            const FalloffF& f = tb.falloff[x.falloff];
+            const double k0 = arrhenius_f(f.k0, lnTf, rcpTf);
+            const double Md = flt_to_dbl(Mr);
+            double Pr, kinf;
+            if (f.flags & kKinfConst) {
+                Pr = Md * k0;
+                kinf = f.ainf;
+            } else {
+                const double ki = arrhenius_f(x.k, lnTf, rcpTf);
+                Pr = (Md * k0) * rcp64(ki + kF32MinPos);
+                kinf = f.ainf * ki;
+            }
+            float lnF;
+            if (f.flags & kFcentConst) {
+                lnF = f.ln_fcent;
+            } else {
+                float F = 0.f;
+                if (f.flags & kTermT3) F = f.c1mA * expf(Tf * f.c3);
+                if (f.flags & kTermT1) F += f.cA * expf(Tf * f.c1);
+                if (f.flags & kTermAConst) F += f.cA;
+                if (f.flags & kTermT2) F += expf(f.cmT2 * rcpTf);
+                lnF = logf(F);
+            }
+            const float Cc = fmaf(-0.67f, lnF, -H.ln10_04);
+            const float Nn = fmaf(-1.27f, lnF, H.ln10_075);
+            const float lnPrC = log_dbl_f32(Pr + kF32MinPos) + Cc;
+            const float f1 = __fdividef(lnPrC, fmaf(-0.14f, lnPrC, Nn));
+            const float Fb = expf(__fdividef(lnF, fmaf(f1, f1, 1.f)));
+            kf = (flt_to_dbl(Fb) * kinf) * (Pr * rcp64(Pr + 1.0));
+        } else if (x.model == 3) {  // Lindemann (reaction.rs:153-159)
+            const FalloffF& f = tb.falloff[x.falloff];
+            const double Ck0 = flt_to_dbl(Mr) * arrhenius_f(f.k0, lnTf, rcpTf);
+            const double ki = arrhenius_f(x.k, lnTf, rcpTf);
+            kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
+        } else {
+            kf = arrhenius_f(x.k, lnTf, rcpTf);
+            if (x.model == 2) kf *= flt_to_dbl(Mr);
+        }
+        // FP64 rate of progress (reaction.rs:269-306) and accumulation (reaction.rs:312-327).
+        const double Rf = conc_product_m(C, x.r_k, x.r_n, x.n_r);
+        double Rnet = Rf;
+        if (x.model != 1) {
+            double p = 0.0;
+            bool first = true;
+            for (int q = 0; q < x.n_net; q++) {
+                const int nu = x.net_n[q], k = x.net_k[q];
+                const double tt = nu > 0 ? ex[k] : exn[k];
+                for (int n = 0; n < (nu > 0 ? nu : -nu); n++) {
+                    p = first ? tt : p * tt;
+                    first = false;
+                }
+            }
+            switch (x.minus_sigma_net) {
+            case 1: p = C0 * p; break;
+            case -1: p = rcpC0 * p; break;
+            case -2: p = (rcpC0 * rcpC0) * p; break;
+            default: break;
+            }
+            Rnet = fma(-p, conc_product_m(C, x.p_k, x.p_n, x.n_p), Rf);
+        }
+        const double cR = kf * Rnet;
+        for (int q = 0; q < x.n_net; q++)
+            wdot[x.net_k[q]] = fma(int_to_double_small(x.net_n[q]), cR, wdot[x.net_k[q]]);
+    }
+    // Energy (reaction.rs:375-384): FP32 polynomials, FP64 sums over the FP64 species rates.
+    double E = 0.0, Cp = 0.0, dtE = 0.0;
+    for (int k = 0; k < K; k++) {
+        const SpeciesF& s = tb.species[k];
+        const int p = piece_of_m(s.split, T);
+        const float* cp = s.cp[p];
+        const float ck = fmaf(cp[4], Tf, cp[3]);
+        const float cpk = fmaf(fmaf(fmaf(ck, Tf, cp[2]), Tf, cp[1]), Tf, cp[0]);
+        Cp = fma(flt_to_dbl(cpk), C[k], Cp);
+        if (k < A) {
+            const float* h = s.h[p];
+            const float hk = fmaf(h[5], rcpTf, fmaf(fmaf(fmaf(fmaf(h[4], Tf, h[3]), Tf, h[2]), Tf, h[1]), Tf, h[0]));
+            E = fma(wdot[k], flt_to_dbl(hk), E);
+            dtE = fma(s.dtE, wdot[k], dtE);
+        }
+    }
+    const double dtT_T = -E * rcp64(Cp);
+    io.out[0][i] = T * dtT_T;
+    io.out[1][i] = V * fma(rcp_pressure_R * T, dtE, dtT_T);
+    for (int k = 0; k < A; k++) io.out[2 + k][i] = wdot[k];
+}
+
+template <int KMAX, bool SMEM>
+__global__ void __launch_bounds__(kBlock) rates_mixed_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
+                                                            const __grid_constant__ RatesArgs<KMAX> io, size_t n,
+                                                            int* status) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint64_t bar;
+    load_math(gtab, reinterpret_cast<const RatesMixedHeader*>(gtab)->off_math);
+    const uint8_t* tab = gtab;
+    if (SMEM) {
+        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
+        tab = smem;
+    }
+    const RatesMixedTables tb(tab);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        rates_mixed_cell<KMAX>(tb, io, i);
+}
+
+// ---------------------------------------------------------------------------------------------------
+template <int KMAX>
+__device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i) {
+    const TransportMixedHeader& H = *reinterpret_cast<const TransportMixedHeader*>(tab);
+    const float* cond = reinterpret_cast<const float*>(tab + H.off_cond);
+    const float* visc = reinterpret_cast<const float*>(tab + H.off_visc);
+    const float* W = reinterpret_cast<const float*>(tab + H.off_W);
+    const float* diff = reinterpret_cast<const float*>(tab + H.off_diff);
+    const float* A2 = reinterpret_cast<const float*>(tab + H.off_A2);
+    const float* AB = reinterpret_cast<const float*>(tab + H.off_AB);
+    const float* B2 = reinterpret_cast<const float*>(tab + H.off_B2);
+    const int K = H.K;
+    float N, Tn;
+    const double* const* amounts;
+    if (io.flags & kFromRates) {
+        const double pressure_R = (io.flags & kUniformPressure) ? io.in[0][0] : io.in[0][i];
+        const float T = dbl_to_flt(io.in[2][i]);
+        N = __fdividef(dbl_to_flt(pressure_R) * dbl_to_flt(io.in[3][i]), T);
+        Tn = T / (float)H.T0;
+        amounts = io.in + 4;
+    } else {
+        N = dbl_to_flt(io.in[0][i]);
+        Tn = dbl_to_flt(io.in[1][i]);
+        amounts = io.in + 2;
+    }
+    const float L1 = logf(Tn), L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
+    auto poly = [&](const float* P) { return fmaf(P[4], L4, fmaf(P[3], L3, fmaf(P[2], L2, fmaf(P[1], L1, P[0])))); };
+
+    float X[KMAX], v[KMAX], Y[KMAX], Z[KMAX];
+    // sum of the non-bulk amounts with an error term (Kahan): the bulk amount is a difference
+    float s = 0.f, comp = 0.f;
+    for (int k = 0; k < K - 1; k++) {
+        X[k] = dbl_to_flt(amounts[k][i]);
+        const float y = X[k] - comp, t = s + y;
+        comp = (t - s) - y;
+        s = t;
+    }
+    X[K - 1] = (N - s) + comp;
+    const float VT = sqrtf(Tn);
+    float MN = 0.f;
+    for (int k = 0; k < K; k++) MN = fmaf(W[k], X[k], MN);
+    const float MVTN = MN * VT;
+
+    float Ac = 0.f, Bc = 0.f;
+    for (int k = 0; k < K; k++) {
+        const float c = poly(cond + 5 * k);
+        Ac = fmaf(X[k], c, Ac);
+        Bc = fmaf(X[k], rcp_f32(c), Bc);
+    }
+    io.out[0][i] = flt_to_dbl((__fdividef(Ac, N) + __fdividef(N, Bc)) * VT);
+
+    for (int k = 0; k < K; k++) {
+        v[k] = poly(visc + 5 * k);
+        const float r = rcp_f32(v[k]);
+        Y[k] = X[k] * r;
+        Z[k] = Y[k] * r;
+    }
+    float mu = 0.f;
+    for (int k0 = 0; k0 < K; k0 += 4) {
+        const float* a2 = A2 + (size_t)k0 * K;
+        const float* ab = AB + (size_t)k0 * K;
+        const float* b2 = B2 + (size_t)k0 * K;
+        float s1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f}, s3[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int j = 0; j < K; j++) {
+            const float xj = X[j], yj = Y[j], zj = Z[j];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                s1[q] = fmaf(a2[q * K + j], xj, s1[q]);
+                s2[q] = fmaf(ab[q * K + j], yj, s2[q]);
+                s3[q] = fmaf(b2[q * K + j], zj, s3[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = k0 + q;
+            if (k < K) mu = fmaf(X[k] * (v[k] * v[k]), rcp_f32(fmaf(v[k], fmaf(v[k], s3[q], s2[q]), s1[q])), mu);
+        }
+    }
+    io.out[1][i] = flt_to_dbl(VT * mu);
+
+    float* S = Y;
+    for (int k = 0; k < K; k++) S[k] = 0.f;
+    const float* P = diff;
+    for (int k = 1; k < K; k++) {
+        const float xk = X[k];
+        float sa = 0.f, sb = 0.f;
+        int j = 0;
+        for (; j + 1 < k; j += 2, P += 10) {
+            const float Ra = rcp_f32(poly(P)), Rb = rcp_f32(poly(P + 5));
+            sa = fmaf(X[j], Ra, sa);
+            sb = fmaf(X[j + 1], Rb, sb);
+            S[j] = fmaf(xk, Ra, S[j]);
+            S[j + 1] = fmaf(xk, Rb, S[j + 1]);
+        }
+        if (j < k) {
+            const float R = rcp_f32(poly(P));
+            sa = fmaf(X[j], R, sa);
+            S[j] = fmaf(xk, R, S[j]);
+            P += 5;
+        }
+        S[k] += sa + sb;
+    }
+    for (int k = 0; k < K; k++) io.out[2 + k][i] = flt_to_dbl(__fdividef(fmaf(-(VT * W[k]), X[k], MVTN), S[k]));
+}
+
+template <int KMAX, bool SMEM>
+__global__ void __launch_bounds__(kTransportBlock) transport_mixed_kernel(const uint8_t* __restrict__ gtab,
+                                                                         uint32_t tab_bytes,
+                                                                         const __grid_constant__ TransportArgs<KMAX> io,
+                                                                         size_t n, int* status) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint64_t bar;
+    const uint8_t* tab = gtab;
+    if (SMEM) {
+        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
+        tab = smem;
+    }
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        transport_mixed_cell<KMAX>(tab, io, i);
+}
+
+// ---------------------------------------------------------------------------------------------------
+namespace {
+template <int BLOCK, class Args, class KS, class KG>
+cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io, size_t n,
+                         cudaStream_t st, int* status) {
+    const bool smem = (int)tab_bytes <= max_table_smem();
+    int per_sm = 1, dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t want = (n + BLOCK - 1) / BLOCK;
+    if (smem) {
+        cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
+        if (e != cudaSuccess) return e;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, 0);
+    }
+    if (per_sm < 1) per_sm = 1;
+    size_t grid = (size_t)sms * per_sm;
+    if (want < grid) grid = want ? want : 1;
+    if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, BLOCK, 0, st>>>(tab, tab_bytes, io, n, status);
+    return cudaGetLastError();
+}
+}  // namespace
+
+#define CB_DISPATCH_M(FN, KERNEL, ARGS, BLOCK)                                                             \
+    cudaError_t FN(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,            \
+                   cudaStream_t st, int* status) {                                                         \
+        switch (kmax) {                                                                                    \
+        case 16: return launch_mixed<BLOCK>(KERNEL<16, true>, KERNEL<16, false>, tab, tab_bytes,           \
+                                            *static_cast<const ARGS<16>*>(args), n, st, status);           \
+        case 64: return launch_mixed<BLOCK>(KERNEL<64, true>, KERNEL<64, false>, tab, tab_bytes,           \
+                                            *static_cast<const ARGS<64>*>(args), n, st, status);           \
+        case 256: return launch_mixed<BLOCK>(KERNEL<256, true>, KERNEL<256, false>, tab, tab_bytes,        \
+                                             *static_cast<const ARGS<256>*>(args), n, st, status);         \
+        default: return cudaErrorInvalidValue;                                                             \
+        }                                                                                                  \
+    }
+CB_DISPATCH_M(launch_rates_mixed, rates_mixed_kernel, RatesArgs, kBlock)
+CB_DISPATCH_M(launch_transport_mixed, transport_mixed_kernel, TransportArgs, kTransportBlock)
+#undef CB_DISPATCH_M
+
+}  // namespace cbg

@@ -8,6 +8,7 @@
 
 #include "collision_integrals.h"
 #include "tables.h"
+#include "tables_mixed.h"
 
 namespace cbg {
 
@@ -418,6 +419,9 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     RatesHeader h;
     std::memset(&h, 0, sizeof h);
     h.K = K; h.A = A; h.R = R; h.n_eff = (int32_t)(eff_rows.size() / K); h.n_falloff = (int32_t)falloff.size();
+    m.n_eff = h.n_eff;
+    // Efficiency rows padded with zero rows to a multiple of 4: the kernel sums four rows per pass.
+    while ((eff_rows.size() / K) % 4) eff_rows.resize(eff_rows.size() + K, 0.0);
     {
         float mx = std::cbrt(FLT_MAX);  // largest f32 whose cube stays finite (reaction.rs:244-251)
         mx = cbrtf(FLT_MAX);
@@ -443,6 +447,81 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     }
     h.total_bytes = align_blob(blob);
     std::memcpy(blob.data(), &h, sizeof h);
+
+    // ---- mixed-precision tables (tables_mixed.h) -----------------------------------------------
+    {
+        auto arr_f = [](double A, double b, double Ea) {
+            ArrheniusF a{};
+            a.b = (float)b; a.mEa = (float)(-Ea); a.lnA = (float)std::log(A);
+            a.has_x = (b != 0.0 || Ea != 0.0) ? 1 : 0;
+            a.A = A;
+            return a;
+        };
+        std::vector<SpeciesF> sf(K);
+        for (int k = 0; k < K; k++) {
+            SpeciesF& s = sf[k];
+            std::memset(&s, 0, sizeof s);
+            s.split = species[k].split;
+            for (int p = 0; p < 2; p++) {
+                for (int i = 0; i < 7; i++) s.g[p][i] = species[k].g[p][i];
+                for (int i = 0; i < 6; i++) s.h[p][i] = (float)species[k].h[p][i];
+                for (int i = 0; i < 5; i++) s.cp[p][i] = (float)species[k].cp[p][i];
+            }
+            s.dtE = species[k].dtE;
+            s.need_exp = species[k].need_exp;
+            s.need_exp_neg = species[k].need_exp_neg;
+        }
+        std::vector<ReactionF> rf(R);
+        std::vector<FalloffF> ff;
+        for (int r = 0; r < R; r++) {
+            const Reaction& x = reactions[r];
+            ReactionF& y = rf[r];
+            std::memset(&y, 0, sizeof y);
+            y.model = x.model; y.minus_sigma_net = x.minus_sigma_net; y.eff_row = x.eff_row; y.falloff = x.falloff;
+            y.n_r = x.n_r; y.n_p = x.n_p; y.n_net = x.n_net;
+            std::memcpy(y.r_k, x.r_k, sizeof y.r_k); std::memcpy(y.p_k, x.p_k, sizeof y.p_k);
+            std::memcpy(y.net_k, x.net_k, sizeof y.net_k); std::memcpy(y.r_n, x.r_n, sizeof y.r_n);
+            std::memcpy(y.p_n, x.p_n, sizeof y.p_n); std::memcpy(y.net_n, x.net_n, sizeof y.net_n);
+            const double* rc = &m.rate[r * 3];
+            if (x.model == CB_TROE) {
+                const double* k0 = &m.k0[r * 3];
+                y.k = arr_f(1.0, rc[1], rc[2]);
+                FalloffF f{};
+                const Falloff& g = falloff[x.falloff];
+                f.k0 = arr_f(k0[0] / rc[0], k0[1], k0[2]);
+                f.ainf = g.ainf;
+                f.c1mA = (float)g.c1mA; f.cA = (float)g.cA; f.c3 = (float)g.c3; f.c1 = (float)g.c1;
+                f.cmT2 = (float)g.cmT2; f.ln_fcent = (float)g.ln_fcent; f.flags = g.flags;
+                y.falloff = (int32_t)ff.size();
+                ff.push_back(f);
+            } else if (x.model == CB_LINDEMANN) {
+                y.k = arr_f(rc[0], rc[1], rc[2]);
+                FalloffF f{};
+                f.k0 = arr_f(m.k0[r * 3], m.k0[r * 3 + 1], m.k0[r * 3 + 2]);
+                y.falloff = (int32_t)ff.size();
+                ff.push_back(f);
+            } else {
+                y.k = arr_f(rc[0], rc[1], rc[2]);
+            }
+        }
+        std::vector<float> efff(eff_rows.begin(), eff_rows.end());
+        RatesMixedHeader hm;
+        std::memset(&hm, 0, sizeof hm);
+        hm.K = K; hm.A = A; hm.R = R; hm.n_eff = h.n_eff; hm.n_falloff = (int32_t)ff.size();
+        hm.M3 = h.M3; hm.cbrt_max = h.cbrt_max; hm.C0 = h.C0; hm.rcp_C0 = h.rcp_C0;
+        hm.ln10_04 = (float)h.ln10_04; hm.ln10_075 = (float)h.ln10_075;
+        std::vector<uint8_t>& b = m.rates_mixed_blob;
+        b.clear();
+        append(b, &hm, 1);
+        hm.off_species = align_blob(b); append(b, sf.data(), sf.size());
+        hm.off_reactions = align_blob(b); append(b, rf.data(), rf.size());
+        hm.off_falloff = align_blob(b); append(b, ff.data(), ff.size());
+        hm.off_eff = align_blob(b); append(b, efff.data(), efff.size());
+        MathTables mt = make_math_tables();
+        hm.off_math = align_blob(b); append(b, &mt, 1);
+        hm.total_bytes = align_blob(b);
+        std::memcpy(b.data(), &hm, sizeof hm);
+    }
 
     // ---- algorithmic work of reaction.rs:356-391 per cell (the reference's operations) ----------
     Work& w = m.rates_work;
@@ -580,6 +659,27 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
     }
     h.total_bytes = align_blob(blob);
     std::memcpy(blob.data(), &h, sizeof h);
+
+    // ---- mixed-precision (all FP32) transport tables ----------------------------------------------
+    {
+        auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+        TransportMixedHeader hm;
+        std::memset(&hm, 0, sizeof hm);
+        hm.K = K; hm.n_pairs = n_pairs; hm.T0 = T0;
+        std::vector<uint8_t>& b = m.transport_mixed_blob;
+        b.clear();
+        append(b, &hm, 1);
+        auto put = [&](const std::vector<double>& v) {
+            int32_t off = align_blob(b);
+            std::vector<float> f = f32(v);
+            append(b, f.data(), f.size());
+            return off;
+        };
+        hm.off_cond = put(cond); hm.off_visc = put(visc); hm.off_W = put(Wc); hm.off_diff = put(diff);
+        hm.off_A2 = put(A2); hm.off_AB = put(AB); hm.off_B2 = put(B2);
+        hm.total_bytes = align_blob(b);
+        std::memcpy(b.data(), &hm, sizeof hm);
+    }
 
     // ---- algorithmic work of transport.rs:179-210 per cell ---------------------------------------
     Work& w = m.transport_work;

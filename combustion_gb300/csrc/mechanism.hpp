@@ -14,6 +14,7 @@ struct Work {
 
 struct HostMechanism {
     int K = 0, R = 0, A = 0;
+    int n_eff = 0;  // reactions with third-body efficiencies (three-body and falloff)
     std::vector<double> W, split, nasa7;  // [K], [K], [K*14]
     std::vector<int32_t> geometry;
     std::vector<double> diameter, well_depth, polarizability, dipole, rot, dof;
@@ -22,12 +23,14 @@ struct HostMechanism {
     std::vector<double> rate, k0, troe, sri, eff;  // [R*3], [R*3], [R*4], [R*5], [R*K]
 
     std::vector<uint8_t> rates_blob;
+    std::vector<uint8_t> rates_mixed_blob;  // tables of the mixed-precision form
     Work rates_work;
 
     bool transport_ready = false;
     double T0 = 0, mu0 = 0, lambda0 = 0;
     std::vector<double> fit_cond, fit_visc, fit_diff;  // raw fits [K*5], [K*5], [K*K*5]
     std::vector<uint8_t> transport_blob;
+    std::vector<uint8_t> transport_mixed_blob;
     Work transport_work;
 };
 

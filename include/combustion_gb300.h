@@ -138,6 +138,19 @@ int cb_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, doubl
 int cb_rates_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* rates_out,
                            double* const* transport_out, uint32_t flags, void* stream);
 
+/* Mixed-precision forms of the three calls above (same inputs, outputs and flags). FP64 is kept for the
+ * Gibbs polynomials and exponentials of the equilibrium constant (reaction.rs:234-304), the
+ * forward-minus-reverse rate of progress (reaction.rs:305-306) and the accumulation into species rates
+ * (reaction.rs:312-327); Arrhenius exponentials, third-body sums, falloff blending, the h/RT and cp/R
+ * polynomials and all of transport run in FP32. No reference counterpart: the reference's FP64 path is
+ * cb_*_f64. Its error against that path is measured by the tests (below 1e-4, condition-scaled). */
+int cb_rates_mixed(cb_mech* mech, size_t n, const double* const* inputs, double* const* outputs,
+                   uint32_t flags, void* stream);
+int cb_transport_mixed(cb_mech* mech, size_t n, const double* const* inputs, double* const* outputs,
+                       uint32_t flags, void* stream);
+int cb_rates_transport_mixed(cb_mech* mech, size_t n, const double* const* inputs, double* const* rates_out,
+                             double* const* transport_out, uint32_t flags, void* stream);
+
 int cb_work_model(const cb_mech* mech, cb_work* rates, cb_work* transport);
 
 /* Diagnostic: FP64 fused multiply-adds per second the current GPU issues (8 independent chains per
