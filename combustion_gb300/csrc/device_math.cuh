@@ -12,19 +12,22 @@ namespace cbg {
 constexpr double kF32Max = 3.4028234663852886e+38;     // f32::MAX as f64
 constexpr double kF32MinPos = 1.1754943508222875e-38;  // f32::MIN_POSITIVE as f64
 
-// Lane-divergent table lookups: shared memory, one copy per block (per translation unit).
-static __shared__ MathTables s_math;
+// Dynamic shared memory of every kernel here. It starts with the MathTables (lane-divergent lookups),
+// which every table blob carries first: either the whole blob is staged there, or only its first
+// kMathBytes.
+extern __shared__ __align__(16) uint8_t cb_dsmem[];
 
-__device__ __forceinline__ double exp64(double x) { return exp_fast(x, s_math.exp2j); }
-__device__ __forceinline__ double log64(double x) { return log_fast(x, s_math); }
+__device__ __forceinline__ const MathTables& smath() { return *reinterpret_cast<const MathTables*>(cb_dsmem); }
+__device__ __forceinline__ double exp64(double x) { return exp_fast(x, smath().exp2j); }
+__device__ __forceinline__ double log64(double x) { return log_fast(x, smath()); }
 __device__ __forceinline__ double rcp64(double x) { return rcp_fast(x); }
 __device__ __forceinline__ double div64(double a, double b) { return div_fast(a, b); }
 
-// Copies the math tables of a blob (byte offset off_math) into s_math; call before any use.
-__device__ __forceinline__ void load_math(const uint8_t* gtab, int off_math) {
-    const double* src = reinterpret_cast<const double*>(gtab + off_math);
-    double* dst = reinterpret_cast<double*>(&s_math);
-    for (int q = threadIdx.x; q < (int)(sizeof(MathTables) / sizeof(double)); q += blockDim.x) dst[q] = src[q];
+// Copies the math tables at the start of a global blob into dynamic shared memory (whole block).
+__device__ __forceinline__ void load_math(const uint8_t* gtab) {
+    const double* src = reinterpret_cast<const double*>(gtab);
+    double* dst = reinterpret_cast<double*>(cb_dsmem);
+    for (int q = threadIdx.x; q < kMathBytes / (int)sizeof(double); q += blockDim.x) dst[q] = src[q];
     __syncthreads();
 }
 

@@ -31,9 +31,16 @@
 
 namespace cbg {
 
+// Out-of-line slow paths: kept as real (almost never taken) branches. Inlined, the compiler turns them
+// into predicated code that every call executes, and predicated-off FP64 instructions still occupy the
+// FP64 pipe (measured: about 2k extra warp-level FP64 instructions per cell in the rates kernels).
+static __device__ __noinline__ double exp_slow(double x) { return exp(x); }
+static __device__ __noinline__ double log_slow(double x) { return log(x); }
+static __device__ __noinline__ double rcp_slow(double y) { return 1.0 / y; }
+
 __device__ __forceinline__ double exp_fast(double x, const double* __restrict__ exp2j) {
     const int hi = __double2hiint(x);
-    if ((hi & 0x7fffffff) >= 0x40862000) return exp(x);  // |x| >= 708, inf or NaN
+    if ((hi & 0x7fffffff) >= 0x40862000) return exp_slow(x);  // |x| >= 708, inf or NaN
     const double t = fma(x, 0x1.71547652b82fep+8, 0x1.8p52);  // 256/ln2, round-to-nearest shifter
     const int n = __double2loint(t);
     const double nd = t - 0x1.8p52;
@@ -49,7 +56,7 @@ __device__ __forceinline__ double exp_fast(double x, const double* __restrict__ 
 
 __device__ __forceinline__ double log_fast(double x, const MathTables& T) {
     const int hi = __double2hiint(x), lo = __double2loint(x);
-    if (hi < 0x00100000 || hi >= 0x7ff00000) return log(x);  // <= 0, subnormal, inf or NaN
+    if (hi < 0x00100000 || hi >= 0x7ff00000) return log_slow(x);  // <= 0, subnormal, inf or NaN
     const int e = (hi >> 20) - 1023;
     const int mant = hi & 0x000fffff;
     const int j = ((mant >> 11) + 1) >> 1;  // nearest multiple of 1/256
@@ -71,7 +78,7 @@ __device__ __forceinline__ double log_fast(double x, const MathTables& T) {
 
 __device__ __forceinline__ double rcp_fast(double y) {
     const int ahi = __double2hiint(y) & 0x7fffffff;
-    if (ahi < 0x00200000 || ahi >= 0x7fd00000) return 1.0 / y;  // 0, tiny, huge, inf or NaN
+    if (ahi < 0x00200000 || ahi >= 0x7fd00000) return rcp_slow(y);  // 0, tiny, huge, inf or NaN
     double r;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(y));
     const double e = fma(-y, r, 1.0);

@@ -36,8 +36,7 @@ __device__ __forceinline__ double arrhenius(const Arrhenius& a, const Temps& t) 
     double k;
     if (a.has_x) {
         double x = fma(a.beta, t.lnT, fma(a.mEa, t.rcpT, a.lnA));
-        k = exp64(x);
-        if (a.factor != kNone) k = factor_of(a.factor, t) * k;
+        k = exp64(x);  // beta includes the power of T (tables.h)
     } else {
         k = a.factor != kNone ? factor_of(a.factor, t) * a.A : a.A;
     }
@@ -54,7 +53,7 @@ struct RatesTables {
     const Falloff* falloff;
     const double* eff;
     __device__ explicit RatesTables(const uint8_t* tab)
-        : H(reinterpret_cast<const RatesHeader*>(tab)),
+        : H(reinterpret_cast<const RatesHeader*>(tab + kMathBytes)),
           species(reinterpret_cast<const Species*>(tab + H->off_species)),
           reactions(reinterpret_cast<const Reaction*>(tab + H->off_reactions)),
           falloff(reinterpret_cast<const Falloff*>(tab + H->off_falloff)),
@@ -64,7 +63,7 @@ struct RatesTables {
 template <int KMAX>
 struct Cell {
     Temps t;
-    double Ctot, C0, rcpC0;
+    double Ctot, C0, rcpC0, rcpC0sq;
     double C[KMAX];              // concentrations, bulk last
     double ex[KMAX], exn[KMAX];  // min(M3, exp(g_k)), min(cbrt(f32::MAX), exp(-g_k))
     double M[4 * KMAX];          // third-body concentrations C + sum (e_k - 1) C_k, one per efficiency row
@@ -103,6 +102,7 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
     c.C[K - 1] = c.Ctot - sum;
     c.C0 = H.C0 * c.t.rcpT;
     c.rcpC0 = H.rcp_C0 * T;
+    c.rcpC0sq = c.rcpC0 * c.rcpC0;
     for (int k = 0; k < A; k++) {
         const Species& s = tb.species[k];
         if (!(s.need_exp | s.need_exp_neg)) continue;
@@ -132,22 +132,26 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
 // seeded with the first factor.
 __device__ __forceinline__ double conc_product(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
     double p = C[ks[0]];
+#pragma unroll 1
     for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+#pragma unroll 1
     for (int q = 1; q < n; q++)
+#pragma unroll 1
         for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
     return p;
 }
 
 // cR of one reaction (reaction.rs:149-309): forward rate constant (with third-body efficiency and
 // falloff), rate of progress against the equilibrium constant, and their product.
-template <int KMAX>
+// MODEL is a compile-time constant: reactions are grouped by model, so no model branch (and no
+// predicated FP64 instruction of another model) is executed per reaction.
+template <int KMAX, int MODEL>
 __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const Cell<KMAX>& c) {
     const RatesHeader& H = *tb.H;
     const Temps& t = c.t;
-    const double M = x.eff_row >= 0 ? c.M[x.eff_row] : c.Ctot;
-    double num, den = 1.0;
-    bool ratio = false;
-    if (x.model == 4) {  // Troe (reaction.rs:160-193)
+    double kf;  // forward rate coefficient: k, k M, or the falloff-blended value
+    if constexpr (MODEL == 4) {  // Troe (reaction.rs:160-193)
+        const double M = c.M[x.eff_row];
         const Falloff& f = tb.falloff[x.falloff];
         const double k0 = arrhenius(f.k0, t);
         double Pr, kinf;
@@ -175,44 +179,61 @@ __device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Rea
         const double lnPrC = log64(Pr + kF32MinPos) + Cc;
         const double f1 = div64(lnPrC, fma(-0.14, lnPrC, Nn));
         const double Fb = exp64(div64(lnF, fma(f1, f1, 1.0)));
-        num = (Fb * kinf) * Pr;
-        den = Pr + 1.0;
-        ratio = true;
-    } else if (x.model == 3) {  // Lindemann (reaction.rs:153-159)
+        kf = div64((Fb * kinf) * Pr, Pr + 1.0);
+    } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
         const Falloff& f = tb.falloff[x.falloff];
-        const double Ck0 = M * arrhenius(f.k0, t);
+        const double Ck0 = c.M[x.eff_row] * arrhenius(f.k0, t);
         const double ki = arrhenius(x.k, t);
-        num = Ck0 * ki;
-        den = (Ck0 + ki) + kF32MinPos;
-        ratio = true;
-    } else {
-        num = arrhenius(x.k, t);
-        if (x.model == 2) num *= M;  // three-body (reaction.rs:152)
+        kf = div64(Ck0 * ki, (Ck0 + ki) + kF32MinPos);
+    } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
+        kf = arrhenius(x.k, t) * c.M[x.eff_row];
+    } else {  // elementary, irreversible
+        kf = arrhenius(x.k, t);
     }
     // Rate of progress (reaction.rs:269-306).
     const double Rf = conc_product(c.C, x.r_k, x.r_n, x.n_r);
     double Rnet = Rf;
-    if (x.model != 1) {
+    if constexpr (MODEL != 1) {
         // 1/Kc: product of the cached Gibbs exponentials, repeated |nu| times, in species order.
-        double p = 0.0;
-        bool first = true;
-        for (int q = 0; q < x.n_net; q++) {
+        const int nu0 = x.net_n[0];
+        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
+        double p = t0;
+#pragma unroll 1
+        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
+#pragma unroll 1
+        for (int q = 1; q < x.n_net; q++) {
             const int nu = x.net_n[q], k = x.net_k[q];
             const double tt = nu > 0 ? c.ex[k] : c.exn[k];
-            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) {
-                p = first ? tt : p * tt;
-                first = false;
-            }
+#pragma unroll 1
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
         }
-        switch (x.minus_sigma_net) {
-        case 1: p = c.C0 * p; break;
-        case -1: p = c.rcpC0 * p; break;
-        case -2: p = (c.rcpC0 * c.rcpC0) * p; break;
-        default: break;
-        }
+        // (P0/RT)^(-sum nu): the factor chosen with integer selects, one multiply for every reaction.
+        const int msn = x.minus_sigma_net;
+        const double cfac = msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
+        p *= cfac;
         Rnet = fma(-p, conc_product(c.C, x.p_k, x.p_n, x.n_p), Rf);
     }
-    return ratio ? div64(Rnet * num, den) : Rnet * num;
+    return kf * Rnet;
+}
+
+template <int KMAX, int MODEL>
+__device__ __forceinline__ void accumulate_group(const RatesTables& tb, const Cell<KMAX>& c, double* wdot) {
+    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
+        const Reaction& x = tb.reactions[r];
+        const double cR = reaction_rate<KMAX, MODEL>(tb, x, c);
+#pragma unroll 1
+        for (int q = 0; q < x.n_net; q++)
+            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
+    }
+}
+
+template <int KMAX, int MODEL>
+__device__ __forceinline__ void rates_of_group(const RatesTables& tb, const Cell<KMAX>& c,
+                                               const ReactionRatesArgs<KMAX>& io, size_t i) {
+    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
+        const Reaction& x = tb.reactions[r];
+        io.out[x.orig][i] = reaction_rate<KMAX, MODEL>(tb, x, c);
+    }
 }
 
 template <int KMAX>
@@ -227,12 +248,12 @@ __device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, siz
     cell_setup<KMAX>(tb, pressure_R, T, V, io.in + 4, i, c);
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
-    for (int r = 0; r < H.R; r++) {  // species_rates (reaction.rs:312-327)
-        const Reaction& x = tb.reactions[r];
-        const double cR = reaction_rate<KMAX>(tb, x, c);
-        for (int q = 0; q < x.n_net; q++)
-            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
-    }
+    // species_rates (reaction.rs:312-327), one loop per reaction model (SRI is rejected at creation)
+    accumulate_group<KMAX, 0>(tb, c, wdot);
+    accumulate_group<KMAX, 1>(tb, c, wdot);
+    accumulate_group<KMAX, 2>(tb, c, wdot);
+    accumulate_group<KMAX, 3>(tb, c, wdot);
+    accumulate_group<KMAX, 4>(tb, c, wdot);
     // Energy and volume (reaction.rs:375-384).
     double E = 0.0;
     for (int k = 0; k < A; k++) {
@@ -260,20 +281,24 @@ template <int KMAX>
 __device__ void reaction_rates_cell(const RatesTables& tb, const ReactionRatesArgs<KMAX>& io, size_t i) {
     Cell<KMAX> c;
     cell_setup<KMAX>(tb, io.in[0][i], io.in[1][i], io.in[2][i], io.in + 3, i, c);
-    for (int r = 0; r < tb.H->R; r++) io.out[r][i] = reaction_rate<KMAX>(tb, tb.reactions[r], c);
+    rates_of_group<KMAX, 0>(tb, c, io, i);
+    rates_of_group<KMAX, 1>(tb, c, io, i);
+    rates_of_group<KMAX, 2>(tb, c, io, i);
+    rates_of_group<KMAX, 3>(tb, c, io, i);
+    rates_of_group<KMAX, 4>(tb, c, io, i);
 }
 
 template <int KMAX, bool SMEM>
 __global__ void __launch_bounds__(kBlock) rates_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                       const __grid_constant__ RatesArgs<KMAX> io, size_t n,
                                                       int* status) {
-    extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
-    load_math(gtab, reinterpret_cast<const RatesHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
-    if (SMEM) {
-        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
-        tab = smem;
+    if (SMEM) {  // the whole blob, math tables first, into dynamic shared memory
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {  // tables read from global memory; only the math tables go to shared memory
+        load_math(gtab);
     }
     const RatesTables tb(tab);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -284,13 +309,13 @@ template <int KMAX, bool SMEM>
 __global__ void __launch_bounds__(kBlock) reaction_rates_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                                const __grid_constant__ ReactionRatesArgs<KMAX> io,
                                                                size_t n, int* status) {
-    extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
-    load_math(gtab, reinterpret_cast<const RatesHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
-    if (SMEM) {
-        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
-        tab = smem;
+    if (SMEM) {  // the whole blob, math tables first, into dynamic shared memory
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {  // tables read from global memory; only the math tables go to shared memory
+        load_math(gtab);
     }
     const RatesTables tb(tab);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -299,8 +324,9 @@ __global__ void __launch_bounds__(kBlock) reaction_rates_kernel(const uint8_t* _
 
 // ---------------------------------------------------------------------------------------------------
 template <int KMAX>
-__device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i) {
-    const TransportHeader& H = *reinterpret_cast<const TransportHeader*>(tab);
+__device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i, size_t o) {
+    // i: the cell's index in the inputs, o: in the outputs (they differ for gathered cells)
+    const TransportHeader& H = *reinterpret_cast<const TransportHeader*>(tab + kMathBytes);
     const double* cond = reinterpret_cast<const double*>(tab + H.off_cond);
     const double* visc = reinterpret_cast<const double*>(tab + H.off_visc);
     const double* W = reinterpret_cast<const double*>(tab + H.off_W);
@@ -344,7 +370,7 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         Ac = fma(X[k], c, Ac);
         Bc = fma(X[k], rcp64(c), Bc);
     }
-    io.out[0][i] = (div64(Ac, N) + div64(N, Bc)) * VT;
+    io.out[0][o] = (div64(Ac, N) + div64(N, Bc)) * VT;
 
     // Viscosity, Wilke mixing (transport.rs:148-158) with the square expanded:
     // sum_j X_j (a + b v_k/v_j)^2 = sum_j a^2 X_j + v_k sum_j 2ab X_j/v_j + v_k^2 sum_j b^2 X_j/v_j^2.
@@ -380,7 +406,7 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
             }
         }
     }
-    io.out[1][i] = VT * mu;
+    io.out[1][o] = VT * mu;
 
     // Mixture-averaged diffusion (transport.rs:162-177); S reuses Y.
     double* S = Y;
@@ -406,23 +432,26 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         }
         S[k] += sa + sb;
     }
-    for (int k = 0; k < K; k++) io.out[2 + k][i] = div64(MVTN - (VT * W[k]) * X[k], S[k]);
+    for (int k = 0; k < K; k++) io.out[2 + k][o] = div64(MVTN - (VT * W[k]) * X[k], S[k]);
 }
 
 template <int KMAX, bool SMEM>
 __global__ void __launch_bounds__(kTransportBlock) transport_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                           const __grid_constant__ TransportArgs<KMAX> io,
                                                           size_t n, int* status) {
-    extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
-    load_math(gtab, reinterpret_cast<const TransportHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
-    if (SMEM) {
-        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
-        tab = smem;
+    if (SMEM) {  // the whole blob, math tables first, into dynamic shared memory
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {  // tables read from global memory; only the math tables go to shared memory
+        load_math(gtab);
     }
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        transport_cell<KMAX>(tab, io, i);
+    if (io.count) n = min(n, (size_t)*io.count);  // gathered cells: the count is known on the device only
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = io.index ? (size_t)(io.index[j] & kIndexMask) : j;
+        transport_cell<KMAX>(tab, io, i, (io.flags & kCompactOut) ? j : i);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -451,13 +480,13 @@ cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32
         if (e != cudaSuccess) return e;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, kMathBytes);
     }
     if (per_sm < 1) per_sm = 1;
     size_t grid = (size_t)sm_count() * per_sm;
     if (want < grid) grid = want ? want : 1;
     if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    else kglobal<<<(unsigned)grid, BLOCK, 0, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, BLOCK, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace
@@ -465,7 +494,7 @@ cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32
 // The elementary functions of the plain path on device arrays (which: 0 exp, 1 log, 2 reciprocal), for
 // accuracy checks against CUDA's own functions.
 __global__ void math_check_kernel(const uint8_t* math, int which, const double* x, double* y, size_t n) {
-    load_math(math, 0);
+    load_math(math);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const double v = x[i];
         y[i] = which == 0 ? exp64(v) : which == 1 ? log64(v) : rcp64(v);
@@ -477,7 +506,7 @@ cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, d
     if (n == 0) return cudaSuccess;
     size_t grid = (n + 255) / 256;
     if (grid > 4096) grid = 4096;
-    math_check_kernel<<<(unsigned)grid, 256, 0, st>>>(math, which, x, y, n);
+    math_check_kernel<<<(unsigned)grid, 256, kMathBytes, st>>>(math, which, x, y, n);
     return cudaGetLastError();
 }
 
@@ -487,7 +516,7 @@ int max_table_smem() {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        v = optin - (int)sizeof(MathTables) - 1024;  // room for the static shared variables
+        v = optin - 1024;  // room for the static shared variables
     }
     return v;
 }

@@ -24,7 +24,7 @@ struct RatesMixedTables {
     const FalloffF* falloff;
     const float* eff;
     __device__ explicit RatesMixedTables(const uint8_t* tab)
-        : H(reinterpret_cast<const RatesMixedHeader*>(tab)),
+        : H(reinterpret_cast<const RatesMixedHeader*>(tab + kMathBytes)),
           species(reinterpret_cast<const SpeciesF*>(tab + H->off_species)),
           reactions(reinterpret_cast<const ReactionF*>(tab + H->off_reactions)),
           falloff(reinterpret_cast<const FalloffF*>(tab + H->off_falloff)),
@@ -43,8 +43,11 @@ __device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, fl
 
 __device__ __forceinline__ double conc_product_m(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
     double p = C[ks[0]];
+#pragma unroll 1
     for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+#pragma unroll 1
     for (int q = 1; q < n; q++)
+#pragma unroll 1
         for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
     return p;
 }
@@ -58,6 +61,97 @@ __device__ __forceinline__ double int_to_double_small(int v) {
     return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
 }
 
+// Per-cell working state of the mixed rates program.
+template <int KMAX>
+struct CellM {
+    double C[KMAX];              // FP64 concentrations, bulk last
+    double ex[KMAX], exn[KMAX];  // FP64 Gibbs exponentials
+    float Mf[4 * KMAX];          // FP32 third-body concentrations, one per efficiency row
+    double C0, rcpC0, rcpC0sq;
+    float Ctotf, Tf, lnTf, rcpTf;
+};
+
+// cR of one reaction. MODEL is a compile-time constant (reactions are grouped by model), so no
+// predicated FP64 instruction of another model's branch is executed.
+template <int KMAX, int MODEL>
+__device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, const ReactionF& x, const CellM<KMAX>& c) {
+    const RatesMixedHeader& H = *tb.H;
+    double kf;  // forward rate coefficient including third body and falloff
+    if constexpr (MODEL == 4) {  // Troe, blending in FP32 (reaction.rs:160-193)
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double Md = flt_to_dbl(c.Mf[x.eff_row]);
+        double Pr, kinf;
+        if (f.flags & kKinfConst) {
+            Pr = Md * k0;
+            kinf = f.ainf;
+        } else {
+            const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+            Pr = (Md * k0) * rcp64(ki + kF32MinPos);
+            kinf = f.ainf * ki;
+        }
+        float lnF;
+        if (f.flags & kFcentConst) {
+            lnF = f.ln_fcent;
+        } else {
+            float F = 0.f;
+            if (f.flags & kTermT3) F = f.c1mA * expf(c.Tf * f.c3);
+            if (f.flags & kTermT1) F += f.cA * expf(c.Tf * f.c1);
+            if (f.flags & kTermAConst) F += f.cA;
+            if (f.flags & kTermT2) F += expf(f.cmT2 * c.rcpTf);
+            lnF = logf(F);
+        }
+        const float Cc = fmaf(-0.67f, lnF, -H.ln10_04);
+        const float Nn = fmaf(-1.27f, lnF, H.ln10_075);
+        const float lnPrC = log_dbl_f32(Pr + kF32MinPos) + Cc;
+        const float f1 = __fdividef(lnPrC, fmaf(-0.14f, lnPrC, Nn));
+        const float Fb = expf(__fdividef(lnF, fmaf(f1, f1, 1.f)));
+        kf = (flt_to_dbl(Fb) * kinf) * (Pr * rcp64(Pr + 1.0));
+    } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double Ck0 = flt_to_dbl(c.Mf[x.eff_row]) * arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+        kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
+    } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
+        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf) * flt_to_dbl(c.Mf[x.eff_row]);
+    } else {
+        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+    }
+    // FP64 rate of progress (reaction.rs:269-306).
+    const double Rf = conc_product_m(c.C, x.r_k, x.r_n, x.n_r);
+    double Rnet = Rf;
+    if constexpr (MODEL != 1) {
+        const int nu0 = x.net_n[0];
+        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
+        double p = t0;
+#pragma unroll 1
+        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
+#pragma unroll 1
+        for (int q = 1; q < x.n_net; q++) {
+            const int nu = x.net_n[q], k = x.net_k[q];
+            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
+#pragma unroll 1
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
+        }
+        const int msn = x.minus_sigma_net;  // (P0/RT)^(-sum nu) chosen by integer selects
+        p *= msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
+        Rnet = fma(-p, conc_product_m(c.C, x.p_k, x.p_n, x.n_p), Rf);
+    }
+    return kf * Rnet;
+}
+
+// Accumulation into the species rates (reaction.rs:312-327), one reaction model.
+template <int KMAX, int MODEL>
+__device__ __forceinline__ void accumulate_group_m(const RatesMixedTables& tb, const CellM<KMAX>& c, double* wdot) {
+    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
+        const ReactionF& x = tb.reactions[r];
+        const double cR = reaction_rate_m<KMAX, MODEL>(tb, x, c);
+#pragma unroll 1
+        for (int q = 0; q < x.n_net; q++)
+            wdot[x.net_k[q]] = fma(int_to_double_small(x.net_n[q]), cR, wdot[x.net_k[q]]);
+    }
+}
+
 template <int KMAX>
 __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMAX>& io, size_t i) {
     const RatesMixedHeader& H = *tb.H;
@@ -66,121 +160,58 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
     const double pressure_R = uniform ? io.in[0][0] : io.in[0][i];
     const double rcp_pressure_R = uniform ? io.in[1][0] : io.in[1][i];
     const double T = io.in[2][i], V = io.in[3][i];
+    CellM<KMAX> c;
     // FP64 prologue (reaction.rs:362-373): temperatures for the Gibbs polynomials, concentrations for
     // the rates of progress.
     const double md = rcp64(V), rcpT = rcp64(T), lnT = log64(T);
     const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
-    double C[KMAX];
-    float Cf[KMAX];
     double sum = 0.0;
     for (int k = 0; k < K - 1; k++) {
-        C[k] = md * max0(io.in[4 + k][i]);
-        sum += C[k];
-        Cf[k] = dbl_to_flt(C[k]);
+        c.C[k] = md * max0(io.in[4 + k][i]);
+        sum += c.C[k];
     }
     const double Ctot = pressure_R * rcpT;
-    C[K - 1] = Ctot - sum;
-    Cf[K - 1] = dbl_to_flt(C[K - 1]);
-    const float Ctotf = dbl_to_flt(Ctot), Tf = dbl_to_flt(T), lnTf = dbl_to_flt(lnT), rcpTf = dbl_to_flt(rcpT);
-    const double C0 = H.C0 * rcpT, rcpC0 = H.rcp_C0 * T;
+    c.C[K - 1] = Ctot - sum;
+    c.Ctotf = dbl_to_flt(Ctot);
+    c.Tf = dbl_to_flt(T);
+    c.lnTf = dbl_to_flt(lnT);
+    c.rcpTf = dbl_to_flt(rcpT);
+    c.C0 = H.C0 * rcpT;
+    c.rcpC0 = H.rcp_C0 * T;
+    c.rcpC0sq = c.rcpC0 * c.rcpC0;
 
     // FP64 Gibbs exponentials (reaction.rs:234-263).
-    double ex[KMAX], exn[KMAX];
     for (int k = 0; k < A; k++) {
         const SpeciesF& s = tb.species[k];
         if (!(s.need_exp | s.need_exp_neg)) continue;
         const double* g = s.g[piece_of_m(s.split, T)];
         const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
-        if (s.need_exp) ex[k] = min_pos(H.M3, exp64(x));
-        if (s.need_exp_neg) exn[k] = min_pos(H.cbrt_max, exp64(-x));
+        if (s.need_exp) c.ex[k] = min_pos(H.M3, exp64(x));
+        if (s.need_exp_neg) c.exn[k] = min_pos(H.cbrt_max, exp64(-x));
     }
     // FP32 third-body sums, four rows per pass.
-    float Mf[4 * KMAX];
     for (int e0 = 0; e0 < H.n_eff; e0 += 4) {
         const float* E = tb.eff + (size_t)e0 * K;
         float s[4] = {0.f, 0.f, 0.f, 0.f};
         for (int k = 0; k < K; k++) {
-            const float ck = Cf[k];
+            const float ck = dbl_to_flt(c.C[k]);  // integer ops, recomputed per pass (no FP32 copy kept)
 #pragma unroll
             for (int q = 0; q < 4; q++) s[q] = fmaf(E[q * K + k], ck, s[q]);
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if (e0 + q < H.n_eff) Mf[e0 + q] = Ctotf + s[q];
+            if (e0 + q < H.n_eff) c.Mf[e0 + q] = c.Ctotf + s[q];
     }
 
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
-    for (int r = 0; r < H.R; r++) {
-        const ReactionF& x = tb.reactions[r];
-        const float Mr = x.eff_row >= 0 ? Mf[x.eff_row] : Ctotf;
-        double kf;  // forward rate coefficient including third body and falloff
-        if (x.model == 4) {  // Troe, blending in FP32 (reaction.rs:160-193)
-            const FalloffF& f = tb.falloff[x.falloff];
-            const double k0 = arrhenius_f(f.k0, lnTf, rcpTf);
-            const double Md = flt_to_dbl(Mr);
-            double Pr, kinf;
-            if (f.flags & kKinfConst) {
-                Pr = Md * k0;
-                kinf = f.ainf;
-            } else {
-                const double ki = arrhenius_f(x.k, lnTf, rcpTf);
-                Pr = (Md * k0) * rcp64(ki + kF32MinPos);
-                kinf = f.ainf * ki;
-            }
-            float lnF;
-            if (f.flags & kFcentConst) {
-                lnF = f.ln_fcent;
-            } else {
-                float F = 0.f;
-                if (f.flags & kTermT3) F = f.c1mA * expf(Tf * f.c3);
-                if (f.flags & kTermT1) F += f.cA * expf(Tf * f.c1);
-                if (f.flags & kTermAConst) F += f.cA;
-                if (f.flags & kTermT2) F += expf(f.cmT2 * rcpTf);
-                lnF = logf(F);
-            }
-            const float Cc = fmaf(-0.67f, lnF, -H.ln10_04);
-            const float Nn = fmaf(-1.27f, lnF, H.ln10_075);
-            const float lnPrC = log_dbl_f32(Pr + kF32MinPos) + Cc;
-            const float f1 = __fdividef(lnPrC, fmaf(-0.14f, lnPrC, Nn));
-            const float Fb = expf(__fdividef(lnF, fmaf(f1, f1, 1.f)));
-            kf = (flt_to_dbl(Fb) * kinf) * (Pr * rcp64(Pr + 1.0));
-        } else if (x.model == 3) {  // Lindemann (reaction.rs:153-159)
-            const FalloffF& f = tb.falloff[x.falloff];
-            const double Ck0 = flt_to_dbl(Mr) * arrhenius_f(f.k0, lnTf, rcpTf);
-            const double ki = arrhenius_f(x.k, lnTf, rcpTf);
-            kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
-        } else {
-            kf = arrhenius_f(x.k, lnTf, rcpTf);
-            if (x.model == 2) kf *= flt_to_dbl(Mr);
-        }
-        // FP64 rate of progress (reaction.rs:269-306) and accumulation (reaction.rs:312-327).
-        const double Rf = conc_product_m(C, x.r_k, x.r_n, x.n_r);
-        double Rnet = Rf;
-        if (x.model != 1) {
-            double p = 0.0;
-            bool first = true;
-            for (int q = 0; q < x.n_net; q++) {
-                const int nu = x.net_n[q], k = x.net_k[q];
-                const double tt = nu > 0 ? ex[k] : exn[k];
-                for (int n = 0; n < (nu > 0 ? nu : -nu); n++) {
-                    p = first ? tt : p * tt;
-                    first = false;
-                }
-            }
-            switch (x.minus_sigma_net) {
-            case 1: p = C0 * p; break;
-            case -1: p = rcpC0 * p; break;
-            case -2: p = (rcpC0 * rcpC0) * p; break;
-            default: break;
-            }
-            Rnet = fma(-p, conc_product_m(C, x.p_k, x.p_n, x.n_p), Rf);
-        }
-        const double cR = kf * Rnet;
-        for (int q = 0; q < x.n_net; q++)
-            wdot[x.net_k[q]] = fma(int_to_double_small(x.net_n[q]), cR, wdot[x.net_k[q]]);
-    }
+    accumulate_group_m<KMAX, 0>(tb, c, wdot);
+    accumulate_group_m<KMAX, 1>(tb, c, wdot);
+    accumulate_group_m<KMAX, 2>(tb, c, wdot);
+    accumulate_group_m<KMAX, 3>(tb, c, wdot);
+    accumulate_group_m<KMAX, 4>(tb, c, wdot);
     // Energy (reaction.rs:375-384): FP32 polynomials, FP64 sums over the FP64 species rates.
+    const float Tf = c.Tf, rcpTf = c.rcpTf;
     double E = 0.0, Cp = 0.0, dtE = 0.0;
     for (int k = 0; k < K; k++) {
         const SpeciesF& s = tb.species[k];
@@ -188,7 +219,7 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
         const float* cp = s.cp[p];
         const float ck = fmaf(cp[4], Tf, cp[3]);
         const float cpk = fmaf(fmaf(fmaf(ck, Tf, cp[2]), Tf, cp[1]), Tf, cp[0]);
-        Cp = fma(flt_to_dbl(cpk), C[k], Cp);
+        Cp = fma(flt_to_dbl(cpk), c.C[k], Cp);
         if (k < A) {
             const float* h = s.h[p];
             const float hk = fmaf(h[5], rcpTf, fmaf(fmaf(fmaf(fmaf(h[4], Tf, h[3]), Tf, h[2]), Tf, h[1]), Tf, h[0]));
@@ -206,13 +237,13 @@ template <int KMAX, bool SMEM>
 __global__ void __launch_bounds__(kBlock) rates_mixed_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                             const __grid_constant__ RatesArgs<KMAX> io, size_t n,
                                                             int* status) {
-    extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
-    load_math(gtab, reinterpret_cast<const RatesMixedHeader*>(gtab)->off_math);
     const uint8_t* tab = gtab;
-    if (SMEM) {
-        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
-        tab = smem;
+    if (SMEM) {  // the whole blob, math tables first, into dynamic shared memory
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {  // tables read from global memory; only the math tables go to shared memory
+        load_math(gtab);
     }
     const RatesMixedTables tb(tab);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -222,7 +253,7 @@ __global__ void __launch_bounds__(kBlock) rates_mixed_kernel(const uint8_t* __re
 // ---------------------------------------------------------------------------------------------------
 template <int KMAX>
 __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i) {
-    const TransportMixedHeader& H = *reinterpret_cast<const TransportMixedHeader*>(tab);
+    const TransportMixedHeader& H = *reinterpret_cast<const TransportMixedHeader*>(tab + kMathBytes);
     const float* cond = reinterpret_cast<const float*>(tab + H.off_cond);
     const float* visc = reinterpret_cast<const float*>(tab + H.off_visc);
     const float* W = reinterpret_cast<const float*>(tab + H.off_W);
@@ -329,12 +360,13 @@ __global__ void __launch_bounds__(kTransportBlock) transport_mixed_kernel(const 
                                                                          uint32_t tab_bytes,
                                                                          const __grid_constant__ TransportArgs<KMAX> io,
                                                                          size_t n, int* status) {
-    extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t bar;
     const uint8_t* tab = gtab;
-    if (SMEM) {
-        if (!stage_to_shared(smem, gtab, tab_bytes, &bar, status)) return;
-        tab = smem;
+    if (SMEM) {  // the whole blob, math tables first, into dynamic shared memory
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {  // tables read from global memory; only the math tables go to shared memory
+        load_math(gtab);
     }
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         transport_mixed_cell<KMAX>(tab, io, i);
@@ -355,13 +387,13 @@ cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_
         if (e != cudaSuccess) return e;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, kMathBytes);
     }
     if (per_sm < 1) per_sm = 1;
     size_t grid = (size_t)sms * per_sm;
     if (want < grid) grid = want ? want : 1;
     if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    else kglobal<<<(unsigned)grid, BLOCK, 0, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, BLOCK, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace

@@ -4,6 +4,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 
 #include "collision_integrals.h"
@@ -44,9 +45,13 @@ Arrhenius make_arrhenius(double A, double b, double Ea) {
     else if (b >= 1.5) { a.factor = kT2; rem = b - 2.; }
     else if (b >= 0.5) { a.factor = kT; rem = b - 1.; }
     else { a.factor = kNone; rem = b; }
-    a.beta = to_f32(rem) != 0.0f ? fold_mul(rem) : 0.0;
+    const double brem = to_f32(rem) != 0.0f ? fold_mul(rem) : 0.0;
     a.mEa = Ea != 0.0 ? fold_mul(-Ea) : 0.0;
-    a.has_x = (a.beta != 0.0 || a.mEa != 0.0) ? 1 : 0;
+    a.has_x = (brem != 0.0 || a.mEa != 0.0) ? 1 : 0;
+    a.has_beta_rem = brem != 0.0;
+    // The kernel folds the peeled power T^m back into the exponent: beta = b' + m (exact in FP64).
+    static const double power[] = {0., -2., -1., 4., 3., 2., 1.};
+    a.beta = brem + power[a.factor];
     a.lnA = fold_add(std::log(A));
     a.A = a.factor != kNone ? fold_mul(A) : A;
     return a;
@@ -61,6 +66,21 @@ void append(std::vector<uint8_t>& blob, const T* p, size_t n) {
 int32_t align_blob(std::vector<uint8_t>& blob) {
     while (blob.size() % kAlign) blob.push_back(0);
     return (int32_t)blob.size();
+}
+
+// A blob is [MathTables][header][sections...]; offsets in the header are from the blob's start.
+template <class H>
+void begin_blob(std::vector<uint8_t>& blob, const H& h) {
+    blob.clear();
+    MathTables mt = make_math_tables();
+    append(blob, &mt, 1);
+    append(blob, &h, 1);
+}
+template <class H>
+void finish_blob(std::vector<uint8_t>& blob, H& h) {
+    h.total_bytes = align_blob(blob);
+    h.off_math = 0;
+    std::memcpy(blob.data() + kMathBytes, &h, sizeof h);
 }
 
 // Least squares min |A x - b| by Householder QR in long double (A is m x n, row-major, m >= n).
@@ -434,19 +454,28 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     h.rcp_C0 = fold_mul(1. / P0);
     h.ln10_04 = 0.4 * std::log(10.);
     h.ln10_075 = 0.75 * std::log(10.);
+    // Reactions grouped by model (stable): the kernels run one specialised loop per model, with no
+    // per-reaction model branches (which the compiler would predicate, costing FP64 pipe slots).
+    std::vector<int> order(R);
+    for (int r = 0; r < R; r++) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reactions[a].model < reactions[b].model; });
+    std::vector<Reaction> grouped(R);
+    for (int i = 0; i < R; i++) {
+        grouped[i] = reactions[order[i]];
+        grouped[i].orig = order[i];
+    }
+    for (int mdl = 0; mdl < 6; mdl++) {
+        int end = 0;
+        while (end < R && grouped[end].model <= mdl) end++;
+        h.group_end[mdl] = end;
+    }
     std::vector<uint8_t>& blob = m.rates_blob;
-    blob.clear();
-    append(blob, &h, 1);
+    begin_blob(blob, h);
     h.off_species = align_blob(blob); append(blob, species.data(), species.size());
-    h.off_reactions = align_blob(blob); append(blob, reactions.data(), reactions.size());
+    h.off_reactions = align_blob(blob); append(blob, grouped.data(), grouped.size());
     h.off_falloff = align_blob(blob); append(blob, falloff.data(), falloff.size());
     h.off_eff = align_blob(blob); append(blob, eff_rows.data(), eff_rows.size());
-    {
-        MathTables mt = make_math_tables();
-        h.off_math = align_blob(blob); append(blob, &mt, 1);
-    }
-    h.total_bytes = align_blob(blob);
-    std::memcpy(blob.data(), &h, sizeof h);
+    finish_blob(blob, h);
 
     // ---- mixed-precision tables (tables_mixed.h) -----------------------------------------------
     {
@@ -510,17 +539,19 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
         hm.K = K; hm.A = A; hm.R = R; hm.n_eff = h.n_eff; hm.n_falloff = (int32_t)ff.size();
         hm.M3 = h.M3; hm.cbrt_max = h.cbrt_max; hm.C0 = h.C0; hm.rcp_C0 = h.rcp_C0;
         hm.ln10_04 = (float)h.ln10_04; hm.ln10_075 = (float)h.ln10_075;
+        std::vector<ReactionF> rfg(R);
+        for (int i = 0; i < R; i++) {
+            rfg[i] = rf[order[i]];
+            rfg[i].orig = order[i];
+        }
+        for (int mdl = 0; mdl < 6; mdl++) hm.group_end[mdl] = h.group_end[mdl];
         std::vector<uint8_t>& b = m.rates_mixed_blob;
-        b.clear();
-        append(b, &hm, 1);
+        begin_blob(b, hm);
         hm.off_species = align_blob(b); append(b, sf.data(), sf.size());
-        hm.off_reactions = align_blob(b); append(b, rf.data(), rf.size());
+        hm.off_reactions = align_blob(b); append(b, rfg.data(), rfg.size());
         hm.off_falloff = align_blob(b); append(b, ff.data(), ff.size());
         hm.off_eff = align_blob(b); append(b, efff.data(), efff.size());
-        MathTables mt = make_math_tables();
-        hm.off_math = align_blob(b); append(b, &mt, 1);
-        hm.total_bytes = align_blob(b);
-        std::memcpy(b.data(), &hm, sizeof hm);
+        finish_blob(b, hm);
     }
 
     // ---- algorithmic work of reaction.rs:356-391 per cell (the reference's operations) ----------
@@ -534,7 +565,10 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     }
     auto arrh_work = [&](const Arrhenius& a) {
         double f = 1;  // min
-        if (a.has_x) { f += (a.beta != 0) + (a.mEa != 0) + (a.beta != 0 && a.mEa != 0) + (a.lnA != 0); add_work(w, 0, 1); }
+        if (a.has_x) {
+            f += a.has_beta_rem + (a.mEa != 0) + (a.has_beta_rem && a.mEa != 0) + (a.lnA != 0);
+            add_work(w, 0, 1);
+        }
         if (a.factor != kNone) f += 1;
         add_work(w, f);
     };
@@ -644,8 +678,7 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
     std::memset(&h, 0, sizeof h);
     h.K = K; h.n_pairs = n_pairs; h.T0 = T0;
     std::vector<uint8_t>& blob = m.transport_blob;
-    blob.clear();
-    append(blob, &h, 1);
+    begin_blob(blob, h);
     h.off_cond = align_blob(blob); append(blob, cond.data(), cond.size());
     h.off_visc = align_blob(blob); append(blob, visc.data(), visc.size());
     h.off_W = align_blob(blob); append(blob, Wc.data(), Wc.size());
@@ -653,12 +686,7 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
     h.off_A2 = align_blob(blob); append(blob, A2.data(), A2.size());
     h.off_AB = align_blob(blob); append(blob, AB.data(), AB.size());
     h.off_B2 = align_blob(blob); append(blob, B2.data(), B2.size());
-    {
-        MathTables mt = make_math_tables();
-        h.off_math = align_blob(blob); append(blob, &mt, 1);
-    }
-    h.total_bytes = align_blob(blob);
-    std::memcpy(blob.data(), &h, sizeof h);
+    finish_blob(blob, h);
 
     // ---- mixed-precision (all FP32) transport tables ----------------------------------------------
     {
@@ -667,8 +695,7 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
         std::memset(&hm, 0, sizeof hm);
         hm.K = K; hm.n_pairs = n_pairs; hm.T0 = T0;
         std::vector<uint8_t>& b = m.transport_mixed_blob;
-        b.clear();
-        append(b, &hm, 1);
+        begin_blob(b, hm);
         auto put = [&](const std::vector<double>& v) {
             int32_t off = align_blob(b);
             std::vector<float> f = f32(v);
@@ -677,8 +704,7 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
         };
         hm.off_cond = put(cond); hm.off_visc = put(visc); hm.off_W = put(Wc); hm.off_diff = put(diff);
         hm.off_A2 = put(A2); hm.off_AB = put(AB); hm.off_B2 = put(B2);
-        hm.total_bytes = align_blob(b);
-        std::memcpy(b.data(), &hm, sizeof hm);
+        finish_blob(b, hm);
     }
 
     // ---- algorithmic work of transport.rs:179-210 per cell ---------------------------------------

@@ -17,11 +17,12 @@ constexpr int kAlign = 16;   // section alignment inside a blob (bulk TMA granul
 // Temperature factor of arrhenius() (reaction.rs:117-125).
 enum Factor : int32_t { kNone = 0, kRcpT2, kRcpT, kT4, kT3, kT2, kT };
 
-// k = min(f32::MAX, factor * exp(beta*lnT + mEa*rcpT + lnA))  when has_x,
-//     min(f32::MAX, factor * A)                                  otherwise (A alone without factor).
+// k = min(f32::MAX, exp(beta*lnT + mEa*rcpT + lnA))  when has_x, where beta = b' + m also carries the
+//     integer power T^m that reaction.rs:117-125 peels off (exp(m lnT) = T^m to a few ulps),
+//     min(f32::MAX, factor * A)                          otherwise (A alone without factor).
 struct Arrhenius {
     double beta, mEa, lnA, A;
-    int32_t factor, has_x, pad0, pad1;
+    int32_t factor, has_x, has_beta_rem, pad1;  // has_beta_rem: the reference program has a b' lnT term
 };
 
 enum FalloffFlags : int32_t {
@@ -41,9 +42,11 @@ struct Falloff {
     int32_t flags, pad;
 };
 
+// Reactions are stored grouped by model (RatesHeader::group_end), each group in the mechanism's order;
+// orig is the reaction's index in the mechanism (per-reaction outputs).
 struct Reaction {
     int32_t model, minus_sigma_net, eff_row, falloff;  // eff_row/falloff: -1 when absent
-    int32_t n_r, n_p, n_net, pad;
+    int32_t n_r, n_p, n_net, orig;
     uint16_t r_k[kMaxSide], p_k[kMaxSide], net_k[kMaxNet];
     int8_t r_n[kMaxSide], p_n[kMaxSide], net_n[kMaxNet];
     Arrhenius k;                        // forward / high-pressure rate constant
@@ -70,9 +73,16 @@ struct MathTables {
     double pad;
 };
 
+// Every blob starts with its MathTables, so that a kernel finds them at the base of its dynamic shared
+// memory whether the rest of the blob is staged there or read from global memory; the blob's header
+// follows at kMathBytes.
+constexpr int kMathBytes = (int)sizeof(MathTables);
+static_assert(kMathBytes % kAlign == 0, "math tables must keep the blob sections aligned");
+
 struct RatesHeader {
     int32_t K, A, R, n_eff, n_falloff, total_bytes;
     int32_t off_species, off_reactions, off_falloff, off_eff, off_math, pad;
+    int32_t group_end[6], pad1[2];  // reactions [group_end[m-1], group_end[m]) have model m
     double M3, cbrt_max, C0, rcp_C0, ln10_04, ln10_075, pad2[2];
 };
 

@@ -28,7 +28,7 @@ struct FalloffF {
 
 struct ReactionF {
     int32_t model, minus_sigma_net, eff_row, falloff;
-    int32_t n_r, n_p, n_net, pad;
+    int32_t n_r, n_p, n_net, orig;
     uint16_t r_k[kMaxSide], p_k[kMaxSide], net_k[kMaxNet];
     int8_t r_n[kMaxSide], p_n[kMaxSide], net_n[kMaxNet];
     ArrheniusF k;
@@ -47,12 +47,13 @@ struct SpeciesF {
 struct RatesMixedHeader {
     int32_t K, A, R, n_eff, n_falloff, total_bytes;
     int32_t off_species, off_reactions, off_falloff, off_eff, off_math, pad;
+    int32_t group_end[6], pad1[2];  // as RatesHeader::group_end
     double M3, cbrt_max, C0, rcp_C0;
     float ln10_04, ln10_075, pad2[2];
 };
 
 struct TransportMixedHeader {
-    int32_t K, n_pairs, total_bytes, pad;
+    int32_t K, n_pairs, total_bytes, off_math;
     int32_t off_cond, off_visc, off_W, off_diff, off_A2, off_AB, off_B2, pad2;
     double T0, pad3;
 };
