@@ -35,7 +35,10 @@ EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_que
            "cb_transport_fit", "cb_transport_coefficients", "cb_rates_f64", "cb_reaction_rates_f64",
            "cb_transport_f64", "cb_rates_transport_f64", "cb_work_model", "cb_synchronize", "cb_last_error",
            "cb_version", "cb_device_fp64_peak", "cb_fp64_math", "cb_rates_mixed", "cb_transport_mixed",
-           "cb_rates_transport_mixed"]
+           "cb_rates_transport_mixed", "cb_generate_cells", "cb_surrogate_create", "cb_surrogate_destroy",
+           "cb_surrogate_query", "cb_surrogate_generate", "cb_surrogate_train", "cb_surrogate_transport",
+           "cb_surrogate_get_params", "cb_surrogate_set_params", "cb_surrogate_normalisation",
+           "cb_surrogate_evaluate"]
 
 
 class CombustionError(RuntimeError):

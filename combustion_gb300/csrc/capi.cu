@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/combustion_gb300.h"
+#include "capi_internal.h"
 #include "kernels.h"
 #include "mechanism.hpp"
 #include "tables.h"
@@ -214,7 +215,42 @@ void to_work(const cbg::Work& w, cb_work* o) {
     o->bytes_in = w.bytes_in; o->bytes_out = w.bytes_out;
 }
 
+template <int KM>
+int gather_launch(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
+                  const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st) {
+    cbg::TransportArgs<KM> a;
+    std::memset(&a, 0, sizeof a);
+    for (int q = 0; q < m->host.K + 3; q++) a.in[q] = in[q];
+    for (int q = 0; q < m->host.K + 2; q++) a.out[q] = out[q];
+    a.flags = (flags & CB_UNIFORM_PRESSURE) | cbg::kFromRates | (compact ? cbg::kCompactOut : 0u);
+    a.index = index;
+    a.count = count;
+    cudaError_t e = cbg::launch_transport(KM, m->d_transport, (uint32_t)m->host.transport_blob.size(), &a, n, st,
+                                          m->d_status);
+    return e == cudaSuccess ? CB_OK : cuda_fail(e, "transport kernel (gathered cells)");
+}
+
 }  // namespace
+
+namespace cbi {
+int fail(int code, const std::string& msg) { return ::fail(code, msg); }
+int cuda_fail(cudaError_t e, const char* what) { return ::cuda_fail(e, what); }
+MechView view(const cb_mech* m) {
+    return MechView{m->host.K, m->host.A, m->device, m->host.transport_ready ? 1 : 0, m->host.T0};
+}
+int transport_gather(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
+                     const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st) {
+    if (!m->host.transport_ready) return ::fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
+    if (n == 0) return CB_OK;
+    switch (m->kmax) {
+    case 16: return gather_launch<16>(m, n, in, out, index, count, compact, flags, st);
+    case 64: return gather_launch<64>(m, n, in, out, index, count, compact, flags, st);
+    case 256: return gather_launch<256>(m, n, in, out, index, count, compact, flags, st);
+    default: return ::fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
+    }
+}
+int check_status(cb_mech* m) { return ::check_status(m); }
+}  // namespace cbi
 
 extern "C" {
 

@@ -31,12 +31,18 @@ struct ReactionRatesArgs {
 // (P/R, R/P, T, V, n...) from which sum n = (P/R * V) / T and T/T0 are derived per cell.
 constexpr uint32_t kUniformPressure = 2u;
 constexpr uint32_t kFromRates = 4u;
+// Gathered cells (the transport surrogate's fallback and audit): cell j of the launch is input cell
+// index[j] & kIndexMask, its outputs go to that cell too or, with kCompactOut, to position j.
+constexpr uint32_t kCompactOut = 8u;
+constexpr uint32_t kIndexMask = 0x7fffffffu;
 
 template <int KMAX>
 struct TransportArgs {
     const double* in[KMAX + 3];  // sum n, T/T0, n_0 .. n_{K-2} (or the rates inputs with kFromRates)
     double* out[KMAX + 2];       // lambda/lambda0, mu/mu0, rhoD_k/mu0
     uint32_t flags;
+    const uint32_t* index;       // gathered cells (null: cell j is input j)
+    const uint32_t* count;       // number of gathered cells, read on the device (null: n)
 };
 
 // Smallest compiled capacity holding K species (0 if none).

@@ -1,0 +1,621 @@
+// Kernels of the learned transport surrogate (declarations and roles in surrogate_kernels.cuh).
+//
+// The GEMM is D[M][N] = A[M][K] B[N][K]^T over BF16 operands with an FP32 accumulator in tensor memory:
+// one 128 x BN output tile per block, operands streamed through a ring of shared-memory stages by TMA
+// (128-byte swizzle, K-major), tcgen05.mma issued by one thread, the accumulator read back by four
+// epilogue warps (one TMEM lane, i.e. one output row, per thread) which apply the layer's element-wise
+// work before anything is written to global memory. Every mbarrier wait is bounded: a wait that runs
+// out sets a status bit, lets in-flight copies land and the block still frees its tensor memory.
+#include <cuda_bf16.h>
+
+#include "device_common.cuh"
+#include "surrogate_kernels.cuh"
+#include "umma.cuh"
+
+namespace cbg {
+namespace sur {
+
+__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// 32 values of one row, columns [n, n + 32), as BF16 (64 contiguous bytes).
+__device__ __forceinline__ void store_row_bf16(__nv_bfloat16* base, int ld, int row, int n, const float* a) {
+    uint4* dst = reinterpret_cast<uint4*>(base + (size_t)row * ld + n);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        dst[j] = make_uint4(pack_bf16(a[8 * j], a[8 * j + 1]), pack_bf16(a[8 * j + 2], a[8 * j + 3]),
+                            pack_bf16(a[8 * j + 4], a[8 * j + 5]), pack_bf16(a[8 * j + 6], a[8 * j + 7]));
+}
+
+// The same values into the transposed matrix: consecutive threads hold consecutive rows, so each of
+// the 32 stores of a warp covers 64 contiguous bytes.
+__device__ __forceinline__ void store_col_bf16(__nv_bfloat16* base, int ld, int row, int n, const float* a) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) base[(size_t)(n + j) * ld + row] = __float2bfloat16_rn(a[j]);
+}
+
+template <int BN, int EPI>
+__device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int warp, int lane, int m0, int n0) {
+    const int q = warp & 3;  // the TMEM lane quarter this warp may read
+    const int row = m0 + q * 32 + lane;
+    const int trow0 = (p.dyn & kDynTarget) ? *p.row0 : 0;
+    float lsum = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 32) {
+        float v[32];
+        umma::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
+        const int n = n0 + c;
+        if constexpr (EPI == kEpiPartial) {
+            float4* dst = reinterpret_cast<float4*>(p.outf + ((size_t)blockIdx.z * p.M + row) * p.ld_outf + n);
+#pragma unroll
+            for (int j = 0; j < 8; j++) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        } else if constexpr (EPI == kEpiLinear) {
+            float4* dst = reinterpret_cast<float4*>(p.outf + (size_t)row * p.ld_outf + n);
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                dst[j] = make_float4(v[4 * j] + p.bias[n + 4 * j], v[4 * j + 1] + p.bias[n + 4 * j + 1],
+                                     v[4 * j + 2] + p.bias[n + 4 * j + 2], v[4 * j + 3] + p.bias[n + 4 * j + 3]);
+        } else if constexpr (EPI == kEpiHidden) {
+            float a[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const float z = v[j] + p.bias[n + j];
+                v[j] = z;
+                a[j] = z * sigmoidf_(z);
+            }
+            if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
+            store_row_bf16(p.out2, p.ld_out2, row, n, a);
+            if (p.outT) store_col_bf16(p.outT, p.ld_outT, row, n, a);
+        } else if constexpr (EPI == kEpiLoss) {
+            const float* t = p.target + (size_t)(trow0 + row) * p.ld_target;
+            float a[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const float y = v[j] + p.bias[n + j];
+                const float d = (n + j < p.n_valid) ? y - t[n + j] : 0.f;
+                lsum = fmaf(d, d, lsum);
+                a[j] = d * p.grad_scale;
+            }
+            store_row_bf16(p.out, p.ld_out, row, n, a);
+            store_col_bf16(p.outT, p.ld_outT, row, n, a);
+        } else if constexpr (EPI == kEpiDgrad) {
+            const uint4* zp = reinterpret_cast<const uint4*>(p.zin + (size_t)row * p.ld_zin + n);
+            float a[32];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint4 w = zp[j];
+                const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
+                    const float z0 = __low2float(b), z1 = __high2float(b);
+                    const float s0 = sigmoidf_(z0), s1 = sigmoidf_(z1);
+                    const int k = 8 * j + 2 * h;
+                    a[k] = v[k] * (s0 * fmaf(z0, 1.f - s0, 1.f));
+                    a[k + 1] = v[k + 1] * (s1 * fmaf(z1, 1.f - s1, 1.f));
+                }
+            }
+            store_row_bf16(p.out, p.ld_out, row, n, a);
+            store_col_bf16(p.outT, p.ld_outT, row, n, a);
+        }
+    }
+    if constexpr (EPI == kEpiLoss) {  // one partial per warp: no barrier among the epilogue warps
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+        if (lane == 0) p.loss[blockIdx.x * 4 + q] = lsum;
+    }
+}
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmParams p) {
+    constexpr uint32_t kA = kBM * 128, kB = BN * 128, kStage = kA + kB;
+    constexpr int STAGES = (kGemmSmem - 1024) / (int)kStage;
+    static_assert(STAGES >= 2, "operand ring needs two stages");
+    constexpr uint32_t kCols = BN;  // TMEM columns: a power of two >= 32
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full;
+    __shared__ uint32_t tmem_s;
+    const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
+    const int kb0 = (int)(((long long)blockIdx.z * p.k_blocks) / p.splits);
+    const int nkb = (int)(((long long)(blockIdx.z + 1) * p.k_blocks) / p.splits) - kb0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            umma::mbar_init(smem_u32(&full[s]), 1);
+            umma::mbar_init(smem_u32(&empty[s]), 1);
+        }
+        umma::mbar_init(smem_u32(&acc_full), 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 1) {
+        umma::tmem_alloc(smem_u32(&tmem_s), kCols);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_s;
+    bool ok = true;
+    if (warp == 0) {
+        if (lane == 0) {  // TMA producer
+            const int off = p.dyn ? *p.row0 : 0;
+            const int ay = p.a_y0 + m0 + ((p.dyn & kDynAy) ? off : 0);
+            const int bx = p.b_x0 + ((p.dyn & kDynBx) ? off : 0);
+            int issued = 0;
+            for (int i = 0; i < nkb; i++) {
+                const int s = i % STAGES;
+                if (i >= STAGES && !umma::mbar_wait(smem_u32(&empty[s]), ((i / STAGES) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t bar = smem_u32(&full[s]), sa = base + (uint32_t)s * kStage;
+                const int kx = (kb0 + i) * kBK;
+                umma::mbar_expect_tx(bar, kStage);
+                umma::tma_load_2d(sa, &ta, bar, p.a_x0 + kx, ay);
+                umma::tma_load_2d(sa + kA, &tb, bar, bx + kx, p.b_y0 + n0);
+                issued = i + 1;
+            }
+            if (!ok)  // let the copies already issued land before the block exits
+                for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; i++)
+                    umma::mbar_wait(smem_u32(&full[i % STAGES]), (i / STAGES) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN);
+            for (int i = 0; i < nkb; i++) {
+                const int s = i % STAGES;
+                if (!umma::mbar_wait(smem_u32(&full[s]), (i / STAGES) & 1)) {
+                    ok = false;
+                    break;
+                }
+                umma::fence_after_sync();
+                const uint32_t sa = base + (uint32_t)s * kStage, sb = sa + kA;
+#pragma unroll
+                for (int k = 0; k < kBK / 16; k++)
+                    umma::mma_bf16(tmem, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k), idesc,
+                                   (i | k) != 0);
+                umma::mma_commit(smem_u32(&empty[s]));  // frees the stage once these MMAs are done
+            }
+            umma::mma_commit(smem_u32(&acc_full));  // every MMA issued above has completed
+        }
+    } else {  // epilogue warps
+        ok = umma::mbar_wait(smem_u32(&acc_full), 0);
+        umma::fence_after_sync();
+        if (ok) epilogue<BN, EPI>(p, tmem, warp, lane, m0, n0);
+    }
+    if (!ok) atomicOr(p.status, kStatusGemmTimeout);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(tmem, kCols);
+    }
+}
+
+template <int BN, int EPI>
+cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
+    dim3 grid(p.M / kBM, p.N / BN, p.splits);
+    gemm_kernel<BN, EPI><<<grid, kGemmThreads, kGemmSmem, st>>>(a, b, p);
+    return cudaGetLastError();
+}
+
+template <int EPI>
+cudaError_t gemm_bn(int BN, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
+    switch (BN) {
+    case 64: return launch_gemm<64, EPI>(a, b, p, st);
+    case 128: return launch_gemm<128, EPI>(a, b, p, st);
+    case 256: return launch_gemm<256, EPI>(a, b, p, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int EPI>
+cudaError_t setup_epi() {
+    cudaError_t e = cudaFuncSetAttribute(gemm_kernel<64, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(gemm_kernel<128, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(gemm_kernel<256, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    return e;
+}
+
+cudaError_t gemm_setup() {
+    cudaError_t e = setup_epi<kEpiPartial>();
+    if (e == cudaSuccess) e = setup_epi<kEpiHidden>();
+    if (e == cudaSuccess) e = setup_epi<kEpiLoss>();
+    if (e == cudaSuccess) e = setup_epi<kEpiDgrad>();
+    if (e == cudaSuccess) e = setup_epi<kEpiLinear>();
+    return e;
+}
+
+cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
+    if (p.M % kBM || p.N % BN || p.splits < 1 || p.splits > p.k_blocks) return cudaErrorInvalidValue;
+    switch (epi) {
+    case kEpiPartial: return gemm_bn<kEpiPartial>(BN, a, b, p, st);
+    case kEpiHidden: return gemm_bn<kEpiHidden>(BN, a, b, p, st);
+    case kEpiLoss: return gemm_bn<kEpiLoss>(BN, a, b, p, st);
+    case kEpiDgrad: return gemm_bn<kEpiDgrad>(BN, a, b, p, st);
+    case kEpiLinear: return gemm_bn<kEpiLinear>(BN, a, b, p, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients).
+__global__ void reduce_partials_kernel(const float* __restrict__ ws, int splits, int M, int N, int transpose,
+                                       float* __restrict__ grad) {
+    const size_t MN = (size_t)M * N;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN; i += (size_t)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int z = 0; z < splits; z++) s += ws[z * MN + i];
+        const size_t m = i / N, n = i % N;
+        grad[transpose ? n * M + m : i] = s;
+    }
+}
+
+cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st) {
+    const size_t MN = (size_t)M * N;
+    reduce_partials_kernel<<<(unsigned)((MN + 255) / 256), 256, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0, grad);
+    return cudaGetLastError();
+}
+
+// out[r] = sum of row r of a BF16 matrix (bias gradients from the transposed output gradients), one
+// block per row, fixed reduction order.
+__global__ void row_sums_kernel(const __nv_bfloat16* __restrict__ T, int cols, int ld, float* __restrict__ out) {
+    __shared__ float part[256];
+    const __nv_bfloat16* r = T + (size_t)blockIdx.x * ld;
+    float s = 0.f;
+    for (int c = threadIdx.x * 8; c < cols; c += 256 * 8) {
+        const uint4 w = *reinterpret_cast<const uint4*>(r + c);
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
+            s += __low2float(b) + __high2float(b);
+        }
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = part[0];
+}
+
+cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st) {
+    if (cols % 8 || ld % 8) return cudaErrorInvalidValue;
+    row_sums_kernel<<<rows, 256, 0, st>>>(T, cols, ld, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Adam on the FP32 master parameters (weights of every layer, then biases), writing the BF16 weights and
+// their transposes that the GEMMs read. The step counter lives on the device (CUDA-graph replays).
+__device__ __forceinline__ void write_bf16_weight(const AdamArgs& a, long long i, float w) {
+    int l = 0;
+    while (l + 1 < a.n_layers && i >= a.L[l + 1].w_off) l++;
+    const AdamLayer& L = a.L[l];
+    const long long r = i - L.w_off;
+    const int o = (int)(r / L.n_in), c = (int)(r % L.n_in);
+    const __nv_bfloat16 b = __float2bfloat16_rn(w);
+    L.W[(size_t)o * L.n_in + c] = b;
+    L.WT[(size_t)c * L.n_out + o] = b;
+}
+
+__global__ void adam_kernel(const AdamArgs a) {
+    const int t = *a.step + 1;
+    const float frac = a.total_steps > 1 ? fminf(1.f, (float)(t - 1) / (float)(a.total_steps - 1)) : 1.f;
+    const float lr = a.lr_final + 0.5f * (a.lr - a.lr_final) * (1.f + cospif(frac));
+    const float bc1 = 1.f - powf(a.b1, (float)t), bc2 = 1.f - powf(a.b2, (float)t);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n_params;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float g = a.g[i];
+        const float m = a.b1 * a.m[i] + (1.f - a.b1) * g;
+        const float v = a.b2 * a.v[i] + (1.f - a.b2) * g * g;
+        a.m[i] = m;
+        a.v[i] = v;
+        const float w = a.p[i] - lr * (m / bc1) / (sqrtf(v / bc2) + a.eps);
+        a.p[i] = w;
+        if (i < a.n_weights) write_bf16_weight(a, i, w);
+    }
+}
+
+cudaError_t adam(const AdamArgs& a, cudaStream_t st) {
+    adam_kernel<<<592, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+__global__ void cast_weights_kernel(const AdamArgs a) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n_weights;
+         i += (long long)gridDim.x * blockDim.x)
+        write_bf16_weight(a, i, a.p[i]);
+}
+
+cudaError_t cast_weights(const AdamArgs& a, cudaStream_t st) {
+    cast_weights_kernel<<<592, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Mean squared error of the step (fixed summation order), next step number and batch position.
+__global__ void finish_step_kernel(const float* loss_part, int n_part, float norm, float* losses, int* step,
+                                   int* row0, int batch, int n_batches) {
+    __shared__ float part[256];
+    float s = 0.f;
+    for (int i = threadIdx.x; i < n_part; i += 256) s += loss_part[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int t = *step;
+        if (losses) losses[t] = part[0] * norm;
+        *step = t + 1;
+        *row0 = ((t + 1) % n_batches) * batch;
+    }
+}
+
+cudaError_t finish_step(const float* loss_part, int n_part, float norm, float* losses, int* step, int* row0,
+                        int batch, int n_batches, cudaStream_t st) {
+    finish_step_kernel<<<1, 256, 0, st>>>(loss_part, n_part, norm, losses, step, row0, batch, n_batches);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Seeded cells on the device, the same counter-based draws as the host generator
+// (combustion_gb300/synthetic.py): SplitMix64 uniforms per (seed, stream, counter), Box-Muller normals,
+// Marsaglia-Tsang Gamma(alpha + 1) boosted by U^(1/alpha), mole fractions from normalised Gamma draws.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform_(uint64_t key, int stream, uint64_t idx) {
+    const uint64_t base = key + ((uint64_t)(stream & 0xFFFFFF) << 40);
+    return (double)(mix64(base + idx * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
+}
+__device__ double normal_(uint64_t key, int stream, uint64_t idx) {
+    const double u1 = uniform_(key, stream, 2 * idx), u2 = uniform_(key, stream, 2 * idx + 1);
+    return sqrt(-2.0 * log1p(-u1)) * cos(2.0 * 3.141592653589793 * u2);
+}
+__device__ double gamma_(double alpha, uint64_t key, int stream, uint64_t idx) {
+    const double a = alpha < 1.0 ? alpha + 1.0 : alpha;
+    const double d = a - 1.0 / 3.0, c = 1.0 / sqrt(9.0 * d);
+    double out = 0.0;
+    for (int rnd = 0; rnd < 64; rnd++) {  // bounded rejection loop (acceptance is above 95 %)
+        const uint64_t sub = idx * 64 + rnd;
+        const double x = normal_(key, stream, sub);
+        const double u = uniform_(key, stream + 1, sub);
+        const double b = 1.0 + c * x;
+        const double v = b * b * b;
+        if (v > 0 && log(fmax(u, 1e-300)) < 0.5 * x * x + d - d * v + d * log(v)) {
+            out = d * v;
+            break;
+        }
+    }
+    if (alpha < 1.0) out *= pow(uniform_(key, stream + 2, idx), 1.0 / alpha);
+    return out;
+}
+
+__global__ void generate_cells_kernel(const CellGenArgs a) {
+    const uint64_t key = mix64(a.seed);
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n; c += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t idx = a.offset + c;
+        const double T = a.T_lo + (a.T_hi - a.T_lo) * uniform_(key, 1, idx);
+        const double P = a.fixed_pressure ? a.P_fixed
+                                          : 101325.0 * exp(a.lnP_lo + (a.lnP_hi - a.lnP_lo) * uniform_(key, 2, idx));
+        const double pressure_R = P / a.R;
+        double sum = 0.0;  // the bulk species' draw only enters the sum
+        for (int k = 0; k < a.K; k++) {
+            const double g = fmax(gamma_(a.alpha, key, 16 + 4 * k, idx), 1e-300);
+            sum += g;
+            if (k < a.K - 1) a.out[4 + k][c] = g;
+        }
+        const double total = pressure_R * 1.0 / T;
+        for (int k = 0; k < a.K - 1; k++) a.out[4 + k][c] = a.out[4 + k][c] / sum * total;
+        a.out[0][c] = pressure_R;
+        a.out[1][c] = 1.0 / pressure_R;
+        a.out[2][c] = T;
+        a.out[3][c] = 1.0;
+    }
+}
+
+cudaError_t generate_cells(const CellGenArgs& a, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    size_t grid = (a.n + 127) / 128;
+    if (grid > 152 * 16) grid = 152 * 16;
+    generate_cells_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Order-preserving map of floats to ints (for atomic min / max).
+__device__ __forceinline__ int ordered(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+
+// Network inputs of one cell (rates layout): log(T/T0), log(P / 1 atm), mole fractions X_0 .. X_{K-1}
+// with the bulk fraction from the total amount (P/R V) / T like the transport kernel's.
+__device__ __forceinline__ float raw_feature(const FeatureArgs& a, size_t c, int j, double logT, double logP,
+                                             double rN, double bulk) {
+    if (j == 0) return (float)logT;
+    if (j == 1) return (float)logP;
+    const int k = j - 2;
+    return (float)((k < a.K - 1 ? a.in[4 + k][c] : bulk) * rN);
+}
+
+__global__ void features_kernel(const FeatureArgs a) {
+    __shared__ int lo_s[kMaxOut], hi_s[kMaxOut];
+    const bool hull = a.hull_lo != nullptr;
+    if (hull) {
+        for (int j = threadIdx.x; j < a.n_feat; j += blockDim.x) {
+            lo_s[j] = 0x7fffffff;
+            hi_s[j] = (int)0x80000000;
+        }
+        __syncthreads();
+    }
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.rows; c += (size_t)gridDim.x * blockDim.x) {
+        __nv_bfloat16* xr = a.X + (a.row0 + c) * a.n_in;
+        if (c >= a.n) {  // padding row
+            for (int j = 0; j < a.n_in; j += 8) *reinterpret_cast<uint4*>(xr + j) = make_uint4(0, 0, 0, 0);
+            if (a.XT)
+                for (int j = 0; j < a.n_in; j++) a.XT[(size_t)j * a.ldXT + a.row0 + c] = __float2bfloat16_rn(0.f);
+            continue;
+        }
+        const double pR = a.uniform_pressure ? a.in[0][0] : a.in[0][c];
+        const double T = a.in[2][c], V = a.in[3][c];
+        const double N = pR * V / T;
+        double s = 0.0;
+        for (int k = 0; k < a.K - 1; k++) s += a.in[4 + k][c];
+        const double bulk = N - s, rN = 1.0 / N;
+        const double logT = log(T / a.T0), logP = log(pR * a.R_over_P0);
+        bool inside = true;
+        for (int j0 = 0; j0 < a.n_in; j0 += 8) {
+            float x[8];
+#pragma unroll
+            for (int h = 0; h < 8; h++) {
+                const int j = j0 + h;
+                float f = 0.f;
+                if (j < a.n_feat) {
+                    f = raw_feature(a, c, j, logT, logP, rN, bulk);
+                    if (a.raw) a.raw[c * a.n_feat + j] = f;
+                    if (a.lo) inside &= (f >= a.lo[j]) & (f <= a.hi[j]);
+                    if (hull) {
+                        atomicMin(&lo_s[j], ordered(f));
+                        atomicMax(&hi_s[j], ordered(f));
+                    }
+                    f = (f - a.mean[j]) * a.rstd[j];
+                }
+                x[h] = f;
+            }
+            *reinterpret_cast<uint4*>(xr + j0) =
+                make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+            if (a.XT)
+#pragma unroll
+                for (int h = 0; h < 8; h++) a.XT[(size_t)(j0 + h) * a.ldXT + a.row0 + c] = __float2bfloat16_rn(x[h]);
+        }
+        if (a.fail_idx) {
+            if (!inside) {
+                a.fail_idx[atomicAdd(a.fail_count, 1u)] = (uint32_t)c;
+            } else if (a.audit_stride && c % a.audit_stride == a.audit_phase) {
+                const uint32_t slot = atomicAdd(a.audit_count, 1u);
+                if (slot < a.audit_cap) a.audit_idx[slot] = (uint32_t)c;
+            }
+        }
+    }
+    if (hull) {
+        __syncthreads();
+        for (int j = threadIdx.x; j < a.n_feat; j += blockDim.x) {
+            atomicMin(&a.hull_lo[j], lo_s[j]);
+            atomicMax(&a.hull_hi[j], hi_s[j]);
+        }
+    }
+}
+
+cudaError_t features(const FeatureArgs& a, cudaStream_t st) {
+    if (a.rows == 0) return cudaSuccess;
+    size_t grid = (a.rows + 127) / 128;
+    if (grid > 152 * 8) grid = 152 * 8;
+    features_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Training targets: normalised logs of the plain kernel's transport outputs.
+__global__ void targets_kernel(const TargetArgs a) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n; c += (size_t)gridDim.x * blockDim.x) {
+        float* y = a.Y + (a.row0 + c) * a.n_out;
+        for (int j0 = 0; j0 < a.n_out; j0 += 4) {
+            float t[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int j = j0 + h;
+                float v = 0.f;
+                if (j < a.n_feat) {
+                    const float l = (float)log(a.out[j][c]);
+                    if (a.raw) a.raw[c * a.n_feat + j] = l;
+                    v = (l - a.mean[j]) * a.rstd[j];
+                }
+                t[h] = v;
+            }
+            *reinterpret_cast<float4*>(y + j0) = make_float4(t[0], t[1], t[2], t[3]);
+        }
+    }
+}
+
+cudaError_t targets(const TargetArgs& a, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    size_t grid = (a.n + 127) / 128;
+    if (grid > 152 * 8) grid = 152 * 8;
+    targets_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Network outputs to transport properties: out_j = exp(mean_j + std_j y_j) in the plain kernel's layout.
+__global__ void outputs_kernel(const OutputArgs a) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n; c += (size_t)gridDim.x * blockDim.x) {
+        const float* y = a.Y + c * a.ldY;
+        for (int j0 = 0; j0 < a.n_feat; j0 += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(y + j0);
+            const float vs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int j = j0 + h;
+                if (j < a.n_feat) a.out[j][c] = (double)__expf(fmaf(a.std[j], vs[h], a.mean[j]));
+            }
+        }
+    }
+}
+
+cudaError_t outputs(const OutputArgs& a, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    size_t grid = (a.n + 127) / 128;
+    if (grid > 152 * 8) grid = 152 * 8;
+    outputs_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// Audited cells: relative error of the surrogate against the plain kernel (per output group), then the
+// plain values replace the surrogate's.
+__global__ void audit_kernel(const AuditArgs a, size_t cap) {
+    size_t n = *a.count;
+    if (n > cap) n = cap;
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = a.idx[j];
+        float mx[3] = {0.f, 0.f, 0.f};
+        double sq[3] = {0.0, 0.0, 0.0};
+        for (int o = 0; o < a.n_feat; o++) {
+            const double ref = a.plain[(size_t)o * a.cap + j];
+            const double e = fabs(a.out[o][c] - ref) / fabs(ref);
+            const int g = o < 2 ? o : 2;
+            mx[g] = fmaxf(mx[g], (float)e);
+            sq[g] += e * e;
+            a.out[o][c] = ref;
+        }
+        for (int g = 0; g < 3; g++) {
+            atomicMax(&a.max_err[g], __float_as_uint(mx[g]));
+            atomicAdd(&a.sum_sq[g], sq[g]);
+        }
+    }
+}
+
+cudaError_t audit(const AuditArgs& a, size_t cap, cudaStream_t st) {
+    if (cap == 0) return cudaSuccess;
+    size_t grid = (cap + 127) / 128;
+    if (grid > 1024) grid = 1024;
+    audit_kernel<<<(unsigned)grid, 128, 0, st>>>(a, cap);
+    return cudaGetLastError();
+}
+
+}  // namespace sur
+}  // namespace cbg

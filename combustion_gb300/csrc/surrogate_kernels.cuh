@@ -1,0 +1,133 @@
+// Kernels of the learned transport surrogate: a BF16 tcgen05 GEMM with fused epilogues (bias + SiLU,
+// MSE loss gradient, SiLU backward, split-K weight-gradient partials), and the element-wise kernels
+// around it (cell generator, features, targets, outputs, gate audit, Adam).
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cbg {
+namespace sur {
+
+constexpr int kGemmThreads = 192;  // warp 0: TMA producer, warp 1: TMEM owner + MMA issuer, warps 2-5: epilogue
+constexpr int kBM = 128;           // rows per tile (one M = 128 MMA, one TMEM lane per row)
+constexpr int kBK = 64;            // K per pipeline stage: one 128-byte swizzle row of BF16
+constexpr int kGemmSmem = 193 * 1024;  // operand ring (stages x (A + B tile)) + alignment; one block per SM
+constexpr int kMaxIn = 259;        // rates-layout inputs for up to 256 species
+constexpr int kMaxOut = 258;       // transport outputs for up to 256 species
+constexpr int kMaxLayers = 8;
+
+enum Epilogue : int {
+    kEpiPartial = 0,  // FP32 accumulator tile to ws[split][M][N] (weight-gradient partials)
+    kEpiHidden = 1,   // z = acc + bias: Z (optional), silu(z) row-major, silu(z) transposed (optional)
+    kEpiLoss = 2,     // y = acc + bias: d = y - target (valid columns), loss partial, d * scale row-major + transposed
+    kEpiDgrad = 3,    // dz = acc * silu'(z_in): row-major + transposed
+    kEpiLinear = 4,   // y = acc + bias to FP32 row-major
+};
+
+enum DynOffset : int { kDynAy = 1, kDynBx = 2, kDynTarget = 4 };
+
+struct GemmParams {
+    int M, N;               // output tile grid: M / 128 by N / BN blocks
+    int k_blocks, splits;   // 64-wide K blocks in total; split z takes [z KB / S, (z + 1) KB / S)
+    int a_x0, a_y0, b_x0, b_y0;  // TMA coordinate offsets (K, row) of A and B
+    const int* row0;        // device row offset added where `dyn` says (training batch position)
+    int dyn;
+    const float* bias;
+    __nv_bfloat16* out;  int ld_out;   // row-major BF16 [M][ld]
+    __nv_bfloat16* out2; int ld_out2;  // row-major BF16 [M][ld]
+    __nv_bfloat16* outT; int ld_outT;  // transposed BF16 [N][ld]
+    const __nv_bfloat16* zin; int ld_zin;  // pre-activations for the SiLU backward
+    const float* target; int ld_target; int n_valid; float grad_scale;
+    float* loss;            // one partial per epilogue warp: [row tile][4]
+    float* outf; int ld_outf;  // FP32 output
+    int* status;
+};
+
+enum SurStatus : int { kStatusGemmTimeout = 2 };
+
+struct CellGenArgs {
+    double* out[kMaxIn];  // P/R, R/P, T, V, n_0 .. n_{K-2}
+    size_t n, offset;
+    int K, fixed_pressure;
+    uint64_t seed;
+    double T_lo, T_hi, lnP_lo, lnP_hi, P_fixed, alpha, R;
+};
+
+struct FeatureArgs {
+    const double* in[kMaxIn];  // rates layout
+    size_t n, rows;            // cells; rows written (>= n, padding rows are zero)
+    int K, n_feat, n_in;
+    uint32_t uniform_pressure;
+    double T0, R_over_P0;
+    const float* mean; const float* rstd;  // normalisation of the raw features
+    __nv_bfloat16* X; size_t row0;          // row-major [.][n_in], rows from row0
+    __nv_bfloat16* XT; size_t ldXT;         // transposed [n_in][ldXT] (optional)
+    float* raw;                             // raw features [n][n_feat] (optional, statistics)
+    int* hull_lo; int* hull_hi;             // order-preserving integer min / max of raw features (optional)
+    const float* lo; const float* hi;       // trust region (inference gate, optional)
+    uint32_t* fail_idx; uint32_t* fail_count;
+    uint32_t* audit_idx; uint32_t* audit_count; uint32_t audit_stride, audit_phase, audit_cap;
+};
+
+struct TargetArgs {
+    const double* out[kMaxOut];  // plain transport outputs
+    size_t n, row0;
+    int n_feat, n_out;
+    const float* mean; const float* rstd;
+    float* Y;                    // [.][n_out] normalised log outputs
+    float* raw;                  // [n][n_feat] log outputs (optional, statistics)
+};
+
+struct OutputArgs {
+    const float* Y; int ldY;
+    size_t n;
+    int n_feat;
+    const float* mean; const float* std;
+    double* out[kMaxOut];
+};
+
+struct AuditArgs {
+    const uint32_t* idx; const uint32_t* count;
+    const double* plain; size_t cap;  // [n_feat][cap] plain outputs of the audited cells
+    double* out[kMaxOut];
+    int n_feat;
+    unsigned* max_err;   // [3] FP32 bits (conductivity, viscosity, diffusion)
+    double* sum_sq;      // [3]
+};
+
+struct AdamLayer {
+    long long w_off;
+    int n_out, n_in;
+    __nv_bfloat16* W;
+    __nv_bfloat16* WT;
+};
+struct AdamArgs {
+    AdamLayer L[kMaxLayers];
+    int n_layers;
+    long long n_weights, n_params;
+    float lr, lr_final, b1, b2, eps;
+    int total_steps;
+    const int* step;
+    float* p; const float* g; float* m; float* v;
+};
+
+// Launchers (surrogate_kernels.cu). gemm_setup() raises the GEMM's shared-memory limit on the current
+// device; it runs before the first GEMM (and outside any stream capture).
+cudaError_t gemm_setup();
+cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st);
+cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st);
+cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st);
+cudaError_t adam(const AdamArgs& a, cudaStream_t st);
+cudaError_t finish_step(const float* loss_part, int n_part, float norm, float* losses, int* step, int* row0,
+                        int batch, int n_batches, cudaStream_t st);
+cudaError_t cast_weights(const AdamArgs& a, cudaStream_t st);
+cudaError_t generate_cells(const CellGenArgs& a, cudaStream_t st);
+cudaError_t features(const FeatureArgs& a, cudaStream_t st);
+cudaError_t targets(const TargetArgs& a, cudaStream_t st);
+cudaError_t outputs(const OutputArgs& a, cudaStream_t st);
+cudaError_t audit(const AuditArgs& a, size_t cap, cudaStream_t st);
+
+}  // namespace sur
+}  // namespace cbg

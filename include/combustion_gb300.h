@@ -163,6 +163,79 @@ int cb_fp64_math(int which, const double* x, double* y, size_t n, void* stream);
 
 /* Blocks until the mechanism's work on `stream` is done and reports any kernel-side failure. */
 int cb_synchronize(cb_mech* mech, void* stream);
+
+/* ---- Seeded synthetic cells on the device ----------------------------------------------------------
+ * No reference counterpart (the reference reads states from Cantera or its own reactor). T uniform on
+ * [T_min, T_max] K, P log-uniform on [P_min, P_max] atm (fixed when equal), V = 1 m^3, mole fractions
+ * Dirichlet(alpha) over all K species, n_k = X_k P V / (R T): the counter-based SplitMix64 draws of the
+ * package's host generator (cell `offset + i` of the seeded sequence). Outputs: K + 3 device arrays of
+ * n doubles in the rates layout. */
+typedef struct cb_cell_distribution {
+    double T_min, T_max;
+    double P_min, P_max;
+    double alpha;
+    uint64_t seed;
+} cb_cell_distribution;
+int cb_generate_cells(cb_mech* mech, size_t n, size_t offset, const cb_cell_distribution* dist,
+                      double* const* outputs, void* stream);
+
+/* ---- Learned transport surrogate -------------------------------------------------------------------
+ * No reference counterpart. A multilayer perceptron maps (log T/T0, log P/atm, X_0 .. X_{K-1}) to the
+ * logs of the plain transport outputs (lambda/lambda0, mu/mu0, rhoD_k/mu0), normalised per column.
+ * BF16 weights and activations, FP32 accumulation on the tcgen05 tensor cores, SiLU hidden layers,
+ * FP32 master weights trained by Adam on the MSE of the normalised outputs, with a cosine learning-rate
+ * decay from lr to lr_final. Training cells come from cb_generate_cells and their targets from the
+ * plain FP64 transport kernel. A per-cell trust gate (raw inputs inside the per-column range of the
+ * training cells) sends other cells to the plain kernel, and a sampled audit recomputes every
+ * audit_stride-th cell with the plain kernel, reports the surrogate's error on it and keeps the plain
+ * values. Inputs of every call: rates-layout device arrays (P/R, R/P, T, V, n_0 .. n_{K-2}). */
+typedef struct cb_surrogate cb_surrogate;
+typedef struct cb_surrogate_desc {
+    int32_t width;          /* hidden width, a multiple of 256 */
+    int32_t hidden_layers;  /* 1 .. 6 */
+    int32_t batch;          /* training rows per step, a multiple of 128 */
+    float lr, lr_final, beta1, beta2, eps;
+    uint64_t seed;          /* weight initialisation */
+} cb_surrogate_desc;
+typedef struct cb_surrogate_info {
+    int32_t n_features, n_in, n_out, width, hidden_layers, batch;
+    int64_t n_params, n_weights, n_train, steps_done;
+    int64_t weight_offset[8], bias_offset[8];  /* layer l: weights [dims[l+1]][dims[l]], then biases */
+    int32_t dims[9];
+} cb_surrogate_info;
+typedef struct cb_surrogate_stats {
+    uint64_t cells, fallback_cells, audited_cells;
+    double audit_max_rel_err[3];  /* conductivity, viscosity, diffusion coefficients */
+    double audit_rms_rel_err[3];
+} cb_surrogate_stats;
+#define CB_SURROGATE_NO_GATE 8u  /* network outputs for every cell: no trust gate, no audit */
+
+int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* desc, cb_surrogate** out);
+int cb_surrogate_destroy(cb_surrogate* s);
+int cb_surrogate_query(const cb_surrogate* s, cb_surrogate_info* info);
+/* Training set: n_train cells (rounded down to whole batches) from `dist`, their plain transport outputs,
+ * the normalisation of inputs and outputs and the trust region. Synchronous. */
+int cb_surrogate_generate(cb_surrogate* s, size_t n_train, const cb_cell_distribution* dist);
+/* `steps` Adam steps over the training set, replayed as one captured CUDA graph per step; losses (host,
+ * `steps` floats, may be NULL) receives each step's mean squared error. Synchronous. */
+int cb_surrogate_train(cb_surrogate* s, int32_t steps, float* losses);
+/* Transport outputs (K + 2 device arrays) of n cells: network, then gate fallback and audit. Flags:
+ * CB_UNIFORM_PRESSURE, CB_SURROGATE_NO_GATE. Returns when the outputs and `stats` (may be NULL) are
+ * final. */
+int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* inputs, double* const* outputs,
+                           uint32_t flags, uint32_t audit_stride, cb_surrogate_stats* stats, void* stream);
+/* Parameters (FP32 master copy, layout of cb_surrogate_info) and normalisation (host arrays of
+ * n_features floats each; any may be NULL). Setting parameters resets the Adam moments. */
+int cb_surrogate_get_params(const cb_surrogate* s, float* params);
+int cb_surrogate_set_params(cb_surrogate* s, const float* params);
+int cb_surrogate_normalisation(const cb_surrogate* s, float* in_mean, float* in_rstd, float* out_mean,
+                               float* out_std, float* in_lo, float* in_hi);
+/* One forward and backward pass on `rows` given rows (a multiple of 128, at most the batch): normalised
+ * features [rows][n_in] and targets [rows][n_out] (host, FP32; features are rounded to BF16). Returns
+ * the mean squared error, the gradient of every parameter (n_params floats) and, when `outputs` is not
+ * NULL, the network outputs [rows][n_out]. Host arrays, synchronous; no parameter is changed. */
+int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features, const float* targets,
+                          float* loss, float* grads, float* outputs);
 const char* cb_last_error(void);
 const char* cb_version(void);
 

@@ -1,0 +1,179 @@
+"""The learned transport surrogate through the C ABI: the device cell generator against the host one,
+the tcgen05 GEMM forward and backward against the FP64 network restatement (oracle/mlp.py), training,
+the trust gate and audit, and what the trained network gains over the plain transport kernel.
+
+Stated error bars: network outputs within 2e-3 and gradients within 1e-2 (norm-relative, per layer) of
+the restatement that rounds the same values to BF16; within 3e-2 / 6e-2 of the unrounded FP64 network.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import util
+from oracle import mlp
+
+pytestmark = pytest.mark.gpu
+
+
+def _mech(config):
+    import combustion_gb300 as cb
+    from combustion_gb300 import synthetic
+    m = util.mechanism(config)
+    mech = cb.Mechanism(m)
+    mech.transport_setup(*synthetic.transport_scales(m))
+    return mech
+
+
+def _nrel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_device_cells_match_host_generator():
+    from combustion_gb300 import surrogate as S
+    from combustion_gb300 import synthetic
+    m = util.mechanism("k53")
+    mech = _mech("k53")
+    n = 4096
+    dev = S.generate_cells(mech, n, S.distribution("k53", seed=1)).cpu().numpy()
+    host = synthetic.generate_cells(m.K, n, "k53", seed=1)
+    assert np.allclose(dev[2], host.temperature, rtol=1e-14, atol=0)
+    assert np.allclose(dev[0], host.pressure_R, rtol=1e-12, atol=0)
+    assert np.array_equal(dev[3], host.volume)
+    rel = np.abs(dev[4:] - host.amounts) / np.maximum(np.abs(host.amounts), 1e-300)
+    # CUDA's and glibc's log/cos/exp differ in the last bits; a rejection test can then rarely flip
+    assert np.mean(rel < 1e-9) > 0.999, np.mean(rel < 1e-9)
+
+
+@pytest.mark.parametrize("hidden,rows", [(2, 512), (4, 1024)])
+def test_forward_backward_against_restatement(hidden, rows):
+    from combustion_gb300 import surrogate as S
+    mech = _mech("k10")
+    s = S.Surrogate(mech, width=256, hidden_layers=hidden, batch=1024, seed=11)
+    info = s.info
+    rng = np.random.default_rng(hidden)
+    p = s.params()
+    # random weights with realistic scale everywhere a gradient flows (padding stays zero)
+    layers = s.layers(p)
+    nf = info.n_features
+    for l, (W, b) in enumerate(layers):
+        fan_in = nf if l == 0 else W.shape[1]
+        rows_l = nf if l == len(layers) - 1 else W.shape[0]
+        cols_l = nf if l == 0 else W.shape[1]
+        W[:rows_l, :cols_l] = rng.normal(0, 1.2 / np.sqrt(fan_in), (rows_l, cols_l))
+        b[:rows_l] = rng.normal(0, 0.1, rows_l)
+    s.set_params(p)
+    X = np.zeros((rows, info.n_in), np.float32)
+    X[:, :nf] = rng.normal(size=(rows, nf))
+    T = np.zeros((rows, info.n_out), np.float32)
+    T[:, :nf] = rng.normal(size=(rows, nf))
+    loss, g, Y = s.evaluate(X, T)
+    layers = s.layers(s.params().astype(np.float64))
+    lb, gb, Yb = mlp.loss_and_grads(layers, X, T, nf, bf=True)
+    l64, g64, Y64 = mlp.loss_and_grads(layers, X, T, nf, bf=False)
+    e_out = _nrel(Y[:, :nf], Yb[:, :nf])
+    print(f"hidden {hidden}: outputs {e_out:.2e} (vs FP64 {_nrel(Y[:, :nf], Y64[:, :nf]):.2e}); loss {loss:.6f} "
+          f"restatement {lb:.6f}")
+    assert e_out < 2e-3
+    assert _nrel(Y[:, :nf], Y64[:, :nf]) < 3e-2
+    assert abs(loss - lb) <= 2e-3 * lb
+    gl = s.layers(g.astype(np.float64))
+    for l in range(len(layers)):
+        for k, name in ((0, "W"), (1, "b")):
+            e_b, e_64 = _nrel(gl[l][k], gb[l][k]), _nrel(gl[l][k], g64[l][k])
+            print(f"  layer {l} d{name}: {e_b:.2e} (vs FP64 {e_64:.2e})")
+            assert e_b < 1e-2, (l, name, e_b)
+            assert e_64 < 6e-2, (l, name, e_64)
+
+
+def _plain_transport(mech, cells):
+    import torch
+    K, A, n = mech.K, mech.A, cells.shape[1]
+    rates = torch.empty((A + 2, n), dtype=torch.float64, device="cuda")
+    tr = torch.empty((K + 2, n), dtype=torch.float64, device="cuda")
+    mech.rates_transport(cells, rates, tr)
+    torch.cuda.synchronize()
+    return tr
+
+
+def _trained(config, n_train, steps, batch, width=256, seed=3):
+    from combustion_gb300 import surrogate as S
+    mech = _mech(config)
+    s = S.Surrogate(mech, width=width, hidden_layers=4, batch=batch, lr=2e-3, lr_final=1e-4, seed=seed)
+    s.generate(n_train, S.distribution(config, seed=2))
+    untrained = s.params()
+    losses = s.train(steps)
+    return mech, s, untrained, losses
+
+
+def test_training_gate_and_audit():
+    import torch
+    from combustion_gb300 import surrogate as S
+    mech, s, untrained, losses = _trained("k10", 1 << 17, 400, 8192)
+    print("loss", losses[0], "->", losses[-1])
+    assert np.all(np.isfinite(losses)) and losses[-1] < losses[0] / 20
+    n = 1 << 16
+    cells = S.generate_cells(mech, n, S.distribution("k10", seed=7))
+    plain = _plain_transport(mech, cells)
+    out = torch.empty_like(plain)
+    st = s.transport(cells, out, gate=False)
+    assert st["fallback_cells"] == 0
+    err = (out - plain).abs() / plain.abs()
+    trained_rms = float(err.pow(2).mean().sqrt())
+    s2 = S.Surrogate(mech, width=256, hidden_layers=4, batch=8192, seed=3)
+    s2.generate(1 << 14, S.distribution("k10", seed=2))
+    s2.set_params(untrained)
+    out2 = torch.empty_like(plain)
+    s2.transport(cells, out2, gate=False)
+    untrained_rms = float(((out2 - plain).abs() / plain.abs()).pow(2).mean().sqrt())
+    print(f"rms rel error: trained {trained_rms:.2e}, untrained {untrained_rms:.2e}; max {float(err.max()):.2e}")
+    assert trained_rms < untrained_rms / 10
+    # gate: cells outside the training temperatures go to the plain kernel, bit for bit
+    cells[2, : n // 4] = 3500.0
+    plain = _plain_transport(mech, cells)
+    out = torch.empty_like(plain)
+    st = s.transport(cells, out, audit_stride=64)
+    print(st)
+    assert st["fallback_cells"] >= n // 4
+    assert torch.equal(out[:, : n // 4], plain[:, : n // 4])
+    assert st["audited_cells"] > 0
+    assert st["audit_max_rel_err"][2] <= float(err.max()) * 4 + 1e-3
+    # every cell is either the network's or the plain kernel's value
+    same = (out == plain).all(dim=0)
+    assert int(same.sum()) >= st["fallback_cells"] + st["audited_cells"]
+
+
+def test_trained_network_gain_over_plain_kernel():
+    """What the trained network gains: transport cells/s through the gated surrogate against the plain
+    FP64 kernel on the same cells (53 species), at the error the audit reports."""
+    import torch
+    from combustion_gb300 import surrogate as S
+    mech, s, _, losses = _trained("k53", 1 << 18, 300, 16384)
+    n = 1 << 20
+    cells = S.generate_cells(mech, n, S.distribution("k53", seed=9))
+    out = torch.empty((mech.K + 2, n), dtype=torch.float64, device="cuda")
+    K = mech.K
+    tin = torch.empty((K + 1, n), dtype=torch.float64, device="cuda")
+    T0 = mech.info.T0
+    tin[0] = cells[0] * cells[3] / cells[2]
+    tin[1] = cells[2] / T0
+    tin[2:] = cells[4:]
+    plain = torch.empty_like(out)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    t_plain = timed(lambda: mech.transport(tin, plain))
+    stats = {}
+    t_sur = timed(lambda: stats.update(s.transport(cells, out, audit_stride=1024)))
+    err = ((out - plain).abs() / plain.abs())
+    print(f"plain {n / t_plain:.3e} cells/s, surrogate {n / t_sur:.3e} cells/s ({t_plain / t_sur:.1f}x); "
+          f"rms rel err {float(err.pow(2).mean().sqrt()):.2e}, audit {stats}")
+    assert t_sur < t_plain
+    assert stats["audited_cells"] > 0
