@@ -140,6 +140,92 @@ def run_reference(args):
     }), flush=True)
 
 
+def measured_bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        v = json.load(open(path)).get("bf16_tflops")
+        if v:
+            return float(v), "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst), of measured"
+    return 1900.0, "fallback 1.9 PFLOP/s bf16, of fallback"
+
+
+def rel_err_groups(x, ref):
+    """Max and RMS relative error of transport outputs per group (conductivity, viscosity, diffusion)."""
+    import torch
+    e = (x - ref).abs() / ref.abs()
+    out = {}
+    for name, rows in (("conductivity", e[0:1]), ("viscosity", e[1:2]), ("diffusion", e[2:])):
+        out[name] = {"max": float(rows.max()), "rms": float(torch.sqrt((rows * rows).mean()))}
+    return out
+
+
+def run_surrogate(args, mech, d_in, r_out, t_out, n, world, stream):
+    """The mixed + surrogate form: the transport MLP is trained here (device generator, plain-kernel
+    targets, tcgen05 training step as a CUDA graph), then mixed rates + gated surrogate transport are
+    timed on the benchmark cells and compared with the plain FP64 transport outputs of this run."""
+    import torch
+    from combustion_gb300 import surrogate as S
+    K = mech.K
+    sur = S.Surrogate(mech, width=256, hidden_layers=4, batch=args.sur_batch, lr=1e-3, lr_final=1e-5, seed=3)
+    t = time.perf_counter()
+    sur.generate(args.sur_train_cells, S.distribution(CONFIG, seed=2))
+    gen_s = time.perf_counter() - t
+    t = time.perf_counter()
+    losses = sur.train(args.sur_steps)
+    train_s = time.perf_counter() - t
+    info = sur.info
+    dims = [info.n_features] + [info.width] * info.hidden_layers + [info.n_features]
+    flops_cell = 2.0 * sum(a * b for a, b in zip(dims[:-1], dims[1:]))
+    s_out = torch.empty_like(t_out)
+    net = sur.transport(d_in, s_out, gate=False)
+    torch.cuda.synchronize()
+    net_err = rel_err_groups(s_out, t_out)
+    gated = sur.transport(d_in, s_out, audit_stride=args.sur_audit, timing=True)
+    torch.cuda.synchronize()
+    gated_err = rel_err_groups(s_out, t_out)
+    m_r = torch.empty_like(r_out)
+
+    def step():
+        mech.rates(d_in, m_r, mixed=True)
+        return sur.transport(d_in, s_out, audit_stride=args.sur_audit)
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        st = step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    peak, peak_src = measured_bf16_peak()
+    net_ms = gated["ms"]["network"]
+    achieved = flops_cell * n / (net_ms * 1e-3) / 1e12
+    train_flops = 3.0 * flops_cell * info.batch
+    return {
+        "cells_per_s": world * n / (ms * 1e-3), "ms_per_step": ms,
+        "api": "cb_rates_mixed + cb_surrogate_transport (gate + audit every %d cells)" % args.sur_audit,
+        "network": {"inputs": info.n_features, "hidden": [info.width] * info.hidden_layers, "outputs": info.n_features,
+                    "activation": "SiLU", "dtype": "bf16 weights/activations, fp32 accumulate (tcgen05)",
+                    "flops_per_cell": flops_cell},
+        "training": {"cells": int(info.n_train), "batch": info.batch, "steps": args.sur_steps,
+                     "optimizer": "Adam lr 1e-3, cosine decay to 1e-5", "loss_first": float(losses[0]),
+                     "loss_last": float(np.mean(losses[-20:])), "generate_s": gen_s, "train_s": train_s,
+                     "ms_per_step": 1e3 * train_s / args.sur_steps,
+                     "tflops": train_flops * args.sur_steps / train_s / 1e12},
+        "error_network_vs_plain_f64": net_err,
+        "error_gated_vs_plain_f64": gated_err,
+        "gate": {"fallback_cells": gated["fallback_cells"], "audited_cells": gated["audited_cells"],
+                 "fallback_rate": gated["fallback_cells"] / n, "audit_max_rel_err": gated["audit_max_rel_err"],
+                 "audit_rms_rel_err": gated["audit_rms_rel_err"]},
+        "phase_ms": gated["ms"],
+        "roofline": {"bound": "tensor", "kernel": "gemm_kernel (5 layers, inference)", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_src,
+                     "flops_per_cell": flops_cell},
+    }
+
+
 def run_ours(args):
     world, rank, local = dist_setup("nccl")
     from combustion_gb300 import synthetic
@@ -236,6 +322,10 @@ def run_ours(args):
         per_cell = json.load(open(tpath)).get(dom, {}).get("dram_bytes_per_cell")
         traffic = per_cell * n if per_cell else None
 
+    surrogate_form = None
+    if not args.no_surrogate:
+        surrogate_form = run_surrogate(args, mech, d_in, r_out, t_out, n, world, stream)
+
     # Parity of this run's outputs on a sample of cells against the FP64 oracle.
     parity = None
     mixed_err = None
@@ -320,6 +410,7 @@ def run_ours(args):
                               "max_err": None if parity is None else max(parity["rates_max_err"], parity["transport_max_err"])},
                 "mixed": {"cells_per_s": world * n / (mixed_ms * 1e-3), "ms_per_step": mixed_ms, "error": mixed_err,
                           "api": "cb_rates_mixed + cb_transport_mixed"},
+                "mixed_surrogate": surrogate_form,
             },
         }
         print(json.dumps(line), flush=True)
@@ -337,6 +428,11 @@ def main():
     ap.add_argument("--ref-cells", type=int, default=1 << 18)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
+    ap.add_argument("--sur-steps", type=int, default=2000)
+    ap.add_argument("--sur-batch", type=int, default=65536)
+    ap.add_argument("--sur-audit", type=int, default=1024)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -135,7 +135,7 @@ struct cb_surrogate {
     CUtensorMap mXi, mHi[2];
     uint32_t *fail_idx = nullptr, *audit_idx = nullptr, *gate_count = nullptr;
     double* audit_plain = nullptr;
-    size_t audit_cap = 0;
+    size_t fail_cap = 0, audit_cap = 0;  // grown to the largest call
     unsigned* err_max = nullptr;
     double* err_sq = nullptr;
     int* status = nullptr;
@@ -317,11 +317,7 @@ int ensure_inference(cb_surrogate* s, size_t rows) {
     SUR_RC(dalloc(&s->Hi[0], rows * s->width));
     SUR_RC(dalloc(&s->Hi[1], rows * s->width));
     SUR_RC(dalloc(&s->Yi, rows * s->n_out));
-    SUR_RC(dalloc(&s->fail_idx, rows));
-    s->audit_cap = rows / 16 + 1024;
-    SUR_RC(dalloc(&s->audit_idx, s->audit_cap));
     SUR_RC(dalloc(&s->gate_count, 2));
-    SUR_RC(dalloc(&s->audit_plain, s->audit_cap * (size_t)(s->K + 2)));
     SUR_RC(dalloc(&s->err_max, 3));
     SUR_RC(dalloc(&s->err_sq, 3));
     SUR_RC(make_map(&s->mXi, s->Xi, s->n_in, rows, kBM));
@@ -824,8 +820,10 @@ int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features_h
 int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* inputs, double* const* outputs,
                            uint32_t flags, uint32_t audit_stride, cb_surrogate_stats* stats, void* stream) {
     if (!s || !inputs || !outputs) return cbi::fail(CB_ERR_INVALID, "null argument");
-    if (flags & ~(CB_UNIFORM_PRESSURE | CB_SURROGATE_NO_GATE)) return cbi::fail(CB_ERR_INVALID, "unknown flag");
+    if (flags & ~(CB_UNIFORM_PRESSURE | CB_SURROGATE_NO_GATE | CB_SURROGATE_TIMING))
+        return cbi::fail(CB_ERR_INVALID, "unknown flag");
     if (!s->have_norm) return cbi::fail(CB_ERR_NOT_READY, "cb_surrogate_generate has not run");
+    if (n >= ((size_t)1 << 31)) return cbi::fail(CB_ERR_INVALID, "at most 2^31 - 1 cells per call");
     const int K = s->K, nf = s->n_feat;
     for (int q = 0; q < K + 3; q++)
         if (!inputs[q]) return cbi::fail(CB_ERR_INVALID, "null input array");
@@ -839,12 +837,52 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
     const bool gate = !(flags & CB_SURROGATE_NO_GATE);
     const bool uniform = flags & CB_UNIFORM_PRESSURE;
     const double T0 = cbi::view(s->mech).T0;
+    // gate lists over the whole call: every cell may fall back; one audited cell per audit_stride
+    const size_t audit_cap = gate && audit_stride ? n / audit_stride + 1 : 0;
+    if (gate && n > s->fail_cap) {
+        cudaFree(s->fail_idx);
+        s->fail_idx = nullptr;
+        s->fail_cap = 0;
+        SUR_RC(dalloc(&s->fail_idx, n));
+        s->fail_cap = n;
+    }
+    if (audit_cap > s->audit_cap) {
+        cudaFree(s->audit_idx);
+        cudaFree(s->audit_plain);
+        s->audit_idx = nullptr;
+        s->audit_plain = nullptr;
+        s->audit_cap = 0;
+        SUR_RC(dalloc(&s->audit_idx, audit_cap));
+        SUR_RC(dalloc(&s->audit_plain, audit_cap * (size_t)(K + 2)));
+        s->audit_cap = audit_cap;
+    }
+    // optional phase timing: features, network, outputs (summed over chunks), then the gate's plain work
+    const bool timing = flags & CB_SURROGATE_TIMING;
+    cudaEvent_t ev[5] = {};
+    double ms[4] = {0, 0, 0, 0};
+    struct EventGuard {
+        cudaEvent_t* ev;
+        ~EventGuard() {
+            for (int i = 0; i < 5; i++)
+                if (ev[i]) cudaEventDestroy(ev[i]);
+        }
+    } guard{ev};
+    if (timing)
+        for (auto& e : ev) SUR_CUDA(cudaEventCreate(&e));
+    auto mark = [&](int i) { return timing ? cudaEventRecord(ev[i], st) : cudaSuccess; };
+    auto elapsed = [&](int i, int j) -> cudaError_t {
+        if (!timing) return cudaSuccess;
+        cudaError_t e = cudaEventSynchronize(ev[j]);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[i], ev[j]);
+        ms[i] += t;
+        return e;
+    };
     SUR_CUDA(cudaMemsetAsync(s->err_max, 0, 3 * sizeof(unsigned), st));
     SUR_CUDA(cudaMemsetAsync(s->err_sq, 0, 3 * sizeof(double), st));
-    uint64_t n_fail = 0, n_audit = 0;
+    if (gate) SUR_CUDA(cudaMemsetAsync(s->gate_count, 0, 2 * sizeof(uint32_t), st));
     std::vector<const double*> in(K + 3);
-    std::vector<double*> out(K + 2), aud(K + 2);
-    for (int q = 0; q < K + 2; q++) aud[q] = s->audit_plain + (size_t)q * s->audit_cap;
+    std::vector<double*> out(K + 2);
     for (size_t lo = 0; lo < n; lo += kInferChunk) {
         const size_t len = std::min(kInferChunk, n - lo);
         const int rows = (int)((len + kBM - 1) / kBM * kBM);
@@ -865,7 +903,6 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
         f.rstd = nrm(s, kInRstd);
         f.X = s->Xi;
         if (gate) {
-            SUR_CUDA(cudaMemsetAsync(s->gate_count, 0, 2 * sizeof(uint32_t), st));
             f.lo = nrm(s, kLo);
             f.hi = nrm(s, kHi);
             f.fail_idx = s->fail_idx;
@@ -873,11 +910,15 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
             f.audit_idx = s->audit_idx;
             f.audit_count = s->gate_count + 1;
             f.audit_stride = audit_stride;
-            f.audit_phase = audit_stride ? (uint32_t)((lo / kInferChunk * 7919u) % audit_stride) : 0u;
-            f.audit_cap = (uint32_t)s->audit_cap;
+            f.audit_phase = audit_stride ? (uint32_t)(7919u % audit_stride) : 0u;
+            f.audit_cap = (uint32_t)audit_cap;
+            f.idx_base = (uint32_t)lo;
         }
+        SUR_CUDA(mark(0));
         SUR_CUDA(features(f, st));
+        SUR_CUDA(mark(1));
         SUR_RC(infer_rows(s, rows, s->mXi, st));
+        SUR_CUDA(mark(2));
         OutputArgs o;
         std::memset(&o, 0, sizeof o);
         o.Y = s->Yi;
@@ -888,30 +929,42 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
         o.std = nrm(s, kOutStd);
         for (int q = 0; q < K + 2; q++) o.out[q] = out[q];
         SUR_CUDA(cbg::sur::outputs(o, st));
-        if (gate) {
-            SUR_RC(cbi::transport_gather(s->mech, len, in.data(), out.data(), s->fail_idx, s->gate_count, false,
-                                         uniform ? CB_UNIFORM_PRESSURE : 0, st));
-            if (audit_stride) {
-                SUR_RC(cbi::transport_gather(s->mech, s->audit_cap, in.data(), aud.data(), s->audit_idx,
-                                             s->gate_count + 1, true, uniform ? CB_UNIFORM_PRESSURE : 0, st));
-                AuditArgs a;
-                std::memset(&a, 0, sizeof a);
-                a.idx = s->audit_idx;
-                a.count = s->gate_count + 1;
-                a.plain = s->audit_plain;
-                a.cap = s->audit_cap;
-                for (int q = 0; q < K + 2; q++) a.out[q] = out[q];
-                a.n_feat = nf;
-                a.max_err = s->err_max;
-                a.sum_sq = s->err_sq;
-                SUR_CUDA(audit(a, s->audit_cap, st));
-            }
-            uint32_t cnt[2];
-            SUR_CUDA(cudaMemcpyAsync(cnt, s->gate_count, sizeof cnt, cudaMemcpyDeviceToHost, st));
-            SUR_CUDA(cudaStreamSynchronize(st));
-            n_fail += cnt[0];
-            n_audit += std::min<uint64_t>(cnt[1], s->audit_cap);
+        SUR_CUDA(mark(3));
+        SUR_CUDA(elapsed(0, 1));
+        SUR_CUDA(elapsed(1, 2));
+        SUR_CUDA(elapsed(2, 3));
+    }
+    uint64_t n_fail = 0, n_audit = 0;
+    if (gate) {
+        uint32_t cnt[2];
+        SUR_CUDA(cudaMemcpyAsync(cnt, s->gate_count, sizeof cnt, cudaMemcpyDeviceToHost, st));
+        SUR_CUDA(cudaStreamSynchronize(st));
+        n_fail = cnt[0];
+        n_audit = std::min<uint64_t>(cnt[1], audit_cap);
+        SUR_CUDA(mark(3));
+        const uint32_t pflags = uniform ? CB_UNIFORM_PRESSURE : 0;
+        if (n_fail)  // the plain kernel writes the rejected cells' outputs in place
+            SUR_RC(cbi::transport_gather(s->mech, n_fail, inputs, outputs, s->fail_idx, s->gate_count, false,
+                                         pflags, st));
+        if (n_audit) {
+            std::vector<double*> aud(K + 2);
+            for (int q = 0; q < K + 2; q++) aud[q] = s->audit_plain + (size_t)q * audit_cap;
+            SUR_RC(cbi::transport_gather(s->mech, n_audit, inputs, aud.data(), s->audit_idx, s->gate_count + 1,
+                                         true, pflags, st));
+            AuditArgs a;
+            std::memset(&a, 0, sizeof a);
+            a.idx = s->audit_idx;
+            a.count = s->gate_count + 1;
+            a.plain = s->audit_plain;
+            a.cap = audit_cap;
+            for (int q = 0; q < K + 2; q++) a.out[q] = outputs[q];
+            a.n_feat = nf;
+            a.max_err = s->err_max;
+            a.sum_sq = s->err_sq;
+            SUR_CUDA(audit(a, n_audit, st));
         }
+        SUR_CUDA(mark(4));
+        SUR_CUDA(elapsed(3, 4));
     }
     unsigned em[3];
     double es[3];
@@ -929,6 +982,10 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
             stats->audit_max_rel_err[gI] = v;
             stats->audit_rms_rel_err[gI] = n_audit ? std::sqrt(es[gI] / counts[gI]) : 0.0;
         }
+        stats->ms_features = ms[0];
+        stats->ms_network = ms[1];
+        stats->ms_outputs = ms[2];
+        stats->ms_gate = ms[3];
     }
     return check_device_status(s);
 }

@@ -506,11 +506,12 @@ __global__ void features_kernel(const FeatureArgs a) {
                 for (int h = 0; h < 8; h++) a.XT[(size_t)(j0 + h) * a.ldXT + a.row0 + c] = __float2bfloat16_rn(x[h]);
         }
         if (a.fail_idx) {
+            const uint32_t cell = a.idx_base + (uint32_t)c;
             if (!inside) {
-                a.fail_idx[atomicAdd(a.fail_count, 1u)] = (uint32_t)c;
-            } else if (a.audit_stride && c % a.audit_stride == a.audit_phase) {
+                a.fail_idx[atomicAdd(a.fail_count, 1u)] = cell;
+            } else if (a.audit_stride && cell % a.audit_stride == a.audit_phase) {
                 const uint32_t slot = atomicAdd(a.audit_count, 1u);
-                if (slot < a.audit_cap) a.audit_idx[slot] = (uint32_t)c;
+                if (slot < a.audit_cap) a.audit_idx[slot] = cell;
             }
         }
     }

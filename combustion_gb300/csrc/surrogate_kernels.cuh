@@ -67,8 +67,9 @@ struct FeatureArgs {
     float* raw;                             // raw features [n][n_feat] (optional, statistics)
     int* hull_lo; int* hull_hi;             // order-preserving integer min / max of raw features (optional)
     const float* lo; const float* hi;       // trust region (inference gate, optional)
-    uint32_t* fail_idx; uint32_t* fail_count;
+    uint32_t* fail_idx; uint32_t* fail_count;  // cells idx_base + c outside the trust region
     uint32_t* audit_idx; uint32_t* audit_count; uint32_t audit_stride, audit_phase, audit_cap;
+    uint32_t idx_base;
 };
 
 struct TargetArgs {

@@ -13,6 +13,7 @@ from . import CombustionError, Mechanism, _check, _ptr_array, lib
 
 CB_UNIFORM_PRESSURE = 2
 CB_SURROGATE_NO_GATE = 8
+CB_SURROGATE_TIMING = 16
 
 
 class cb_cell_distribution(C.Structure):
@@ -35,11 +36,15 @@ class cb_surrogate_info(C.Structure):
 
 class cb_surrogate_stats(C.Structure):
     _fields_ = [("cells", C.c_uint64), ("fallback_cells", C.c_uint64), ("audited_cells", C.c_uint64),
-                ("audit_max_rel_err", C.c_double * 3), ("audit_rms_rel_err", C.c_double * 3)]
+                ("audit_max_rel_err", C.c_double * 3), ("audit_rms_rel_err", C.c_double * 3),
+                ("ms_features", C.c_double), ("ms_network", C.c_double), ("ms_outputs", C.c_double),
+                ("ms_gate", C.c_double)]
 
     def as_dict(self):
         return {"cells": self.cells, "fallback_cells": self.fallback_cells, "audited_cells": self.audited_cells,
-                "audit_max_rel_err": list(self.audit_max_rel_err), "audit_rms_rel_err": list(self.audit_rms_rel_err)}
+                "audit_max_rel_err": list(self.audit_max_rel_err), "audit_rms_rel_err": list(self.audit_rms_rel_err),
+                "ms": {"features": self.ms_features, "network": self.ms_network, "outputs": self.ms_outputs,
+                       "gate": self.ms_gate}}
 
 
 # Cell distributions of the named workloads (T in K, P in atm, Dirichlet alpha).
@@ -168,11 +173,13 @@ class Surrogate:
                                            y.ctypes.data if outputs else None))
         return loss.value, g, y
 
-    def transport(self, inputs, outputs, audit_stride=1024, gate=True, uniform_pressure=False, stream=None):
+    def transport(self, inputs, outputs, audit_stride=1024, gate=True, uniform_pressure=False, stream=None,
+                  timing=False):
         """Rates-layout inputs [K+3, n] -> transport outputs [K+2, n] (torch CUDA float64). Returns stats."""
         ins, _ = Mechanism._rows(inputs)
         outs, n = Mechanism._rows(outputs)
         flags = (0 if gate else CB_SURROGATE_NO_GATE) | (CB_UNIFORM_PRESSURE if uniform_pressure else 0)
+        flags |= CB_SURROGATE_TIMING if timing else 0
         st = cb_surrogate_stats()
         _check(lib().cb_surrogate_transport(self.h, n, _ptr_array(ins), _ptr_array(outs), flags, audit_stride,
                                             C.byref(st), Mechanism._stream(stream)))

@@ -207,8 +207,11 @@ typedef struct cb_surrogate_stats {
     uint64_t cells, fallback_cells, audited_cells;
     double audit_max_rel_err[3];  /* conductivity, viscosity, diffusion coefficients */
     double audit_rms_rel_err[3];
+    /* with CB_SURROGATE_TIMING: device milliseconds of the phases (CUDA events on the call's stream) */
+    double ms_features, ms_network, ms_outputs, ms_gate;
 } cb_surrogate_stats;
 #define CB_SURROGATE_NO_GATE 8u  /* network outputs for every cell: no trust gate, no audit */
+#define CB_SURROGATE_TIMING 16u  /* time the phases of the call */
 
 int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* desc, cb_surrogate** out);
 int cb_surrogate_destroy(cb_surrogate* s);
