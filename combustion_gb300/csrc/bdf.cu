@@ -1,0 +1,1232 @@
+// Batched constant-pressure reactors: a variable-order (1-5), variable-step BDF integrator in
+// backward-difference form with Newton iterations on an analytic Jacobian, one warp per reactor.
+//
+// Role in the reference: the reactor loop of plot.rs:32-118 (state u = [T, V, n_active], du/dt = the
+// rates function's outputs, reaction.rs:356-391) and the cvode crate's BDF (cvode/lib.rs:17-47: CV_BDF,
+// dense linear solver, difference-quotient Jacobian). Here many reactors advance together: each warp
+// owns one reactor at a time, taken from a work queue, and keeps its iteration matrix (LU with partial
+// pivoting), difference array and rates scratch in shared memory; the rates program runs
+// warp-cooperatively (lanes split species, third-body rows and reactions; per-species sums in the
+// reactions' order). Launches are slices of at most `slice_steps` steps per reactor so that reactors of
+// uneven stiffness rebalance between launches; a CUDA graph replays the slice sequence.
+//
+// Method (the published variable-step BDF of Shampine & Reichelt, "The MATLAB ODE suite", SIAM J. Sci.
+// Comput. 18(1), 1997, with kappa = 0): predictor y_pred = sum_{j<=q} D_j, corrector
+// d - c f(t_new, y_pred + d) + psi = 0 with c = h / gamma_q and psi = sum_{j=1..q} gamma_j D_j / gamma_q,
+// solved by at most 4 Newton iterations on (I - c J); local error (1/(q+1)) d against atol + rtol |y|;
+// step and order from the error norms of orders q-1, q, q+1 after q+1 steps of equal size; the
+// difference array is rescaled by the R U matrices when h changes. J is recomputed only when Newton
+// fails with a Jacobian from an earlier step; (I - c J) is refactorised after a step or order change
+// and after a Newton failure, but kept after a rejected error test (Newton converged with it).
+// Jacobian: species and volume columns analytic (mass action, third-body and falloff efficiencies with
+// the Troe broadening held fixed), T and V rows by the chain rule through the energy equation, the
+// temperature column by one forward difference.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/combustion_gb300.h"
+#include "capi_internal.h"
+#include "device_common.cuh"
+#include "device_math.cuh"
+#include "rates_core.cuh"
+#include "tables.h"
+
+namespace cbg {
+namespace bdf {
+
+constexpr int kMaxOrder = 5;
+constexpr int kDRows = kMaxOrder + 3;
+constexpr int kNewtonMaxIter = 4;
+constexpr double kMinFactor = 0.2, kMaxFactor = 10.0;
+constexpr int kMaxN = 66;  // state size limit: the iteration matrix stays in shared memory
+
+enum State : int { kNew = 0, kRunning = 1, kDone = 2, kFailStep = 3, kFailSteps = 4, kFailLU = 5 };
+
+struct Head {
+    double t, h;
+    double ign_t, ign_g, ta, ga, tc, gc, tp, gp;  // max dT/dt, its neighbours, the previous sample
+    int q, n_equal, state, jac_current;
+    int steps, rhs, jacs, lus, newton_fail, err_fail, need_next, pad;
+};
+
+struct Params {
+    const uint8_t* tab;
+    uint32_t tab_bytes;
+    int smem_tables;
+    int off_csr_start, off_csr;  // per-species reaction lists inside the blob
+    int K, A, R, N, LD, n_eff;
+    uint32_t ws_bytes;           // per-warp workspace
+    int n;
+    double rtol, atol, t_end, h_min;
+    int max_steps, slice_steps;
+    const double* pR;  // P/R per reactor
+    Head* head;
+    double* D;  // [n][kDRows][N]
+    double* J;  // [n][N][N]
+    int* queue;
+    int* done;
+    int* status;
+    // evaluation hook: states [m][N] -> f [m][N], J [m][N][N]
+    const double* eval_y;
+    double* eval_f;
+    double* eval_J;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// Concentrations, Gibbs exponentials and third-body sums in shared memory, viewed as a rates "cell".
+struct WarpCell {
+    Temps t;
+    double C0, rcpC0, rcpC0sq;
+    const double* C;
+    const double* ex;
+    const double* exn;
+    const double* M;
+};
+
+struct Work {
+    double *LU, *D, *ypred, *psi, *scale, *y, *d, *f, *b, *tmp, *C, *ex, *exn, *M, *hk, *cpk, *cR, *kf, *pK, *sM, *rdiag;
+    int* piv;
+};
+
+__host__ __device__ inline size_t workspace_doubles(int K, int A, int R, int N, int LD, int n_eff) {
+    return (size_t)N * LD + (size_t)kDRows * N + 8 * (size_t)N + K + 2 * (size_t)A + n_eff + A + K + 4 * (size_t)R + N;
+}
+
+__device__ Work carve(const Params& p, uint8_t* base) {
+    Work w;
+    double* q = reinterpret_cast<double*>(base);
+    auto take = [&](size_t n) {
+        double* r = q;
+        q += n;
+        return r;
+    };
+    const int N = p.N;
+    w.LU = take((size_t)N * p.LD);
+    w.D = take((size_t)kDRows * N);
+    w.ypred = take(N);
+    w.psi = take(N);
+    w.scale = take(N);
+    w.y = take(N);
+    w.d = take(N);
+    w.f = take(N);
+    w.b = take(N);
+    w.tmp = take(N);
+    w.C = take(p.K);
+    w.ex = take(p.A);
+    w.exn = take(p.A);
+    w.M = take(p.n_eff);
+    w.hk = take(p.A);
+    w.cpk = take(p.K);
+    w.cR = take(p.R);
+    w.kf = take(p.R);
+    w.pK = take(p.R);
+    w.sM = take(p.R);
+    w.rdiag = take(N);
+    w.piv = reinterpret_cast<int*>(q);
+    return w;
+}
+
+struct Mech {
+    RatesTables tb;
+    const int* csr_start;
+    const int* csr;
+    __device__ Mech(const uint8_t* tab, const Params& p)
+        : tb(tab), csr_start(reinterpret_cast<const int*>(tab + p.off_csr_start)),
+          csr(reinterpret_cast<const int*>(tab + p.off_csr)) {}
+};
+
+struct RhsOut {
+    double T, V, md, Ctot, S, E, Cp, dtE;
+};
+
+// du/dt of the reactor: the outputs of reaction.rs:356-391 at state y = [T, V, n_0 .. n_{A-1}].
+template <bool PARTS>
+__device__ RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
+                           double* f, int lane) {
+    const RatesHeader& H = *m.tb.H;
+    const int K = p.K, A = p.A, R = p.R;
+    RhsOut o;
+    const double T = y[0], V = y[1];
+    WarpCell c;
+    c.t.T = T;
+    c.t.rcpT = rcp64(T);
+    c.t.lnT = log64(T);
+    c.t.T2 = T * T;
+    c.t.T3 = T * c.t.T2;
+    c.t.T4 = c.t.T2 * c.t.T2;
+    c.t.rcpT2 = c.t.rcpT * c.t.rcpT;
+    const double md = rcp64(V);
+    double s = 0.0;
+    for (int k = lane; k < K - 1; k += 32) {
+        const double ck = md * max0(y[2 + k]);
+        w.C[k] = ck;
+        s += ck;
+    }
+    s = warp_sum(s);
+    const double Ctot = pR * c.t.rcpT;
+    if (lane == 0) w.C[K - 1] = Ctot - s;
+    c.C0 = H.C0 * c.t.rcpT;
+    c.rcpC0 = H.rcp_C0 * T;
+    c.rcpC0sq = c.rcpC0 * c.rcpC0;
+    for (int k = lane; k < K; k += 32) {
+        const Species& sp = m.tb.species[k];
+        const int pc = piece_of(sp.split, T);
+        const double* cp = sp.cp[pc];
+        w.cpk[k] = fma(cp[4], c.t.T4, fma(cp[3], c.t.T3, fma(cp[2], c.t.T2, fma(cp[1], T, cp[0]))));
+        if (k < A) {
+            const double* h = sp.h[pc];
+            w.hk[k] = fma(h[5], c.t.rcpT, fma(h[4], c.t.T4, fma(h[3], c.t.T3, fma(h[2], c.t.T2, fma(h[1], T, h[0])))));
+            if (sp.need_exp | sp.need_exp_neg) {
+                const double* g = sp.g[pc];
+                const double x = fma(g[6], c.t.rcpT, fma(g[5], c.t.T4, fma(g[4], c.t.T3, fma(g[3], c.t.T2,
+                                 fma(g[2], T, fma(g[1], c.t.lnT, g[0]))))));
+                if (sp.need_exp) w.ex[k] = min_pos(H.M3, exp64(x));
+                if (sp.need_exp_neg) w.exn[k] = min_pos(H.cbrt_max, exp64(-x));
+            }
+        }
+    }
+    __syncwarp();
+    for (int e = lane; e < H.n_eff; e += 32) {
+        const double* E = m.tb.eff + (size_t)e * K;
+        double sum = 0.0;
+        for (int k = 0; k < K; k++) sum = fma(E[k], w.C[k], sum);
+        w.M[e] = Ctot + sum;
+    }
+    __syncwarp();
+    c.C = w.C;
+    c.ex = w.ex;
+    c.exn = w.exn;
+    c.M = w.M;
+    for (int r = lane; r < R; r += 32) {
+        const Reaction& x = m.tb.reactions[r];
+        ReactionParts pp;
+        double cR;
+        switch (x.model) {
+        case 0: cR = reaction_eval<0, PARTS>(m.tb, x, c, &pp); break;
+        case 1: cR = reaction_eval<1, PARTS>(m.tb, x, c, &pp); break;
+        case 2: cR = reaction_eval<2, PARTS>(m.tb, x, c, &pp); break;
+        case 3: cR = reaction_eval<3, PARTS>(m.tb, x, c, &pp); break;
+        default: cR = reaction_eval<4, PARTS>(m.tb, x, c, &pp); break;
+        }
+        w.cR[r] = cR;
+        if (PARTS) {
+            w.kf[r] = pp.kf;
+            w.pK[r] = pp.pK;
+            w.sM[r] = pp.dkf_dM * pp.Rnet;
+        }
+    }
+    __syncwarp();
+    double E = 0.0, dtE = 0.0, Cp = 0.0;
+    for (int k = lane; k < A; k += 32) {
+        double wk = 0.0;
+        for (int q = m.csr_start[k]; q < m.csr_start[k + 1]; q++) {
+            const int e = m.csr[q];
+            wk = fma(small_int_to_double((int)(int8_t)(e & 0xff)), w.cR[e >> 8], wk);
+        }
+        f[2 + k] = wk;
+        E = fma(wk, w.hk[k], E);
+        dtE = fma(m.tb.species[k].dtE, wk, dtE);
+    }
+    for (int k = lane; k < K; k += 32) Cp = fma(w.cpk[k], w.C[k], Cp);
+    E = warp_sum(E);
+    dtE = warp_sum(dtE);
+    Cp = warp_sum(Cp);
+    const double dtT_T = div64(-E, Cp);
+    if (lane == 0) {
+        f[0] = T * dtT_T;
+        f[1] = V * fma(rP * T, dtE, dtT_T);
+    }
+    __syncwarp();
+    o.T = T;
+    o.V = V;
+    o.md = md;
+    o.Ctot = Ctot;
+    o.S = s;
+    o.E = E;
+    o.Cp = Cp;
+    o.dtE = dtE;
+    return o;
+}
+
+// d/dC_{ks[i]} of prod_q C_{ks[q]}^{ns[q]}: one factor of species ks[i] removed, times its multiplicity.
+__device__ __forceinline__ double deriv_product(const double* C, const uint16_t* ks, const int8_t* ns, int n, int i) {
+    double p = small_int_to_double(ns[i]);
+    for (int q = 0; q < n; q++) {
+        const int mq = q == i ? ns[q] - 1 : ns[q];
+        for (int t = 0; t < mq; t++) p *= C[ks[q]];
+    }
+    return p;
+}
+
+// Jacobian of du/dt at y into w.LU (rows of LD), also stored to Jg [N][N]; w.f receives f(y).
+__device__ void jacobian_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
+                              double* Jg, int lane) {
+    const int K = p.K, A = p.A, N = p.N, LD = p.LD;
+    const RhsOut o = rhs_warp<true>(p, m, w, pR, rP, y, w.f, lane);
+    double* Jm = w.LU;
+    // species rows: G[k][j] = d wdot_k / d C_j (bulk column kept in column 0 for now)
+    for (int k = lane; k < A; k += 32) {
+        double* row = Jm + (size_t)(2 + k) * LD;
+        for (int j = 0; j < N; j++) row[j] = 0.0;
+        for (int q = m.csr_start[k]; q < m.csr_start[k + 1]; q++) {
+            const int e = m.csr[q];
+            const int r = e >> 8;
+            const double nu = small_int_to_double((int)(int8_t)(e & 0xff));
+            const Reaction& x = m.tb.reactions[r];
+            const double a = nu * w.kf[r];
+            for (int i = 0; i < x.n_r; i++) {
+                const int j = x.r_k[i];
+                row[j == K - 1 ? 0 : 2 + j] += a * deriv_product(w.C, x.r_k, x.r_n, x.n_r, i);
+            }
+            if (x.model != 1) {
+                const double b = -a * w.pK[r];
+                for (int i = 0; i < x.n_p; i++) {
+                    const int j = x.p_k[i];
+                    row[j == K - 1 ? 0 : 2 + j] += b * deriv_product(w.C, x.p_k, x.p_n, x.n_p, i);
+                }
+            }
+            if (x.eff_row >= 0) {  // M = C_total + sum (e_j - 1) C_j
+                const double sm = nu * w.sM[r];
+                const double* E = m.tb.eff + (size_t)x.eff_row * K;
+                for (int j = 0; j < K - 1; j++) row[2 + j] = fma(sm, E[j], row[2 + j]);
+                row[0] = fma(sm, E[K - 1], row[0]);
+            }
+        }
+        // to the state variables: C_j = n_j / V (j < K-1), C_bulk = C_total - sum_j C_j
+        const double gb = row[0];
+        double sv = 0.0;
+        for (int i = 0; i < K - 1; i++) {
+            const double gi = row[2 + i];
+            sv = fma(gi, w.C[i], sv);
+            row[2 + i] = (gi - gb) * o.md;
+        }
+        row[1] = -o.md * fma(-gb, o.S, sv);
+        row[0] = 0.0;
+    }
+    // d(C_p)/dV needs sum_{i<K-1} cp_i C_i
+    double scp = 0.0;
+    for (int i = lane; i < K - 1; i += 32) scp = fma(w.cpk[i], w.C[i], scp);
+    scp = warp_sum(scp);
+    __syncwarp();
+    // T and V rows through dT/dt = -T E / Cp and dV/dt = V (dT/dt / T + R/P T dtE)
+    const double rcpT = rcp64(o.T), rCp = rcp64(o.Cp);
+    const double a0 = -o.T * rCp, b0 = (o.T * o.E) * (rCp * rCp);
+    const double cpb = w.cpk[K - 1];
+    for (int j = 1 + lane; j < N; j += 32) {
+        double sh = 0.0, se = 0.0;
+        for (int k = 0; k < A; k++) {
+            const double jk = Jm[(size_t)(2 + k) * LD + j];
+            sh = fma(w.hk[k], jk, sh);
+            se = fma(m.tb.species[k].dtE, jk, se);
+        }
+        const double dCp = j == 1 ? -o.md * fma(-cpb, o.S, scp) : (w.cpk[j - 2] - cpb) * o.md;
+        const double j0 = fma(a0, sh, b0 * dCp);
+        double j1 = o.V * fma(rP * o.T, se, j0 * rcpT);
+        if (j == 1) j1 += w.f[1] * o.md;
+        Jm[j] = j0;
+        Jm[(size_t)LD + j] = j1;
+    }
+    __syncwarp();
+    // temperature column: forward difference
+    const double dT = 1.4901161193847656e-8 * fmax(fabs(o.T), 1.0);
+    for (int i = lane; i < N; i += 32) w.b[i] = y[i];
+    __syncwarp();
+    if (lane == 0) w.b[0] = y[0] + dT;
+    __syncwarp();
+    const double dTa = w.b[0] - y[0];  // the increment actually represented
+    rhs_warp<false>(p, m, w, pR, rP, w.b, w.tmp, lane);
+    const double rdT = 1.0 / dTa;
+    for (int i = lane; i < N; i += 32) Jm[(size_t)i * LD] = (w.tmp[i] - w.f[i]) * rdT;
+    __syncwarp();
+    if (Jg)
+        for (int idx = lane; idx < N * N; idx += 32) Jg[idx] = Jm[(size_t)(idx / N) * LD + idx % N];
+    __syncwarp();
+}
+
+// In-place LU with partial pivoting of the N x N matrix in A (rows of LD); false on a zero pivot.
+__device__ bool lu_warp(double* A, int N, int LD, int* piv, double* rdiag, int lane) {
+    for (int k = 0; k < N; k++) {
+        double best = -1.0;
+        int bi = k;
+        for (int i = k + lane; i < N; i += 32) {
+            const double v = fabs(A[(size_t)i * LD + k]);
+            if (v > best) {
+                best = v;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        best = __shfl_sync(0xffffffffu, best, 0);
+        bi = __shfl_sync(0xffffffffu, bi, 0);
+        if (!(best > 0.0) || !(best < 1e300)) return false;
+        if (lane == 0) piv[k] = bi;
+        if (bi != k)
+            for (int j = lane; j < N; j += 32) {
+                const double t = A[(size_t)k * LD + j];
+                A[(size_t)k * LD + j] = A[(size_t)bi * LD + j];
+                A[(size_t)bi * LD + j] = t;
+            }
+        __syncwarp();
+        const double rp = 1.0 / A[(size_t)k * LD + k];
+        if (lane == 0) rdiag[k] = rp;
+        for (int i = k + 1 + lane; i < N; i += 32) A[(size_t)i * LD + k] *= rp;
+        __syncwarp();
+        for (int j = k + 1 + lane; j < N; j += 32) {
+            const double akj = A[(size_t)k * LD + j];
+            for (int i = k + 1; i < N; i++) A[(size_t)i * LD + j] = fma(-A[(size_t)i * LD + k], akj, A[(size_t)i * LD + j]);
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+__device__ void lu_solve_warp(const double* A, int N, int LD, const int* piv, const double* rdiag, double* b, int lane) {
+    if (lane == 0)
+        for (int k = 0; k < N; k++) {
+            const int pk = piv[k];
+            if (pk != k) {
+                const double t = b[k];
+                b[k] = b[pk];
+                b[pk] = t;
+            }
+        }
+    __syncwarp();
+    for (int k = 0; k < N; k++) {
+        const double bk = b[k];
+        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-A[(size_t)i * LD + k], bk, b[i]);
+        __syncwarp();
+    }
+    for (int k = N - 1; k >= 0; k--) {
+        const double bk = b[k] * rdiag[k];
+        __syncwarp();
+        if (lane == 0) b[k] = bk;
+        for (int i = lane; i < k; i += 32) b[i] = fma(-A[(size_t)i * LD + k], bk, b[i]);
+        __syncwarp();
+    }
+}
+
+// I - c J (J in w.LU already when `fresh`, else from global) factorised in w.LU.
+__device__ bool build_lu(const Params& p, const Work& w, const double* Jg, double c, bool fresh, int lane) {
+    const int N = p.N, LD = p.LD;
+    for (int idx = lane; idx < N * N; idx += 32) {
+        const int i = idx / N, j = idx % N;
+        const double Jij = fresh ? w.LU[(size_t)i * LD + j] : Jg[idx];
+        w.LU[(size_t)i * LD + j] = (i == j ? 1.0 : 0.0) - c * Jij;
+    }
+    __syncwarp();
+    return lu_warp(w.LU, N, LD, w.piv, w.rdiag, lane);
+}
+
+__device__ __forceinline__ double rms_scaled(const double* x, const double* scale, int N, int lane) {
+    double s = 0.0;
+    for (int i = lane; i < N; i += 32) {
+        const double v = x[i] / scale[i];
+        s = fma(v, v, s);
+    }
+    return sqrt(warp_sum(s) / N);
+}
+
+// D[0..q] <- (R U)^T D[0..q], R = R(q, factor), U = R(q, 1) (step size change by `factor`).
+__device__ void change_D(double* D, int N, int q, double factor, int lane) {
+    double R[kMaxOrder + 1][kMaxOrder + 1], U[kMaxOrder + 1][kMaxOrder + 1];
+    for (int j = 0; j <= q; j++) {
+        R[0][j] = 1.0;
+        U[0][j] = 1.0;
+    }
+    for (int i = 1; i <= q; i++)
+        for (int j = 0; j <= q; j++) {
+            const double mr = j == 0 ? 0.0 : ((double)(i - 1) - factor * j) / i;
+            const double mu = j == 0 ? 0.0 : ((double)(i - 1) - (double)j) / i;
+            R[i][j] = R[i - 1][j] * mr;
+            U[i][j] = U[i - 1][j] * mu;
+        }
+    double RU[kMaxOrder + 1][kMaxOrder + 1];
+    for (int i = 0; i <= q; i++)
+        for (int j = 0; j <= q; j++) {
+            double s = 0.0;
+            for (int k = 0; k <= q; k++) s = fma(R[i][k], U[k][j], s);
+            RU[i][j] = s;
+        }
+    for (int col = lane; col < N; col += 32) {
+        double old[kMaxOrder + 1];
+        for (int m = 0; m <= q; m++) old[m] = D[(size_t)m * N + col];
+        for (int i = 0; i <= q; i++) {
+            double s = 0.0;
+            for (int m = 0; m <= q; m++) s = fma(RU[m][i], old[m], s);
+            D[(size_t)i * N + col] = s;
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ double gamma_k(int k) {  // sum_{i=1..k} 1/i
+    double g = 0.0;
+    for (int i = 1; i <= k; i++) g += 1.0 / i;
+    return g;
+}
+
+// One reactor for at most `budget` steps (warp-uniform control flow).
+__device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, int lane) {
+    const int N = p.N;
+    Head hd = p.head[r];
+    if (hd.state != kNew && hd.state != kRunning) return;
+    double* Dg = p.D + (size_t)r * kDRows * N;
+    double* Jg = p.J + (size_t)r * N * N;
+    const double pR = p.pR[r], rP = 1.0 / pR;
+    for (int i = lane; i < kDRows * N; i += 32) w.D[i] = Dg[i];
+    __syncwarp();
+    bool lu_valid = false;
+    if (hd.state == kNew) {
+        // f(y0), initial step (Hairer, Norsett and Wanner, Solving ODEs I, II.4), D_1 = h f(y0), J(y0)
+        for (int i = lane; i < N; i += 32) w.y[i] = w.D[i];
+        __syncwarp();
+        rhs_warp<false>(p, m, w, pR, rP, w.y, w.f, lane);
+        hd.rhs++;
+        for (int i = lane; i < N; i += 32) w.scale[i] = p.atol + p.rtol * fabs(w.y[i]);
+        __syncwarp();
+        const double d0 = rms_scaled(w.y, w.scale, N, lane), d1 = rms_scaled(w.f, w.scale, N, lane);
+        const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
+        for (int i = lane; i < N; i += 32) w.b[i] = fma(h0, w.f[i], w.y[i]);
+        __syncwarp();
+        rhs_warp<false>(p, m, w, pR, rP, w.b, w.tmp, lane);
+        hd.rhs++;
+        for (int i = lane; i < N; i += 32) w.b[i] = w.tmp[i] - w.f[i];
+        __syncwarp();
+        const double d2 = rms_scaled(w.b, w.scale, N, lane) / h0;
+        const double h1 = (d1 <= 1e-15 && d2 <= 1e-15) ? fmax(1e-6, h0 * 1e-3) : sqrt(0.01 / fmax(d1, d2));
+        double h = fmin(100.0 * h0, h1);
+        h = fmin(h, p.t_end);
+        for (int i = lane; i < N; i += 32) {
+            w.D[N + i] = h * w.f[i];
+            for (int j = 2; j < kDRows; j++) w.D[(size_t)j * N + i] = 0.0;
+        }
+        __syncwarp();
+        const double g0 = w.f[0];
+        hd.t = 0.0;
+        hd.h = h;
+        hd.q = 1;
+        hd.n_equal = 0;
+        hd.ign_t = 0.0;
+        hd.ign_g = g0;
+        hd.ta = hd.ga = hd.tc = hd.gc = NAN;
+        hd.tp = 0.0;
+        hd.gp = g0;
+        hd.need_next = 1;
+        jacobian_warp(p, m, w, pR, rP, w.y, Jg, lane);
+        hd.jacs++;
+        hd.rhs += 2;
+        hd.jac_current = 1;
+        lu_valid = build_lu(p, w, Jg, h / gamma_k(1), true, lane);
+        hd.lus++;
+        hd.state = kRunning;
+    }
+    const double newton_tol = fmax(10.0 * 2.220446049250313e-16 / p.rtol, fmin(0.03, sqrt(p.rtol)));
+    int budget = p.slice_steps;
+    // every rejected attempt shrinks h, so attempts are bounded; the cap only bounds one launch's length
+    int attempts = 8 * p.slice_steps + 64;
+    while (hd.state == kRunning && budget > 0 && attempts-- > 0) {
+        if (hd.steps >= p.max_steps) {
+            hd.state = kFailSteps;
+            break;
+        }
+        int q = hd.q;
+        double h = hd.h;
+        if (hd.t + h > p.t_end) {  // land on t_end
+            const double hn = p.t_end - hd.t;
+            change_D(w.D, N, q, hn / h, lane);
+            h = hn;
+            hd.n_equal = 0;
+            lu_valid = false;
+        }
+        if (!(h >= p.h_min)) {
+            hd.state = kFailStep;
+            break;
+        }
+        const double t_new = hd.t + h;
+        const double gq = gamma_k(q);
+        const double c = h / gq;
+        for (int i = lane; i < N; i += 32) {
+            double yp = 0.0, ps = 0.0;
+            for (int j = 0; j <= q; j++) yp += w.D[(size_t)j * N + i];
+            for (int j = 1; j <= q; j++) ps = fma(gamma_k(j), w.D[(size_t)j * N + i], ps);
+            w.ypred[i] = yp;
+            w.psi[i] = ps / gq;
+            w.scale[i] = p.atol + p.rtol * fabs(yp);
+            w.y[i] = yp;
+            w.d[i] = 0.0;
+        }
+        __syncwarp();
+        if (!lu_valid) {
+            lu_valid = build_lu(p, w, Jg, c, false, lane);
+            hd.lus++;
+        }
+        // Newton iterations on d - c f(t_new, ypred + d) + psi = 0
+        bool converged = false;
+        int n_iter = 0;
+        double dy_norm_old = -1.0;
+        if (lu_valid) {
+            for (int k = 0; k < kNewtonMaxIter; k++) {
+                rhs_warp<false>(p, m, w, pR, rP, w.y, w.f, lane);
+                hd.rhs++;
+                n_iter = k + 1;
+                bool finite = true;
+                for (int i = lane; i < N; i += 32) {
+                    const double fi = w.f[i];
+                    finite &= (fabs(fi) < 1e300);
+                    w.b[i] = fma(c, fi, -w.psi[i]) - w.d[i];
+                }
+                if (!__all_sync(0xffffffffu, finite)) break;
+                __syncwarp();
+                lu_solve_warp(w.LU, N, p.LD, w.piv, w.rdiag, w.b, lane);
+                const double dy_norm = rms_scaled(w.b, w.scale, N, lane);
+                const double rate = dy_norm_old >= 0.0 ? dy_norm / dy_norm_old : -1.0;
+                if (rate >= 0.0 && (rate >= 1.0 || pow(rate, (double)(kNewtonMaxIter - k)) / (1.0 - rate) * dy_norm > newton_tol))
+                    break;
+                for (int i = lane; i < N; i += 32) {
+                    w.y[i] += w.b[i];
+                    w.d[i] += w.b[i];
+                }
+                __syncwarp();
+                if (dy_norm == 0.0 || (rate >= 0.0 && rate / (1.0 - rate) * dy_norm < newton_tol)) {
+                    converged = true;
+                    break;
+                }
+                dy_norm_old = dy_norm;
+            }
+        }
+        if (!converged) {
+            hd.newton_fail++;
+            if (!hd.jac_current) {  // a fresh Jacobian at the predicted state, same step
+                jacobian_warp(p, m, w, pR, rP, w.ypred, Jg, lane);
+                hd.jacs++;
+                hd.rhs += 2;
+                hd.jac_current = 1;
+                lu_valid = build_lu(p, w, Jg, c, true, lane);
+                hd.lus++;
+                hd.h = h;
+                continue;
+            }
+            change_D(w.D, N, q, 0.5, lane);
+            hd.h = 0.5 * h;
+            hd.n_equal = 0;
+            lu_valid = false;
+            continue;
+        }
+        const double safety = 0.9 * (2 * kNewtonMaxIter + 1) / (2 * kNewtonMaxIter + n_iter);
+        for (int i = lane; i < N; i += 32) {
+            w.scale[i] = p.atol + p.rtol * fabs(w.y[i]);
+            w.b[i] = w.d[i] / (q + 1);  // error = error_const(q) d
+        }
+        __syncwarp();
+        const double err_norm = rms_scaled(w.b, w.scale, N, lane);
+        if (err_norm > 1.0) {
+            hd.err_fail++;
+            const double factor = fmax(kMinFactor, safety * pow(err_norm, -1.0 / (q + 1)));
+            change_D(w.D, N, q, factor, lane);
+            hd.h = h * factor;
+            hd.n_equal = 0;
+            continue;  // the factorisation of the failed step is kept: Newton converged with it
+        }
+        // accepted
+        hd.steps++;
+        budget--;
+        hd.t = t_new;
+        hd.jac_current = 0;
+        for (int i = lane; i < N; i += 32) {
+            const double di = w.d[i];
+            w.D[(size_t)(q + 2) * N + i] = di - w.D[(size_t)(q + 1) * N + i];
+            w.D[(size_t)(q + 1) * N + i] = di;
+            for (int j = q; j >= 0; j--) w.D[(size_t)j * N + i] += w.D[(size_t)(j + 1) * N + i];
+        }
+        __syncwarp();
+        hd.n_equal++;
+        // dT/dt at the new point from the backward differences: h y' = sum_{j=1..q} D_j / j
+        double g = 0.0;
+        for (int j = 1; j <= q; j++) g += w.D[(size_t)j * N] / j;
+        g /= h;
+        if (hd.need_next) {
+            hd.tc = t_new;
+            hd.gc = g;
+            hd.need_next = 0;
+        }
+        if (g > hd.ign_g) {
+            hd.ta = hd.tp;
+            hd.ga = hd.gp;
+            hd.ign_t = t_new;
+            hd.ign_g = g;
+            hd.need_next = 1;
+        }
+        hd.tp = t_new;
+        hd.gp = g;
+        if (t_new >= p.t_end) {
+            hd.state = kDone;
+            hd.h = h;
+            break;
+        }
+        if (hd.n_equal < q + 1) {
+            hd.h = h;
+            continue;
+        }
+        // order and step size
+        const double inf = 1e300;
+        double em = inf, ep = inf;
+        if (q > 1) {
+            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)q * N + i] / q;
+            __syncwarp();
+            em = rms_scaled(w.b, w.scale, N, lane);
+        }
+        if (q < kMaxOrder) {
+            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)(q + 2) * N + i] / (q + 2);
+            __syncwarp();
+            ep = rms_scaled(w.b, w.scale, N, lane);
+        }
+        const double fm = em >= inf ? 0.0 : (em > 0.0 ? pow(em, -1.0 / q) : inf);
+        const double fz = err_norm > 0.0 ? pow(err_norm, -1.0 / (q + 1)) : inf;
+        const double fp = ep >= inf ? 0.0 : (ep > 0.0 ? pow(ep, -1.0 / (q + 2)) : inf);
+        int dq = 0;
+        double best = fz;
+        if (fm > best) {
+            best = fm;
+            dq = -1;
+        }
+        if (fp > best) {
+            best = fp;
+            dq = 1;
+        }
+        q += dq;
+        const double factor = fmin(kMaxFactor, safety * best);
+        change_D(w.D, N, q, factor, lane);
+        hd.q = q;
+        hd.h = h * factor;
+        hd.n_equal = 0;
+        lu_valid = false;
+    }
+    for (int i = lane; i < kDRows * N; i += 32) Dg[i] = w.D[i];
+    if (lane == 0) {
+        p.head[r] = hd;
+        if (hd.state != kRunning) atomicAdd(p.done, 1);
+    }
+    __syncwarp();
+}
+
+__global__ void slice_kernel(const Params p) {
+    __shared__ uint64_t bar;
+    const uint8_t* tab = p.tab;
+    if (p.smem_tables) {
+        if (!stage_to_shared(cb_dsmem, p.tab, p.tab_bytes, &bar, p.status)) return;
+        tab = cb_dsmem;
+    } else {
+        load_math(p.tab);
+    }
+    const Mech m(tab, p);
+    const size_t tab_smem = p.smem_tables ? ((p.tab_bytes + 127) & ~127u) : (size_t)kMathBytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Work w = carve(p, cb_dsmem + tab_smem + (size_t)warp * p.ws_bytes);
+    for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(p.queue, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= p.n) break;
+        integrate(p, m, w, r, lane);
+    }
+}
+
+// Evaluation hook: f and J at given states, one warp per state.
+__global__ void eval_kernel(const Params p, int count) {
+    const uint8_t* tab = p.tab;
+    __shared__ uint64_t bar;
+    if (p.smem_tables) {
+        if (!stage_to_shared(cb_dsmem, p.tab, p.tab_bytes, &bar, p.status)) return;
+        tab = cb_dsmem;
+    } else {
+        load_math(p.tab);
+    }
+    const Mech m(tab, p);
+    const size_t tab_smem = p.smem_tables ? ((p.tab_bytes + 127) & ~127u) : (size_t)kMathBytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Work w = carve(p, cb_dsmem + tab_smem + (size_t)warp * p.ws_bytes);
+    const int N = p.N;
+    for (int s = blockIdx.x * (blockDim.x >> 5) + warp; s < count; s += gridDim.x * (blockDim.x >> 5)) {
+        for (int i = lane; i < N; i += 32) w.y[i] = p.eval_y[(size_t)s * N + i];
+        __syncwarp();
+        jacobian_warp(p, m, w, p.pR[s], 1.0 / p.pR[s], w.y, p.eval_J + (size_t)s * N * N, lane);
+        for (int i = lane; i < N; i += 32) p.eval_f[(size_t)s * N + i] = w.f[i];
+        __syncwarp();
+    }
+}
+
+}  // namespace bdf
+}  // namespace cbg
+
+using namespace cbg::bdf;
+
+struct cb_reactors {
+    cb_mech* mech = nullptr;
+    int device = 0;
+    int K = 0, A = 0, R = 0, N = 0, LD = 0, n_eff = 0;
+    size_t n = 0;
+    cb_bdf_options opt{};
+    std::vector<uint8_t> blob;
+    int off_csr_start = 0, off_csr = 0;
+    uint8_t* d_tab = nullptr;
+    double* pR = nullptr;
+    Head* head = nullptr;
+    double* D = nullptr;
+    double* J = nullptr;
+    int* counters = nullptr;  // queue, done, status
+    int warps = 0, smem_tables = -1;  // launch shape (0 / -1: autotune)
+    bool have_state = false;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+#define BDF_CUDA(call)                                           \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return cbi::cuda_fail(e_, #call); \
+    } while (0)
+
+uint32_t ws_bytes(const cb_reactors* s) {
+    const size_t d = workspace_doubles(s->K, s->A, s->R, s->N, s->LD, s->n_eff);
+    return (uint32_t)(((d * sizeof(double) + (size_t)s->N * sizeof(int)) + 127) & ~(size_t)127);
+}
+
+size_t smem_bytes(const cb_reactors* s, int warps, int tables) {
+    const size_t tab = tables ? ((s->blob.size() + 127) & ~(size_t)127) : (size_t)cbg::kMathBytes;
+    return tab + (size_t)warps * ws_bytes(s);
+}
+
+int max_smem() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v - 1024;
+}
+
+int sm_count() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+}
+
+Params params(cb_reactors* s, int tables) {
+    Params p;
+    std::memset(&p, 0, sizeof p);
+    p.tab = s->d_tab;
+    p.tab_bytes = (uint32_t)s->blob.size();
+    p.smem_tables = tables;
+    p.off_csr_start = s->off_csr_start;
+    p.off_csr = s->off_csr;
+    p.K = s->K;
+    p.A = s->A;
+    p.R = s->R;
+    p.N = s->N;
+    p.LD = s->LD;
+    p.n_eff = s->n_eff;
+    p.ws_bytes = ws_bytes(s);
+    p.n = (int)s->n;
+    p.rtol = s->opt.rtol;
+    p.atol = s->opt.atol;
+    p.t_end = s->opt.t_end;
+    p.h_min = 1e-20;
+    p.max_steps = s->opt.max_steps;
+    p.slice_steps = s->opt.slice_steps;
+    p.pR = s->pR;
+    p.head = s->head;
+    p.D = s->D;
+    p.J = s->J;
+    p.queue = s->counters;
+    p.done = s->counters + 1;
+    p.status = s->counters + 2;
+    return p;
+}
+
+// Shared-memory limit and grid of a launch shape (outside any stream capture).
+cudaError_t prepare_slice(cb_reactors* s, int warps, int tables, int* grid) {
+    const size_t smem = smem_bytes(s, warps, tables);
+    cudaError_t e = cudaFuncSetAttribute(slice_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice_kernel, 32 * warps, smem);
+    if (e != cudaSuccess) return e;
+    *grid = sm_count() * (per_sm < 1 ? 1 : per_sm);
+    return cudaSuccess;
+}
+
+cudaError_t launch_slice(cb_reactors* s, int warps, int tables, int grid, cudaStream_t st) {
+    slice_kernel<<<grid, 32 * warps, smem_bytes(s, warps, tables), st>>>(params(s, tables));
+    return cudaGetLastError();
+}
+
+bool shape_fits(cb_reactors* s, int warps, int tables) { return (int)smem_bytes(s, warps, tables) <= max_smem(); }
+
+}  // namespace
+
+extern "C" {
+
+int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_reactors** out) {
+    if (!mech || !opt || !out) return cbi::fail(CB_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (n == 0 || n > (1u << 30)) return cbi::fail(CB_ERR_INVALID, "reactor count out of range");
+    if (!(opt->rtol > 0) || !(opt->atol > 0) || !(opt->t_end > 0) || opt->max_steps <= 0)
+        return cbi::fail(CB_ERR_INVALID, "bad integrator options");
+    const cbi::MechView v = cbi::view(mech);
+    if (v.A != v.K - 1)
+        return cbi::fail(CB_ERR_UNSUPPORTED, "reactors need every non-bulk species active (inert non-bulk species "
+                                             "would be parameters, not state)");
+    if (v.K + 1 > kMaxN) return cbi::fail(CB_ERR_UNSUPPORTED, "at most 65 species for the batched integrator");
+    cb_reactors* s = new cb_reactors();
+    s->mech = mech;
+    s->device = v.device;
+    s->K = v.K;
+    s->A = v.A;
+    s->N = v.A + 2;
+    s->LD = s->N | 1;
+    s->n = n;
+    s->opt = *opt;
+    if (s->opt.slice_steps <= 0) s->opt.slice_steps = 256;
+    s->warps = opt->warps_per_block;
+    s->smem_tables = opt->tables_in_shared;
+    // tables: the rates blob, then the per-species (reaction, coefficient) lists in reaction order
+    const std::vector<uint8_t>& rb = *v.rates_blob;
+    cbg::RatesHeader H;
+    std::memcpy(&H, rb.data() + cbg::kMathBytes, sizeof H);
+    s->R = H.R;
+    s->n_eff = H.n_eff;
+    std::vector<std::vector<int>> lists(s->A);
+    for (int r = 0; r < H.R; r++) {
+        cbg::Reaction x;
+        std::memcpy(&x, rb.data() + H.off_reactions + (size_t)r * sizeof x, sizeof x);
+        for (int q = 0; q < x.n_net; q++)
+            if (x.net_k[q] < s->A) lists[x.net_k[q]].push_back((r << 8) | (x.net_n[q] & 0xff));
+    }
+    s->blob = rb;
+    while (s->blob.size() % 16) s->blob.push_back(0);
+    s->off_csr_start = (int)s->blob.size();
+    std::vector<int> start(s->A + 1, 0), flat;
+    for (int k = 0; k < s->A; k++) {
+        start[k] = (int)flat.size();
+        flat.insert(flat.end(), lists[k].begin(), lists[k].end());
+    }
+    start[s->A] = (int)flat.size();
+    s->blob.resize(s->blob.size() + start.size() * 4);
+    std::memcpy(s->blob.data() + s->off_csr_start, start.data(), start.size() * 4);
+    while (s->blob.size() % 16) s->blob.push_back(0);
+    s->off_csr = (int)s->blob.size();
+    s->blob.resize(s->blob.size() + std::max<size_t>(flat.size(), 1) * 4);
+    if (!flat.empty()) std::memcpy(s->blob.data() + s->off_csr, flat.data(), flat.size() * 4);
+    while (s->blob.size() % 16) s->blob.push_back(0);
+    auto fail_free = [&](int rc) {
+        cb_reactors_destroy(s);
+        return rc;
+    };
+    cudaError_t e = cudaSetDevice(s->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_tab, s->blob.size());
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_tab, s->blob.data(), s->blob.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&s->pR, n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->head, n * sizeof(Head));
+    if (e == cudaSuccess) e = cudaMalloc(&s->D, n * kDRows * (size_t)s->N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->J, n * (size_t)s->N * s->N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->counters, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(s->counters, 0, 4 * sizeof(int));
+    if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor batch allocation"));
+    if (!shape_fits(s, 1, 0)) return fail_free(cbi::fail(CB_ERR_UNSUPPORTED, "reactor workspace exceeds shared memory"));
+    *out = s;
+    return CB_OK;
+}
+
+int cb_reactors_destroy(cb_reactors* s) {
+    if (!s) return CB_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) {
+        cudaStreamSynchronize(s->stream);
+        cudaStreamDestroy(s->stream);
+    }
+    cudaFree(s->d_tab);
+    cudaFree(s->pR);
+    cudaFree(s->head);
+    cudaFree(s->D);
+    cudaFree(s->J);
+    cudaFree(s->counters);
+    delete s;
+    return CB_OK;
+}
+
+int cb_reactors_set_state(cb_reactors* s, const double* pressure_R, const double* T, const double* V,
+                          const double* amounts) {
+    if (!s || !pressure_R || !T || !V || !amounts) return cbi::fail(CB_ERR_INVALID, "null argument");
+    const size_t n = s->n;
+    const int N = s->N;
+    std::vector<double> D(n * kDRows * (size_t)N, 0.0);
+    for (size_t r = 0; r < n; r++) {
+        if (!(T[r] > 0) || !(V[r] > 0) || !(pressure_R[r] > 0)) return cbi::fail(CB_ERR_INVALID, "non-positive T, V or P");
+        double* y = D.data() + r * kDRows * N;
+        y[0] = T[r];
+        y[1] = V[r];
+        for (int k = 0; k < s->A; k++) y[2 + k] = amounts[(size_t)k * n + r];
+    }
+    BDF_CUDA(cudaSetDevice(s->device));
+    BDF_CUDA(cudaMemcpy(s->D, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice));
+    BDF_CUDA(cudaMemcpy(s->pR, pressure_R, n * sizeof(double), cudaMemcpyHostToDevice));
+    BDF_CUDA(cudaMemset(s->head, 0, n * sizeof(Head)));
+    BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
+    s->have_state = true;
+    return CB_OK;
+}
+
+int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuning* out) {
+    if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
+    if (!s->have_state) return cbi::fail(CB_ERR_NOT_READY, "cb_reactors_set_state has not run");
+    BDF_CUDA(cudaSetDevice(s->device));
+    // candidates: reactors in flight per block, tables in shared memory or read through L1
+    struct Cand { int warps, tables; };
+    std::vector<Cand> cands;
+    for (int tables = 1; tables >= 0; tables--)
+        for (int w = 1; w <= 8; w++)
+            if (shape_fits(s, w, tables)) cands.push_back({w, tables});
+    if (cands.empty()) return cbi::fail(CB_ERR_UNSUPPORTED, "no launch shape fits");
+    // calibrate on copies of the state: a few slices of the first reactors, then restore the state
+    const size_t n_cal = std::min<size_t>(s->n, calib_reactors > 0 ? (size_t)calib_reactors : 4096);
+    const size_t hb = s->n * sizeof(Head), db = s->n * kDRows * (size_t)s->N * sizeof(double);
+    std::vector<uint8_t> h0(hb), d0(db);
+    BDF_CUDA(cudaMemcpy(h0.data(), s->head, hb, cudaMemcpyDeviceToHost));
+    BDF_CUDA(cudaMemcpy(d0.data(), s->D, db, cudaMemcpyDeviceToHost));
+    const size_t n_save = s->n;
+    const int steps_save = s->opt.slice_steps;
+    s->n = n_cal;
+    s->opt.slice_steps = 16;
+    double best = 1e300;
+    Cand pick = cands[0];
+    cudaEvent_t a, b;
+    BDF_CUDA(cudaEventCreate(&a));
+    BDF_CUDA(cudaEventCreate(&b));
+    int tried = 0;
+    for (const Cand& c : cands) {
+        cudaMemcpy(s->head, h0.data(), n_cal * sizeof(Head), cudaMemcpyHostToDevice);
+        cudaMemcpy(s->D, d0.data(), n_cal * kDRows * (size_t)s->N * sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemset(s->counters, 0, 4 * sizeof(int));
+        int grid = 0;
+        if (prepare_slice(s, c.warps, c.tables, &grid) != cudaSuccess) continue;
+        cudaEventRecord(a, s->stream);
+        for (int rep = 0; rep < 2; rep++) {  // two slices: the first includes each reactor's start-up
+            cudaMemsetAsync(s->counters, 0, sizeof(int), s->stream);
+            if (launch_slice(s, c.warps, c.tables, grid, s->stream) != cudaSuccess) break;
+        }
+        cudaEventRecord(b, s->stream);
+        if (cudaEventSynchronize(b) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (out && tried < 16) {
+            out->candidates[tried].warps_per_block = c.warps;
+            out->candidates[tried].tables_in_shared = c.tables;
+            out->candidates[tried].ms = ms;
+        }
+        tried++;
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    s->n = n_save;
+    s->opt.slice_steps = steps_save;
+    BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
+    BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
+    BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
+    BDF_CUDA(cudaGetLastError());
+    s->warps = pick.warps;
+    s->smem_tables = pick.tables;
+    if (out) {
+        out->warps_per_block = pick.warps;
+        out->tables_in_shared = pick.tables;
+        out->n_candidates = std::min(tried, 16);
+        out->calib_reactors = (int32_t)n_cal;
+    }
+    int st = 0;
+    BDF_CUDA(cudaMemcpy(&st, s->counters + 2, sizeof st, cudaMemcpyDeviceToHost));
+    if (st) return cbi::fail(CB_ERR_DEVICE, "table staging wait ran out during tuning");
+    return CB_OK;
+}
+
+int cb_reactors_integrate(cb_reactors* s, cb_reactor_stats* stats) {
+    if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
+    if (!s->have_state) return cbi::fail(CB_ERR_NOT_READY, "cb_reactors_set_state has not run");
+    BDF_CUDA(cudaSetDevice(s->device));
+    if (s->warps <= 0 || s->smem_tables < 0) {
+        int rc = cb_reactors_autotune(s, 0, nullptr);
+        if (rc) return rc;
+    }
+    if (!shape_fits(s, s->warps, s->smem_tables)) return cbi::fail(CB_ERR_INVALID, "launch shape exceeds shared memory");
+    cudaStream_t st = s->stream;
+    int grid = 0;
+    BDF_CUDA(prepare_slice(s, s->warps, s->smem_tables, &grid));
+    // one graph: G slices, each a queue reset and a slice launch
+    const int G = 4;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BDF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int g = 0; g < G && e == cudaSuccess; g++) {
+        e = cudaMemsetAsync(s->counters, 0, sizeof(int), st);
+        if (e == cudaSuccess) e = launch_slice(s, s->warps, s->smem_tables, grid, st);
+    }
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cbi::cuda_fail(e != cudaSuccess ? e : e2, "reactor slice capture");
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cbi::cuda_fail(e, "reactor slice graph");
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, st);
+    // every replay advances each unfinished reactor by up to G slices; bounded by the step limit
+    const long long max_replays = (long long)s->opt.max_steps / ((long long)G * s->opt.slice_steps) + 4;
+    int done = 0, replays = 0;
+    for (long long rep = 0; rep < max_replays; rep++) {
+        e = cudaGraphLaunch(exec, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&done, s->counters + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        replays++;
+        if (e != cudaSuccess || done >= (int)s->n) break;
+    }
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaGraphExecDestroy(exec);
+    if (e != cudaSuccess) return cbi::cuda_fail(e, "reactor integration");
+    int status = 0;
+    BDF_CUDA(cudaMemcpy(&status, s->counters + 2, sizeof status, cudaMemcpyDeviceToHost));
+    if (status) return cbi::fail(CB_ERR_DEVICE, "table staging wait ran out");
+    if (stats) {
+        std::memset(stats, 0, sizeof *stats);
+        std::vector<Head> h(s->n);
+        BDF_CUDA(cudaMemcpy(h.data(), s->head, s->n * sizeof(Head), cudaMemcpyDeviceToHost));
+        for (const Head& x : h) {
+            stats->steps += x.steps;
+            stats->rhs_evals += x.rhs;
+            stats->jacobians += x.jacs;
+            stats->factorizations += x.lus;
+            stats->newton_failures += x.newton_fail;
+            stats->error_failures += x.err_fail;
+            if (x.state == kDone) stats->finished++;
+            else if (x.state != kRunning && x.state != kNew) stats->failed++;
+        }
+        stats->ms = ms;
+        stats->warps_per_block = s->warps;
+        stats->tables_in_shared = s->smem_tables;
+        stats->graph_replays = replays;
+        stats->slices = replays * G;
+    }
+    return CB_OK;
+}
+
+int cb_reactors_results(cb_reactors* s, double* ignition_delay, double* state, int32_t* status, int32_t* steps) {
+    if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
+    BDF_CUDA(cudaSetDevice(s->device));
+    const size_t n = s->n;
+    const int N = s->N;
+    std::vector<Head> h(n);
+    BDF_CUDA(cudaMemcpy(h.data(), s->head, n * sizeof(Head), cudaMemcpyDeviceToHost));
+    if (state) {
+        std::vector<double> D(n * kDRows * (size_t)N);
+        BDF_CUDA(cudaMemcpy(D.data(), s->D, D.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < n; r++)
+            for (int i = 0; i < N; i++) state[(size_t)i * n + r] = D[r * kDRows * N + i];
+    }
+    for (size_t r = 0; r < n; r++) {
+        const Head& x = h[r];
+        if (ignition_delay) {
+            // vertex of the parabola through the samples around the largest dT/dt
+            double t = x.ign_t;
+            if (std::isfinite(x.ta) && std::isfinite(x.tc) && x.tc > x.ign_t && x.ta < x.ign_t && !x.need_next) {
+                const double d1 = x.ign_t - x.ta, d2 = x.ign_t - x.tc;
+                const double num = d1 * d1 * (x.ign_g - x.gc) - d2 * d2 * (x.ign_g - x.ga);
+                const double den = d1 * (x.ign_g - x.gc) - d2 * (x.ign_g - x.ga);
+                if (den != 0.0) {
+                    const double v = x.ign_t - 0.5 * num / den;
+                    if (v > x.ta && v < x.tc) t = v;
+                }
+            }
+            ignition_delay[r] = t;
+        }
+        if (status) status[r] = x.state;
+        if (steps) steps[r] = x.steps;
+    }
+    return CB_OK;
+}
+
+int cb_reactors_eval(cb_reactors* s, int32_t m, const double* pressure_R, const double* states, double* f, double* J) {
+    if (!s || !pressure_R || !states || !f || !J || m <= 0) return cbi::fail(CB_ERR_INVALID, "bad argument");
+    BDF_CUDA(cudaSetDevice(s->device));
+    const int N = s->N;
+    double *dy = nullptr, *df = nullptr, *dJ = nullptr, *dp = nullptr;
+    auto cleanup = [&](int rc) {
+        cudaFree(dy);
+        cudaFree(df);
+        cudaFree(dJ);
+        cudaFree(dp);
+        return rc;
+    };
+    cudaError_t e = cudaMalloc(&dy, (size_t)m * N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&df, (size_t)m * N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dJ, (size_t)m * N * N * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dp, (size_t)m * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(dy, states, (size_t)m * N * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dp, pressure_R, (size_t)m * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cleanup(cbi::cuda_fail(e, "evaluation buffers"));
+    Params p = params(s, shape_fits(s, 1, 1) ? 1 : 0);
+    p.pR = dp;
+    p.eval_y = dy;
+    p.eval_f = df;
+    p.eval_J = dJ;
+    const size_t smem = smem_bytes(s, 1, p.smem_tables);
+    e = cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) {
+        eval_kernel<<<std::min(m, sm_count()), 32, smem, s->stream>>>(p, m);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(f, df, (size_t)m * N * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(J, dJ, (size_t)m * N * N * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cleanup(cbi::cuda_fail(e, "evaluation"));
+    int st = 0;
+    cudaMemcpy(&st, s->counters + 2, sizeof st, cudaMemcpyDeviceToHost);
+    if (st) return cleanup(cbi::fail(CB_ERR_DEVICE, "table staging wait ran out"));
+    return cleanup(CB_OK);
+}
+
+}  // extern "C"

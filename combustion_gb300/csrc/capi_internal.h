@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/combustion_gb300.h"
 
@@ -17,6 +18,7 @@ struct MechView {
     int K, A, device;
     int transport_ready;
     double T0;
+    const std::vector<uint8_t>* rates_blob;  // host copy of the rates tables
 };
 MechView view(const cb_mech* m);
 

@@ -10,55 +10,10 @@
 #include "device_common.cuh"
 #include "device_math.cuh"
 #include "kernels.h"
+#include "rates_core.cuh"
 #include "tables.h"
 
 namespace cbg {
-
-
-struct Temps {
-    double lnT, T, T2, T3, T4, rcpT, rcpT2;
-};
-
-__device__ __forceinline__ double factor_of(int f, const Temps& t) {
-    switch (f) {
-    case kRcpT2: return t.rcpT2;
-    case kRcpT: return t.rcpT;
-    case kT4: return t.T4;
-    case kT3: return t.T3;
-    case kT2: return t.T2;
-    case kT: return t.T;
-    default: return 1.0;
-    }
-}
-
-// arrhenius() of reaction.rs:113-139; the has_x and factor branches are uniform across the warp.
-__device__ __forceinline__ double arrhenius(const Arrhenius& a, const Temps& t) {
-    double k;
-    if (a.has_x) {
-        double x = fma(a.beta, t.lnT, fma(a.mEa, t.rcpT, a.lnA));
-        k = exp64(x);  // beta includes the power of T (tables.h)
-    } else {
-        k = a.factor != kNone ? factor_of(a.factor, t) * a.A : a.A;
-    }
-    return min_pos(kF32Max, k);
-}
-
-// Piece 0 for T <= split (lib.rs:15); NaN splits (one piece) select piece 0 as well.
-__device__ __forceinline__ int piece_of(double split, double T) { return bits(T) <= bits(split) ? 0 : 1; }
-
-struct RatesTables {
-    const RatesHeader* H;
-    const Species* species;
-    const Reaction* reactions;
-    const Falloff* falloff;
-    const double* eff;
-    __device__ explicit RatesTables(const uint8_t* tab)
-        : H(reinterpret_cast<const RatesHeader*>(tab + kMathBytes)),
-          species(reinterpret_cast<const Species*>(tab + H->off_species)),
-          reactions(reinterpret_cast<const Reaction*>(tab + H->off_reactions)),
-          falloff(reinterpret_cast<const Falloff*>(tab + H->off_falloff)),
-          eff(reinterpret_cast<const double*>(tab + H->off_eff)) {}
-};
 
 template <int KMAX>
 struct Cell {
@@ -68,16 +23,6 @@ struct Cell {
     double ex[KMAX], exn[KMAX];  // min(M3, exp(g_k)), min(cbrt(f32::MAX), exp(-g_k))
     double M[4 * KMAX];          // third-body concentrations C + sum (e_k - 1) C_k, one per efficiency row
 };
-
-// (double)v for a small integer with integer instructions only (no FP64 conversion on the FP64 pipe).
-__device__ __forceinline__ double small_int_to_double(int v) {
-    if (v == 0) return 0.0;
-    const unsigned a = v < 0 ? (unsigned)(-v) : (unsigned)v;
-    const int e = 31 - __clz(a);
-    const unsigned long long mant = (unsigned long long)(a ^ (1u << e)) << (52 - e);
-    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
-}
 
 // Prologue of reaction.rs:362-373 and the Gibbs exponentials of reaction.rs:234-263.
 template <int KMAX>
@@ -128,99 +73,11 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
     }
 }
 
-// Product of concentrations with multiplicities (product_of_exponentiations, reaction.rs:53-63),
-// seeded with the first factor.
-__device__ __forceinline__ double conc_product(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
-    double p = C[ks[0]];
-#pragma unroll 1
-    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
-#pragma unroll 1
-    for (int q = 1; q < n; q++)
-#pragma unroll 1
-        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
-    return p;
-}
-
-// cR of one reaction (reaction.rs:149-309): forward rate constant (with third-body efficiency and
-// falloff), rate of progress against the equilibrium constant, and their product.
-// MODEL is a compile-time constant: reactions are grouped by model, so no model branch (and no
-// predicated FP64 instruction of another model) is executed per reaction.
-template <int KMAX, int MODEL>
-__device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const Cell<KMAX>& c) {
-    const RatesHeader& H = *tb.H;
-    const Temps& t = c.t;
-    double kf;  // forward rate coefficient: k, k M, or the falloff-blended value
-    if constexpr (MODEL == 4) {  // Troe (reaction.rs:160-193)
-        const double M = c.M[x.eff_row];
-        const Falloff& f = tb.falloff[x.falloff];
-        const double k0 = arrhenius(f.k0, t);
-        double Pr, kinf;
-        if (f.flags & kKinfConst) {
-            Pr = M * k0;
-            kinf = f.ainf;
-        } else {
-            const double ki = arrhenius(x.k, t);
-            Pr = div64(M * k0, ki + kF32MinPos);
-            kinf = f.ainf * ki;
-        }
-        double lnF;
-        if (f.flags & kFcentConst) {
-            lnF = f.ln_fcent;
-        } else {
-            double F = 0.0;
-            if (f.flags & kTermT3) F = f.c1mA * exp64(t.T * f.c3);
-            if (f.flags & kTermT1) F += f.cA * exp64(t.T * f.c1);
-            if (f.flags & kTermAConst) F += f.cA;
-            if (f.flags & kTermT2) F += exp64(f.cmT2 * t.rcpT);
-            lnF = log64(F);
-        }
-        const double Cc = fma(-0.67, lnF, -H.ln10_04);
-        const double Nn = fma(-1.27, lnF, H.ln10_075);
-        const double lnPrC = log64(Pr + kF32MinPos) + Cc;
-        const double f1 = div64(lnPrC, fma(-0.14, lnPrC, Nn));
-        const double Fb = exp64(div64(lnF, fma(f1, f1, 1.0)));
-        kf = div64((Fb * kinf) * Pr, Pr + 1.0);
-    } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
-        const Falloff& f = tb.falloff[x.falloff];
-        const double Ck0 = c.M[x.eff_row] * arrhenius(f.k0, t);
-        const double ki = arrhenius(x.k, t);
-        kf = div64(Ck0 * ki, (Ck0 + ki) + kF32MinPos);
-    } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
-        kf = arrhenius(x.k, t) * c.M[x.eff_row];
-    } else {  // elementary, irreversible
-        kf = arrhenius(x.k, t);
-    }
-    // Rate of progress (reaction.rs:269-306).
-    const double Rf = conc_product(c.C, x.r_k, x.r_n, x.n_r);
-    double Rnet = Rf;
-    if constexpr (MODEL != 1) {
-        // 1/Kc: product of the cached Gibbs exponentials, repeated |nu| times, in species order.
-        const int nu0 = x.net_n[0];
-        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
-        double p = t0;
-#pragma unroll 1
-        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
-#pragma unroll 1
-        for (int q = 1; q < x.n_net; q++) {
-            const int nu = x.net_n[q], k = x.net_k[q];
-            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
-#pragma unroll 1
-            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
-        }
-        // (P0/RT)^(-sum nu): the factor chosen with integer selects, one multiply for every reaction.
-        const int msn = x.minus_sigma_net;
-        const double cfac = msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
-        p *= cfac;
-        Rnet = fma(-p, conc_product(c.C, x.p_k, x.p_n, x.n_p), Rf);
-    }
-    return kf * Rnet;
-}
-
 template <int KMAX, int MODEL>
 __device__ __forceinline__ void accumulate_group(const RatesTables& tb, const Cell<KMAX>& c, double* wdot) {
     for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
         const Reaction& x = tb.reactions[r];
-        const double cR = reaction_rate<KMAX, MODEL>(tb, x, c);
+        const double cR = reaction_rate<MODEL>(tb, x, c);
 #pragma unroll 1
         for (int q = 0; q < x.n_net; q++)
             wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
@@ -232,7 +89,7 @@ __device__ __forceinline__ void rates_of_group(const RatesTables& tb, const Cell
                                                const ReactionRatesArgs<KMAX>& io, size_t i) {
     for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
         const Reaction& x = tb.reactions[r];
-        io.out[x.orig][i] = reaction_rate<KMAX, MODEL>(tb, x, c);
+        io.out[x.orig][i] = reaction_rate<MODEL>(tb, x, c);
     }
 }
 
@@ -467,26 +324,34 @@ int sm_count() {
     return sms;
 }
 
+template <class Args>
+bool gathered(const Args&) { return false; }
+template <int KMAX>
+bool gathered(const TransportArgs<KMAX>& io) { return io.index != nullptr; }
+
 // Persistent grid: as many blocks as fit on the GPU at once (each stages the tables once), never more
 // than the cells need. Tables go to shared memory when they fit, else they are read through L1/L2.
 template <int BLOCK, class Args, class KS, class KG>
 cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io,
                                 size_t n, cudaStream_t st, int* status) {
     const bool smem = (int)tab_bytes <= max_table_smem();
+    // Gathered cells are few (a trust gate's fallback or audit): one warp per block spreads them over
+    // every SM instead of filling a few blocks.
+    const int block = gathered(io) ? 32 : BLOCK;
     int per_sm = 1;
-    const size_t want = (n + BLOCK - 1) / BLOCK;
+    const size_t want = (n + block - 1) / block;
     if (smem) {
         cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
         if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, block, tab_bytes);
     } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, kMathBytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, block, kMathBytes);
     }
     if (per_sm < 1) per_sm = 1;
     size_t grid = (size_t)sm_count() * per_sm;
     if (want < grid) grid = want ? want : 1;
-    if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    else kglobal<<<(unsigned)grid, BLOCK, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
+    if (smem) ksmem<<<(unsigned)grid, block, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, block, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace

@@ -257,6 +257,71 @@ def generate_mechanism(config: str = "k53", seed: int = 0) -> Mechanism:
     return mech
 
 
+def generate_reactor_mechanism(config: str = "k53", seed: int = 0) -> Mechanism:
+    """A well-posed variant of the named mechanism shape for constant-pressure reactors.
+
+    The rates workload's kinetics (A up to 1e16 cm-mol-s with b up to 3, enthalpies of formation spread
+    over +-5e4 K so that equilibrium constants reach e^+-70, random molar masses without element balance)
+    drive a constant-pressure reactor (plot.rs:32-118 formulation) to runaway within picoseconds: reverse
+    rates of 1e20 mol/m^3/s, volumes growing or collapsing without bound; no integrator, the reference's
+    included, reaches 1 ms. This variant keeps the species (heat capacities, entropies, transport), the
+    reaction counts per model and the reacting species of every reaction, and changes:
+      - products are added or removed so that each reaction conserves moles;
+      - every species gets the bulk species' molar mass (the volume then follows n R T / P);
+      - enthalpies of formation are scaled by 0.1, and species 0 (fuel) and 1 (oxidiser) get 1.5e4 K
+        (h/R) more, so that consuming them releases heat;
+      - A log-uniform on [1e11, 1e13] cm-mol-s, b = 0, activation energy U[30, 45] kcal/mol plus the
+        reaction enthalpy when that is positive (both directions keep a barrier; falloff k0: A times
+        log-uniform [1e3, 1e5]).
+    Heat release then accelerates the reactions: an induction time, then ignition.
+    """
+    m = generate_mechanism(config, seed)
+    K, Rn = m.K, m.R
+    s = _Stream(seed, 2)
+    m.molar_mass = np.full(K, m.molar_mass[K - 1])
+
+    def H_R(k, T):  # h/R of species k at T
+        a = m.nasa7[k, 0 if T <= m.nasa7_split[k] else 1]
+        return a[0] * T + a[1] * T**2 / 2 + a[2] * T**3 / 3 + a[3] * T**4 / 4 + a[4] * T**5 / 5 + a[5]
+
+    for k in range(K):
+        h298 = H_R(k, 298.15)
+        target = 0.1 * h298 + (1.5e4 if k in (0, 1) else 0.0)
+        m.nasa7[k, :, 5] += target - h298
+    ea_K_per_kcal = 1000.0 * J_PER_CAL / R
+    for r in range(Rn):
+        lhs, rhs = m.reactants[r].astype(int), m.products[r].astype(int)
+        forced = r if r < K - 1 else None
+        while rhs.sum() < lhs.sum():
+            k = s.int(K - 1)
+            if k != forced:
+                rhs[k] += 1
+        while rhs.sum() > lhs.sum():
+            nz = [k for k in range(K) if rhs[k] > 0]
+            rhs[nz[s.int(len(nz))]] -= 1
+        if (rhs == lhs).all() or (forced is not None and rhs[forced] == lhs[forced]):
+            # keep the reaction changing its forced species: swap one product for another species
+            nz = [k for k in range(K) if rhs[k] > 0]
+            rhs[nz[0]] -= 1
+            k = s.int(K - 1)
+            while k == forced or k == nz[0]:
+                k = s.int(K - 1)
+            rhs[k] += 1
+        m.reactants[r], m.products[r] = lhs.astype(np.uint8), rhs.astype(np.uint8)
+        dH = sum(rhs[k] * H_R(k, 1200.0) for k in range(K)) - sum(lhs[k] * H_R(k, 1200.0) for k in range(K))
+        n_react = int(lhs.sum())
+        A_cgs = s.log_range(1e11, 1e13)
+        Ea = s.range(30.0, 45.0) * ea_K_per_kcal + max(0.0, dH)
+        order_ = n_react + (1 if m.model[r] == THREE_BODY else 0)
+        m.rate[r] = (A_cgs * 1e-6 ** (order_ - 1), 0.0, Ea)
+        if m.model[r] == TROE:
+            A0_cgs = A_cgs * s.log_range(1e3, 1e5)
+            m.k0[r] = (A0_cgs * 1e-6 ** n_react, 0.0, Ea)
+    m.meta = {"config": config, "seed": seed, "variant": "reactor"}
+    assert m.active() == K - 1
+    return m
+
+
 def transport_scales(mech: Mechanism, T0: float = 1000.0, equivalence_ratio: float = 1.0):
     """(T0, viscosity0, conductivity0) of cantera.rs:60-76: fuel = species 0, oxidiser = species 1,
     diluent = last species, 1 atm, unit diffusivity."""

@@ -242,6 +242,51 @@ int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features, 
 const char* cb_last_error(void);
 const char* cb_version(void);
 
+/* ---- Batched constant-pressure reactors (variable-order BDF) ----------------------------------------
+ * Replaces the reactor loop of plot.rs:32-118 with the cvode crate's role (cvode/lib.rs:17-47: BDF,
+ * dense Newton): state u = [T, V, n_0 .. n_{A-1}] at fixed P/R, du/dt = the outputs of cb_rates_f64 for
+ * that state (reaction.rs:356-391). Needs every non-bulk species active (A = K - 1) and K <= 65.
+ * Every reactor is integrated from t = 0 to t_end with its own step size and order (1-5) against
+ * atol + rtol |u_i| for every component; its ignition delay is the time of the largest dT/dt (the
+ * vertex of a parabola through the samples around it). The host side is synchronous. */
+typedef struct cb_reactors cb_reactors;
+typedef struct cb_bdf_options {
+    double rtol, atol;
+    double t_end;               /* s */
+    int32_t max_steps;          /* per reactor; reactors that need more end with status 4 */
+    int32_t slice_steps;        /* steps per reactor per kernel launch (0: 256) */
+    int32_t warps_per_block;    /* reactors in flight per block (0: autotuned) */
+    int32_t tables_in_shared;   /* 1: mechanism tables in shared memory, 0: through L1, -1: autotuned */
+} cb_bdf_options;
+typedef struct cb_reactor_stats {
+    uint64_t steps, rhs_evals, jacobians, factorizations, newton_failures, error_failures;
+    uint64_t finished, failed;
+    double ms;                  /* device time of the integration */
+    int32_t warps_per_block, tables_in_shared, graph_replays, slices;
+} cb_reactor_stats;
+typedef struct cb_reactor_tuning {
+    int32_t warps_per_block, tables_in_shared, n_candidates, calib_reactors;
+    struct { int32_t warps_per_block, tables_in_shared; double ms; } candidates[16];
+} cb_reactor_tuning;
+int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* options, cb_reactors** out);
+int cb_reactors_destroy(cb_reactors* batch);
+/* Initial states (host arrays): pressure_R [n], T [n], V [n], amounts [A][n] (active species). */
+int cb_reactors_set_state(cb_reactors* batch, const double* pressure_R, const double* T, const double* V,
+                          const double* amounts);
+/* Times the launch shapes that fit (reactors per block, table placement) on copies of the first
+ * calib_reactors reactors (0: 4096) and keeps the fastest; the state is left as it was. */
+int cb_reactors_autotune(cb_reactors* batch, int32_t calib_reactors, cb_reactor_tuning* result);
+/* Integrates every reactor to t_end (autotuning first when the shape is not set). */
+int cb_reactors_integrate(cb_reactors* batch, cb_reactor_stats* stats);
+/* Per reactor (host arrays, any may be NULL): ignition delay [n] (s), final state [A+2][n],
+ * status [n] (2 done, 3 step size underflow, 4 step limit, 1 unfinished), accepted steps [n]. */
+int cb_reactors_results(cb_reactors* batch, double* ignition_delay, double* state, int32_t* status,
+                        int32_t* steps);
+/* The integrator's du/dt and Jacobian at m given states (host): pressure_R [m], states [m][A+2] ->
+ * f [m][A+2], J [m][A+2][A+2] (row i: d f_i / d u_j). Synchronous. */
+int cb_reactors_eval(cb_reactors* batch, int32_t m, const double* pressure_R, const double* states, double* f,
+                     double* J);
+
 #ifdef __cplusplus
 }
 #endif

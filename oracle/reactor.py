@@ -1,0 +1,48 @@
+"""CPU reference for the batched reactors (TEST INFRASTRUCTURE ONLY: the checker of the GPU integrator;
+the product library never uses it).
+
+One reactor at a time with scipy's BDF (scipy.integrate.solve_ivp, method "BDF", finite-difference
+Jacobian): the role of the reference's cvode crate (cvode/lib.rs:17-47: CVODE BDF, dense solver,
+difference-quotient Jacobian) on the FP64 rates restatement of the oracle (reaction.rs:356-391). The
+ignition delay is the time of the largest dT/dt over the accepted steps, refined by the vertex of the
+parabola through the samples around it (the GPU integrator's definition).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def rhs(o, pressure_R, y):
+    """du/dt for u = [T, V, n_0 .. n_{A-1}] (rows) or a batch of states (columns)."""
+    y = np.asarray(y, dtype=np.float64)
+    Y = y.reshape(len(y), -1)
+    n = Y.shape[1]
+    ins = [np.full(n, pressure_R), np.full(n, 1.0 / pressure_R)] + [np.ascontiguousarray(r) for r in Y]
+    out = o.rates(ins)
+    return out if y.ndim == 2 else out[:, 0]
+
+
+def ignition_time(t, g):
+    """Vertex of the parabola through the largest sample of g and its neighbours (or the sample)."""
+    i = int(np.argmax(g))
+    if 0 < i < len(t) - 1:
+        ta, tb, tc = t[i - 1], t[i], t[i + 1]
+        ga, gb, gc = g[i - 1], g[i], g[i + 1]
+        d1, d2 = tb - ta, tb - tc
+        den = d1 * (gb - gc) - d2 * (gb - ga)
+        if den != 0.0:
+            v = tb - 0.5 * (d1 * d1 * (gb - gc) - d2 * d2 * (gb - ga)) / den
+            if ta < v < tc:
+                return float(v)
+    return float(t[i])
+
+
+def integrate(o, pressure_R, y0, t_end, rtol=1e-9, atol=1e-14):
+    """(ignition delay, final state, number of steps) of one reactor."""
+    from scipy.integrate import solve_ivp
+    sol = solve_ivp(lambda t, y: rhs(o, pressure_R, y), (0.0, t_end), np.asarray(y0, dtype=np.float64),
+                    method="BDF", rtol=rtol, atol=atol)
+    if sol.status != 0:
+        raise RuntimeError(sol.message)
+    g = rhs(o, pressure_R, sol.y)[0]
+    return ignition_time(sol.t, g), sol.y[:, -1], len(sol.t) - 1

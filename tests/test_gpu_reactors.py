@@ -1,0 +1,101 @@
+"""The batched BDF reactors through the C ABI: the integrator's warp-cooperative du/dt against the FP64
+oracle, its Jacobian against finite differences of the oracle, ignition delays against the CPU
+reference integration (scipy's BDF on the oracle, oracle/reactor.py), the autotuner and the graph
+replays. Stated error bars: du/dt within 1e-12 of the oracle (condition-scaled); ignition delays at
+rtol 1e-6 within 0.1 % of the reference integration at rtol 1e-9 (test reactors) and, over 2048
+reactors against the same integrator at rtol 1e-10, within 0.1 % at the median and 0.5 % at most (the
+difference is the rtol 1e-6 integration error); final temperatures within 1e-5.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import util
+from oracle import reactor
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(config, n, **kw):
+    import combustion_gb300 as cb
+    from combustion_gb300 import reactors as RX
+    from combustion_gb300 import synthetic
+    m = synthetic.generate_reactor_mechanism(config)
+    mech = cb.Mechanism(m)
+    R = RX.Reactors(mech, n, **kw)
+    pR, T, V, am = RX.initial_states(m.K, n, seed=4)
+    R.set_state(pR, T, V, am)
+    return m, mech, R, (pR, T, V, am)
+
+
+@pytest.mark.parametrize("config", ["k10", "k53"])
+def test_rhs_and_jacobian_against_oracle(config):
+    from combustion_gb300 import synthetic
+    m, mech, R, _ = _setup(config, 4)
+    o = oracle.Oracle(m)
+    cells = synthetic.generate_cells(m.K, 16, config if config != "k10" else "k10", seed=5)
+    pR = cells.pressure_R
+    Y = np.vstack([cells.temperature, cells.volume, cells.amounts]).T.copy()
+    f, J = R.eval(pR, Y)
+    ins = o.rates_inputs(cells)
+    ref, sc = o.rates(ins, scale=True)
+    err = util.cond_err(f.T, ref, sc)
+    print(config, "du/dt max cond err %.2e" % err.max())
+    assert err.max() <= util.PLAIN_TOL * 10
+    # Jacobian against central differences of the oracle
+    worst = 0.0
+    for s in range(4):
+        y = Y[s]
+        Jfd = np.zeros_like(J[s])
+        for j in range(len(y)):
+            h = 1e-6 * max(abs(y[j]), 1e-3 * (abs(y[0]) if j == 0 else max(1e-30, abs(y[2:]).max())))
+            yp, ym = y.copy(), y.copy()
+            yp[j] += h
+            ym[j] -= h
+            Jfd[:, j] = (reactor.rhs(o, pR[s], yp) - reactor.rhs(o, pR[s], ym)) / (yp[j] - ym[j])
+        rel = np.linalg.norm(J[s] - Jfd) / np.linalg.norm(Jfd)
+        worst = max(worst, rel)
+        # the species block without falloff broadening terms is exact up to differencing error
+    print(config, "Jacobian rel err (Frobenius) %.2e" % worst)
+    assert worst < 2e-2
+
+
+@pytest.mark.parametrize("config,n", [("k10", 8), ("k53", 3)])
+def test_ignition_delays_against_cpu_bdf(config, n):
+    m, mech, R, (pR, T, V, am) = _setup(config, n, rtol=1e-6, atol=1e-12, t_end=1e-3)
+    st = R.integrate()
+    res = R.results()
+    print(config, st)
+    assert st["finished"] == n and st["failed"] == 0
+    o = oracle.Oracle(m)
+    for i in range(n):
+        y0 = np.concatenate([[T[i], V[i]], am[:, i]])
+        tau, yf, steps = reactor.integrate(o, pR[i], y0, 1e-3, rtol=1e-9, atol=1e-15)
+        g = res["ignition_delay"][i]
+        print(f"  reactor {i}: GPU tau {g:.6e} ({res['steps'][i]} steps), CPU tau {tau:.6e} ({steps} steps), "
+              f"T_end {res['state'][0, i]:.4f} / {yf[0]:.4f}")
+        assert abs(g - tau) <= 1e-3 * tau
+        assert abs(res["state"][0, i] - yf[0]) <= 1e-5 * yf[0]
+
+
+def test_autotune_graph_replays_and_tolerance_convergence():
+    n = 2048
+    m, mech, R, state = _setup("k10", n, rtol=1e-6, atol=1e-12, t_end=1e-3, slice_steps=64)
+    tune = R.autotune(512)
+    print(tune)
+    assert tune["candidates"] and tune["warps_per_block"] >= 1
+    st = R.integrate()
+    print(st)
+    assert st["finished"] == n and st["graph_replays"] >= 2  # 64-step slices: several replays
+    res = R.results()
+    import combustion_gb300 as cb
+    from combustion_gb300 import reactors as RX
+    tight = RX.Reactors(mech, n, rtol=1e-10, atol=1e-16, t_end=1e-3, warps_per_block=tune["warps_per_block"],
+                        tables_in_shared=tune["tables_in_shared"])
+    tight.set_state(*state)
+    st2 = tight.integrate()
+    ref = tight.results()
+    assert st2["finished"] == n
+    rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
+    print("ignition delay vs rtol 1e-10: max rel diff %.2e, median %.2e" % (rel.max(), np.median(rel)))
+    assert np.median(rel) <= 1e-3 and rel.max() <= 5e-3
