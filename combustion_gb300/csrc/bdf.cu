@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -886,6 +887,17 @@ cudaError_t launch_slice(cb_reactors* s, int warps, int tables, int grid, cudaSt
 
 bool shape_fits(cb_reactors* s, int warps, int tables) { return (int)smem_bytes(s, warps, tables) <= max_smem(); }
 
+// Scratch of cb_reactors_eval_noalloc, in the module's static device memory instead of cudaMalloc:
+// states, pressures, du/dt and Jacobians of one call, at most kEvalScratchDoubles doubles (4 MiB; 167
+// states at 53 species). Its address is resolved once per device (cudaGetSymbolAddress) by the first
+// call on that device. Every element a call reads back is written by that call's kernel, so nothing in
+// it has to start at zero; two calls in flight at once on one device share it and race.
+constexpr size_t kEvalScratchDoubles = (size_t)1 << 19;
+constexpr int kMaxDevices = 64;
+static __device__ __align__(256) double g_eval_scratch[kEvalScratchDoubles];
+std::mutex g_eval_scratch_mu;
+double* g_eval_scratch_addr[kMaxDevices] = {};
+
 }  // namespace
 
 extern "C" {
@@ -1227,6 +1239,58 @@ int cb_reactors_eval(cb_reactors* s, int32_t m, const double* pressure_R, const 
     cudaMemcpy(&st, s->counters + 2, sizeof st, cudaMemcpyDeviceToHost);
     if (st) return cleanup(cbi::fail(CB_ERR_DEVICE, "table staging wait ran out"));
     return cleanup(CB_OK);
+}
+
+// No-allocation variant of cb_reactors_eval (same arguments and results): for callers that evaluate
+// du/dt and Jacobians inside a time-critical loop (an implicit solver's Newton iterations on the host,
+// a controller) and must not allocate per call: cudaMalloc and cudaFree cost tens of microseconds,
+// cudaFree synchronises the whole device (stalling, e.g., a reactor integration running on another
+// stream), and under a caching allocator that reserves the GPU's memory cudaMalloc can fail outright.
+int cb_reactors_eval_noalloc(cb_reactors* s, int32_t m, const double* pressure_R, const double* states, double* f,
+                             double* J) {
+    if (!s || !pressure_R || !states || !f || !J || m <= 0) return cbi::fail(CB_ERR_INVALID, "bad argument");
+    const int N = s->N;
+    const size_t per_state = (size_t)N * N + 2 * (size_t)N + 1;
+    const size_t max_states = kEvalScratchDoubles / per_state;
+    if ((size_t)m > max_states)
+        return cbi::fail(CB_ERR_INVALID, "cb_reactors_eval_noalloc: at most " + std::to_string(max_states) +
+                                             " states per call for this mechanism (fixed 4 MiB device scratch)");
+    if (s->device < 0 || s->device >= kMaxDevices) return cbi::fail(CB_ERR_UNSUPPORTED, "device index above 63");
+    BDF_CUDA(cudaSetDevice(s->device));
+    double* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_eval_scratch_mu);
+        if (!g_eval_scratch_addr[s->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_eval_scratch);
+            if (e != cudaSuccess) return cbi::cuda_fail(e, "cudaGetSymbolAddress(evaluation scratch)");
+            g_eval_scratch_addr[s->device] = static_cast<double*>(p);
+        }
+        base = g_eval_scratch_addr[s->device];
+    }
+    double* dy = base;
+    double* dp = dy + (size_t)m * N;
+    double* df = dp + m;
+    double* dJ = df + (size_t)m * N;
+    cudaStream_t st = s->stream;
+    BDF_CUDA(cudaMemcpyAsync(dy, states, (size_t)m * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    BDF_CUDA(cudaMemcpyAsync(dp, pressure_R, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st));
+    Params p = params(s, shape_fits(s, 1, 1) ? 1 : 0);
+    p.pR = dp;
+    p.eval_y = dy;
+    p.eval_f = df;
+    p.eval_J = dJ;
+    const size_t smem = smem_bytes(s, 1, p.smem_tables);
+    BDF_CUDA(cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    eval_kernel<<<std::min(m, sm_count()), 32, smem, st>>>(p, m);
+    BDF_CUDA(cudaGetLastError());
+    BDF_CUDA(cudaMemcpyAsync(f, df, (size_t)m * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BDF_CUDA(cudaMemcpyAsync(J, dJ, (size_t)m * N * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BDF_CUDA(cudaStreamSynchronize(st));
+    int status = 0;
+    BDF_CUDA(cudaMemcpy(&status, s->counters + 2, sizeof status, cudaMemcpyDeviceToHost));
+    if (status) return cbi::fail(CB_ERR_DEVICE, "table staging wait ran out");
+    return CB_OK;
 }
 
 }  // extern "C"
