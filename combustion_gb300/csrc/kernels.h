@@ -5,9 +5,10 @@
 
 namespace cbg {
 
-// Threads per block. The rates tables (94 KB at K = 53) fit twice per SM: 2 x 128 threads give two warps
-// per SM sub-partition. The transport tables (135 KB) fit once, so that kernel runs 256-thread blocks.
-constexpr int kBlock = 128;
+// Threads per block. The rates tables (94 KB at K = 53) fit twice per SM: 2 x 256 threads give four
+// warps per SM sub-partition to hide the latency of the thread-local arrays. The transport tables
+// (135 KB) fit once, so that kernel runs 256-thread blocks as well.
+constexpr int kBlock = 256;
 constexpr int kTransportBlock = 256;
 
 // One pointer per input / output array (struct of arrays), passed by value as a kernel parameter.
