@@ -487,7 +487,7 @@ def main():
     ap.add_argument("--no-reactors", action="store_true")
     ap.add_argument("--reactors", type=int, default=16384)
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
-    ap.add_argument("--sur-steps", type=int, default=2000)
+    ap.add_argument("--sur-steps", type=int, default=6000)
     ap.add_argument("--sur-batch", type=int, default=65536)
     ap.add_argument("--sur-audit", type=int, default=1024)
     args = ap.parse_args()

@@ -242,6 +242,18 @@ int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features, 
 const char* cb_last_error(void);
 const char* cb_version(void);
 
+/* ---- Cantera-YAML mechanisms ------------------------------------------------------------------------
+ * Replaces the reference's loader and builder front end (yaml.rs:54-171 + lib.rs:20-140): reads a
+ * Cantera YAML mechanism (units cm/s/mol, activation energy K or cal/mol; elementary, irreversible,
+ * three-body, falloff with Troe / SRI / Lindemann, single-rate pressure-dependent-Arrhenius) into SI
+ * arrays with the species some reaction changes first. cb_yaml_desc fills a cb_mech_desc whose pointers
+ * stay valid until cb_yaml_free; cb_yaml_species_name returns the k-th species' name in that order. */
+typedef struct cb_yaml_mech cb_yaml_mech;
+int cb_yaml_load(const char* text, size_t length, cb_yaml_mech** out);
+int cb_yaml_desc(const cb_yaml_mech* mech, cb_mech_desc* desc);
+const char* cb_yaml_species_name(const cb_yaml_mech* mech, int32_t k);
+int cb_yaml_free(cb_yaml_mech* mech);
+
 /* ---- Batched constant-pressure reactors (variable-order BDF) ----------------------------------------
  * Replaces the reactor loop of plot.rs:32-118 with the cvode crate's role (cvode/lib.rs:17-47: BDF,
  * dense Newton): state u = [T, V, n_0 .. n_{A-1}] at fixed P/R, du/dt = the outputs of cb_rates_f64 for
