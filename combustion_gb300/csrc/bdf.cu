@@ -223,7 +223,8 @@ __device__ RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double
         case 1: cR = reaction_eval<1, PARTS>(m.tb, x, c, &pp); break;
         case 2: cR = reaction_eval<2, PARTS>(m.tb, x, c, &pp); break;
         case 3: cR = reaction_eval<3, PARTS>(m.tb, x, c, &pp); break;
-        default: cR = reaction_eval<4, PARTS>(m.tb, x, c, &pp); break;
+        case 4: cR = reaction_eval<4, PARTS>(m.tb, x, c, &pp); break;
+        default: cR = reaction_eval<5, PARTS>(m.tb, x, c, &pp); break;
         }
         w.cR[r] = cR;
         if (PARTS) {

@@ -105,12 +105,13 @@ __device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, siz
     cell_setup<KMAX>(tb, pressure_R, T, V, io.in + 4, i, c);
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
-    // species_rates (reaction.rs:312-327), one loop per reaction model (SRI is rejected at creation)
+    // species_rates (reaction.rs:312-327), one loop per reaction model
     accumulate_group<KMAX, 0>(tb, c, wdot);
     accumulate_group<KMAX, 1>(tb, c, wdot);
     accumulate_group<KMAX, 2>(tb, c, wdot);
     accumulate_group<KMAX, 3>(tb, c, wdot);
     accumulate_group<KMAX, 4>(tb, c, wdot);
+    accumulate_group<KMAX, 5>(tb, c, wdot);
     // Energy and volume (reaction.rs:375-384).
     double E = 0.0;
     for (int k = 0; k < A; k++) {
@@ -143,6 +144,7 @@ __device__ void reaction_rates_cell(const RatesTables& tb, const ReactionRatesAr
     rates_of_group<KMAX, 2>(tb, c, io, i);
     rates_of_group<KMAX, 3>(tb, c, io, i);
     rates_of_group<KMAX, 4>(tb, c, io, i);
+    rates_of_group<KMAX, 5>(tb, c, io, i);
 }
 
 template <int KMAX, bool SMEM>

@@ -112,6 +112,18 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
         const double Ck0 = flt_to_dbl(c.Mf[x.eff_row]) * arrhenius_f(f.k0, c.lnTf, c.rcpTf);
         const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
         kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
+    } else if constexpr (MODEL == 5) {  // SRI (reaction.rs:194-203, commented formula), blending in FP32
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+        const double Pr = (flt_to_dbl(c.Mf[x.eff_row]) * k0) * rcp64(ki + kF32MinPos);
+        const float lP = log_dbl_f32(Pr + kF32MinPos);
+        float base = expf(f.smrC * c.Tf);
+        if (f.sri_flags & kSriA) base = fmaf(f.sA, expf(f.smB * c.rcpTf), base);
+        float F = expf(__fdividef(logf(base), fmaf(lP, lP, 1.f)));
+        if (f.sri_flags & kSriD) F *= f.sD;
+        if (f.sri_flags & kSriE) F *= expf(f.sE * c.lnTf);
+        kf = (flt_to_dbl(F) * ki) * (Pr * rcp64(Pr + 1.0));
     } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
         kf = arrhenius_f(x.k, c.lnTf, c.rcpTf) * flt_to_dbl(c.Mf[x.eff_row]);
     } else {
@@ -210,6 +222,7 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
     accumulate_group_m<KMAX, 2>(tb, c, wdot);
     accumulate_group_m<KMAX, 3>(tb, c, wdot);
     accumulate_group_m<KMAX, 4>(tb, c, wdot);
+    accumulate_group_m<KMAX, 5>(tb, c, wdot);
     // Energy (reaction.rs:375-384): FP32 polynomials, FP64 sums over the FP64 species rates.
     const float Tf = c.Tf, rcpTf = c.rcpTf;
     double E = 0.0, Cp = 0.0, dtE = 0.0;

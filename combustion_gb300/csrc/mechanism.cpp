@@ -352,7 +352,6 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
         x.model = m.model[r];
         x.eff_row = -1; x.falloff = -1;
         if (x.model < CB_ELEMENTARY || x.model > CB_SRI) { err = "bad reaction model"; return CB_ERR_INVALID; }
-        if (x.model == CB_SRI) { err = "SRI falloff is unimplemented in the reference (reaction.rs:194-203)"; return CB_ERR_UNSUPPORTED; }
         const uint8_t* re = &m.reactants[(size_t)r * K];
         const uint8_t* pr = &m.products[(size_t)r * K];
         int sum_r = 0, sum_p = 0;
@@ -384,7 +383,7 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
         }
         const double* rc = &m.rate[r * 3];
         if (!(rc[0] > 0.)) { err = "pre-exponential factors must be positive"; return CB_ERR_MECHANISM; }
-        if (x.model == CB_THREE_BODY || x.model == CB_LINDEMANN || x.model == CB_TROE) {
+        if (x.model == CB_THREE_BODY || x.model == CB_LINDEMANN || x.model == CB_TROE || x.model == CB_SRI) {
             x.eff_row = (int32_t)(eff_rows.size() / K);
             const double* e = &m.eff[(size_t)r * K];
             for (int k = 0; k < K; k++) {
@@ -429,6 +428,27 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
             std::memset(&f, 0, sizeof f);
             f.k0 = make_arrhenius(m.k0[r * 3], m.k0[r * 3 + 1], m.k0[r * 3 + 2]);
             x.k = make_arrhenius(rc[0], rc[1], rc[2]);
+            x.falloff = (int32_t)falloff.size();
+            falloff.push_back(f);
+        } else if (x.model == CB_SRI) {
+            // The reference leaves SRI unimplemented (reaction.rs:194-203); this follows its commented
+            // formula: Pr = M k0 / (k_inf + f32::MIN_POSITIVE) with unscaled k0 and k_inf,
+            // F = D (A exp(-B/T) + exp(-T/C))^(1/(1 + ln(Pr + f32::MIN_POSITIVE)^2)) T^E.
+            if (!d->k0 || !d->sri) { err = "SRI reactions need k0 and sri arrays"; return CB_ERR_INVALID; }
+            const double* s = &m.sri[r * 5];
+            if (!(s[2] != 0.) || !(s[3] > 0.)) { err = "SRI needs C != 0 and D > 0"; return CB_ERR_MECHANISM; }
+            Falloff f;
+            std::memset(&f, 0, sizeof f);
+            f.k0 = make_arrhenius(m.k0[r * 3], m.k0[r * 3 + 1], m.k0[r * 3 + 2]);
+            x.k = make_arrhenius(rc[0], rc[1], rc[2]);
+            f.sA = fold_mul(s[0]);
+            f.smB = fold_mul(-s[1]);
+            f.smrC = fold_mul(-1. / s[2]);
+            f.sD = fold_mul(s[3]);
+            f.sE = fold_mul(s[4]);
+            if (f.sA != 0.) f.sri_flags |= kSriA;
+            if (f.sD != 1.) f.sri_flags |= kSriD;
+            if (f.sE != 0.) f.sri_flags |= kSriE;
             x.falloff = (int32_t)falloff.size();
             falloff.push_back(f);
         } else {
@@ -523,10 +543,15 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
                 f.cmT2 = (float)g.cmT2; f.ln_fcent = (float)g.ln_fcent; f.flags = g.flags;
                 y.falloff = (int32_t)ff.size();
                 ff.push_back(f);
-            } else if (x.model == CB_LINDEMANN) {
+            } else if (x.model == CB_LINDEMANN || x.model == CB_SRI) {
                 y.k = arr_f(rc[0], rc[1], rc[2]);
                 FalloffF f{};
                 f.k0 = arr_f(m.k0[r * 3], m.k0[r * 3 + 1], m.k0[r * 3 + 2]);
+                if (x.model == CB_SRI) {
+                    const Falloff& g = falloff[x.falloff];
+                    f.sA = (float)g.sA; f.smB = (float)g.smB; f.smrC = (float)g.smrC; f.sD = (float)g.sD;
+                    f.sE = (float)g.sE; f.sri_flags = g.sri_flags;
+                }
                 y.falloff = (int32_t)ff.size();
                 ff.push_back(f);
             } else {
@@ -592,6 +617,12 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
             add_work(w, 12, 1, 1, 3);  // C, N, lnPr+C, f1, F, numerator, denominator
         } else if (x.model == CB_LINDEMANN) {
             arrh_work(falloff[x.falloff].k0); arrh_work(x.k); add_work(w, 5, 0, 0, 1);
+        } else if (x.model == CB_SRI) {
+            const Falloff& f = falloff[x.falloff];
+            arrh_work(f.k0); arrh_work(x.k);
+            // Pr, ln(Pr + eps), the base's terms, its log, the power, T^E, F, numerator, denominator
+            add_work(w, 2 + 2 + 3.0 * !!(f.sri_flags & kSriA) + 2 + 3 + 1.0 * !!(f.sri_flags & kSriD) + 2.0 * !!(f.sri_flags & kSriE) + 4,
+                     1 + !!(f.sri_flags & kSriA) + 1 + !!(f.sri_flags & kSriE), 2, 2);
         } else {
             arrh_work(x.k);
             if (x.model == CB_THREE_BODY) add_work(w, 1);

@@ -143,6 +143,22 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
             const double q = div64(ki, (Ck0 + ki) + kF32MinPos);
             parts->dkf_dM = k0 * (q * q);
         }
+    } else if constexpr (MODEL == 5) {  // SRI: the commented formula of reaction.rs:194-203
+        const Falloff& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius(f.k0, t);
+        const double ki = arrhenius(x.k, t);
+        const double Pr = div64(c.M[x.eff_row] * k0, ki + kF32MinPos);
+        const double lP = log64(Pr + kF32MinPos);
+        double base = exp64(f.smrC * t.T);
+        if (f.sri_flags & kSriA) base = fma(f.sA, exp64(f.smB * t.rcpT), base);
+        double F = exp64(log64(base) * rcp64(fma(lP, lP, 1.0)));
+        if (f.sri_flags & kSriD) F = f.sD * F;
+        if (f.sri_flags & kSriE) F *= exp64(f.sE * t.lnT);
+        kf = div64((F * ki) * Pr, Pr + 1.0);
+        if constexpr (PARTS) {  // F held constant, as for Troe
+            const double r1 = rcp64(Pr + 1.0);
+            parts->dkf_dM = ((F * ki) * div64(k0, ki + kF32MinPos)) * (r1 * r1);
+        }
     } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
         const double k = arrhenius(x.k, t);
         kf = k * c.M[x.eff_row];

@@ -34,12 +34,17 @@ enum FalloffFlags : int32_t {
     kFcentConst = 32,  // Fcent has no runtime term: lnFcent = ln_fcent
 };
 
+// SRI blending F = D (A exp(-B/T) + exp(-T/C))^(1/(1 + ln(Pr)^2)) T^E (the reference's commented
+// formula, reaction.rs:194-203): which optional factors are present.
+enum SriFlags : int32_t { kSriA = 1, kSriD = 2, kSriE = 4 };
+
 struct Falloff {
     Arrhenius k0;                       // low-pressure rate constant (Troe: A divided by A_inf)
     double ainf;                        // canonical A_inf multiplying the Troe k_inf
     double c1mA, cA, c3, c1, cmT2;      // canonical (1-A), A, -1/T3, -1/T1, -T2
     double ln_fcent;                    // lnFcent when constant
-    int32_t flags, pad;
+    int32_t flags, sri_flags;
+    double sA, smB, smrC, sD, sE;       // SRI: canonical A, -B, -1/C, D, E
 };
 
 // Reactions are stored grouped by model (RatesHeader::group_end), each group in the mechanism's order;

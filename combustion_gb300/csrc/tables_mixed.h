@@ -23,7 +23,8 @@ struct FalloffF {
     ArrheniusF k0;
     double ainf;                    // A_inf (FP64: k_inf can exceed the FP32 range)
     float c1mA, cA, c3, c1, cmT2, ln_fcent;
-    int32_t flags, pad;
+    int32_t flags, sri_flags;
+    float sA, smB, smrC, sD, sE, pad;  // SRI constants (tables.h)
 };
 
 struct ReactionF {

@@ -59,6 +59,7 @@ typedef struct {
     double troe_1mA, troe_A, troe_c3, troe_c1, troe_mT2; /* canonical Fcent constants */
     int troe_t1, troe_t2; /* T1 < 1e30, T2 finite */
     int fcent_const; double fcent_value;
+    double sri_A, sri_mB, sri_mrC, sri_D, sri_E; /* canonical SRI constants: A, -B, -1/C, D, E */
     int n_eff; int* eff_k; double* eff_c; /* non-unit efficiencies: species and (e-1) (0 => plain C_k) */
     int n_r; int* r_k; int* r_n;          /* reactant species and multiplicities */
     int n_p; int* p_k; int* p_n;          /* product species and multiplicities */
@@ -208,8 +209,7 @@ or_mech* or_mech_new(int K, int R, const double* molar_mass, const double* nasa7
             if (x->n_net == 0) fail(m, "reversible reaction without net change of an active species");
             if (-x->sigma_net < -2 || -x->sigma_net > 1) fail(m, "unsupported net order (reaction.rs:298-303)");
         }
-        if (x->model == SRI) fail(m, "SRI falloff is unimplemented in the reference (reaction.rs:194-203)");
-        if (x->model == THREE_BODY || x->model == LINDEMANN || x->model == TROE) {
+        if (x->model == THREE_BODY || x->model == LINDEMANN || x->model == TROE || x->model == SRI) {
             const double* e = &m->eff[(size_t)r * K];
             x->eff_k = malloc(K * sizeof(int)); x->eff_c = malloc(K * sizeof(double));
             for (int k = 0; k < K; k++) {
@@ -243,6 +243,18 @@ or_mech* or_mech_new(int K, int R, const double* molar_mass, const double* nasa7
         } else if (x->model == LINDEMANN) {
             arrh_build(&x->k0, m->k0[r * 3], m->k0[r * 3 + 1], m->k0[r * 3 + 2]);
             arrh_build(&x->k, rc[0], rc[1], rc[2]);
+        } else if (x->model == SRI) {
+            /* the reference leaves SRI unimplemented; its commented formula (reaction.rs:194-203) uses
+               the unscaled k0 and k_inf and F = D (A exp(-B/T) + exp(-T/C))^(1/(1 + ln(Pr)^2)) T^E */
+            const double* s = &m->sri[r * 5];
+            if (!(s[2] != 0.) || !(s[3] > 0.)) fail(m, "SRI needs C != 0 and D > 0");
+            arrh_build(&x->k0, m->k0[r * 3], m->k0[r * 3 + 1], m->k0[r * 3 + 2]);
+            arrh_build(&x->k, rc[0], rc[1], rc[2]);
+            x->sri_A = canon_mul(s[0]);
+            x->sri_mB = canon_mul(-s[1]);
+            x->sri_mrC = canon_mul(-1. / s[2]);
+            x->sri_D = canon_mul(s[3]);
+            x->sri_E = canon_mul(s[4]);
         } else {
             arrh_build(&x->k, rc[0], rc[1], rc[2]);
         }
@@ -407,6 +419,21 @@ static double reaction_cR(const or_mech* m, const reaction_t* x, cell_t* c, doub
         double f1 = lnPrC / (-0.14 * lnPrC + Nn);
         double Fb = exp(lnFcent / (f1 * f1 + 1.));
         n = (Fb * kinf_e) * Pr;
+        d = Pr + 1.; has_d = 1;
+        break;
+    }
+    case SRI: {
+        double M = efficiency(x, c);
+        double k0 = arrh_eval(&x->k0, t);
+        double kinf = arrh_eval(&x->k, t);
+        double Pr = (M * k0) / (kinf + F32MINPOS);
+        double lP = log(Pr + F32MINPOS);
+        double base = exp(x->sri_mrC * t->T);
+        if (x->sri_A != 0.) base = x->sri_A * exp(x->sri_mB * t->rcpT) + base;
+        double F = exp(log(base) * (1. / (1. + lP * lP)));
+        if (x->sri_D != 1.) F = x->sri_D * F;
+        if (x->sri_E != 0.) F = F * exp(x->sri_E * t->lnT);
+        n = (F * kinf) * Pr;
         d = Pr + 1.; has_d = 1;
         break;
     }

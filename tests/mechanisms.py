@@ -66,3 +66,24 @@ def branch_mechanism():
 
 def cells_for(m, n, seed=7):
     return s.generate_cells(m.K, n, "k10", seed=seed)
+
+
+def sri_mechanism():
+    """The seeded 10-species mechanism with SRI falloff reactions (the reference leaves SRI unimplemented;
+    the library follows its commented formula, reaction.rs:194-203): its two Troe reactions become SRI
+    (one with A = 0, D != 1, E != 0) and one elementary reaction becomes SRI with the typical defaults."""
+    m = copy.deepcopy(s.generate_mechanism("k10"))
+    K = m.K
+    rows = {r: int(m.model[r]) for r in range(m.R)}
+    elem = [r for r, k in rows.items() if k == s.ELEMENTARY]
+    troe = [r for r, k in rows.items() if k == s.TROE]
+    for r, p in zip(troe + [elem[0]], [(0.45, 797.0, 979.0, 1.0, 0.0), (0.0, 0.0, 1500.0, 1.3, 0.2),
+                                       (1.2, 350.0, 2200.0, 0.8, -0.3)]):
+        m.model[r] = s.SRI
+        m.sri[r] = p
+        if not m.k0[r].any():
+            m.k0[r] = (m.rate[r, 0] * 1e3 * 1e-6, m.rate[r, 1] - 0.5, m.rate[r, 2] * 0.8)
+            m.efficiencies[r] = np.linspace(0.7, 3.0, K)
+    m.meta = {"config": "sri"}
+    assert m.active() == K - 1
+    return m

@@ -118,7 +118,7 @@ def rates(mech, P_R, rcpP_R, T, V, n):
     for r in range(Rn):
         model = int(mech.model[r])
         A_, b_, Ea_ = mech.rate[r]
-        if model in (2, 3, 4):
+        if model in (2, 3, 4, 5):
             e = mech.efficiencies[r]
             terms = []
             for k in range(K):
@@ -178,6 +178,22 @@ def rates(mech, P_R, rcpP_R, T, V, n):
             Ck0 = M * arrhenius(A0, b0, Ea0, t)
             ki = arrhenius(A_, b_, Ea_, t)
             nn, d = Ck0 * ki, (Ck0 + ki) + F32MINPOS
+        elif model == 5:  # SRI, the reference's commented formula (reaction.rs:194-203)
+            A0, b0, Ea0 = mech.k0[r]
+            k0 = arrhenius(A0, b0, Ea0, t)
+            ki = arrhenius(A_, b_, Ea_, t)
+            Pr = (M * k0) / (ki + F32MINPOS)
+            lP = np.log(Pr + F32MINPOS)
+            sa, sb, sc, sd, se = mech.sri[r]
+            base = np.exp(canon_mul(-1.0 / sc) * T)
+            if canon_mul(sa) != 0:
+                base = canon_mul(sa) * np.exp(canon_mul(-sb) * t["rcpT"]) + base
+            F = np.exp(np.log(base) * (1.0 / (1.0 + lP * lP)))
+            if canon_mul(sd) != 1:
+                F = canon_mul(sd) * F
+            if canon_mul(se) != 0:
+                F = F * np.exp(canon_mul(se) * t["lnT"])
+            nn, d = (F * ki) * Pr, Pr + 1.0
         else:
             raise NotImplementedError(model)
         re, pr = mech.reactants[r], mech.products[r]

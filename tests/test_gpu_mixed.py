@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import util
-from mechanisms import branch_mechanism, cells_for
+from mechanisms import branch_mechanism, cells_for, sri_mechanism
 
 pytestmark = pytest.mark.gpu
 NTHREADS = os.cpu_count() or 4
@@ -66,9 +66,10 @@ def test_mixed_rates_and_transport(config, n):
     assert _report(f"mixed transport {config} rhoD", tt[2:], tref[2:], tsc[2:]).max() <= MIXED_TOL
 
 
-def test_mixed_branch_mechanism_and_fused_host_path():
+@pytest.mark.parametrize("name", ["branches", "sri"])
+def test_mixed_branch_mechanism_and_fused_host_path(name):
     import torch
-    m = branch_mechanism()
+    m = branch_mechanism() if name == "branches" else sri_mechanism()
     mech, o = _setup(m)
     cells = cells_for(m, 4096)
     rin = o.rates_inputs(cells)
@@ -77,8 +78,8 @@ def test_mixed_branch_mechanism_and_fused_host_path():
     rref, rsc = o.rates(rin, scale=True)
     tin = [(rin[0] * rin[3]) / rin[2], rin[2] / o.T0] + rin[4:]
     tref, tsc = o.transport(tin, scale=True)
-    assert _report("mixed fused rates branches", ro, rref, rsc).max() <= MIXED_TOL
-    assert _report("mixed fused transport branches", to, tref, tsc).max() <= MIXED_TOL
+    assert _report(f"mixed fused rates {name}", ro, rref, rsc).max() <= MIXED_TOL
+    assert _report(f"mixed fused transport {name}", to, tref, tsc).max() <= MIXED_TOL
     d_r = torch.empty((mech.A + 2, cells.n), dtype=torch.float64, device="cuda")
     d_t = torch.empty((mech.K + 2, cells.n), dtype=torch.float64, device="cuda")
     mech.rates_transport(_dev(rin), d_r, d_t, mixed=True)

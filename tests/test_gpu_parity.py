@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import util
-from mechanisms import branch_mechanism, cells_for
+from mechanisms import branch_mechanism, cells_for, sri_mechanism
 
 pytestmark = pytest.mark.gpu
 NTHREADS = os.cpu_count() or 4
@@ -107,6 +107,16 @@ def test_branch_mechanism_parity():
     assert _report("rates branches", x, ref, scale).max() <= util.PLAIN_TOL
     x, ref, scale = _run_transport(mech, o, cells)
     assert _report("transport branches", x, ref, scale).max() <= util.PLAIN_TOL
+
+
+def test_sri_mechanism_parity():
+    # SRI falloff: the reference's commented formula (reaction.rs:194-203), restated by the oracle
+    m = sri_mechanism()
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = cells_for(m, 4096)
+    x, ref, scale = _run_rates(mech, o, cells)
+    assert _report("rates sri", x, ref, scale).max() <= util.PLAIN_TOL
 
 
 @pytest.mark.parametrize("n", [0, 1, 31, 127, 129, 1000])

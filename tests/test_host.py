@@ -62,12 +62,18 @@ def test_rejects_non_prefix_active_species():
     _rejects(m, cb.CB_ERR_MECHANISM)
 
 
-def test_rejects_sri_like_the_reference():
+def test_sri_follows_the_reference_commented_formula():
+    # the reference panics on SRI (unimplemented!, reaction.rs:194-203); the library and the oracle
+    # evaluate its commented formula, and reject parameters it cannot take (C = 0, D <= 0)
     cb = _cb()
-    m = copy.deepcopy(util.mechanism("k10"))
-    r = int(np.flatnonzero(m.model == synthetic.TROE)[0])
-    m.model[r] = synthetic.SRI
-    assert "SRI" in _rejects(m, cb.CB_ERR_UNSUPPORTED)
+    from mechanisms import sri_mechanism
+    m = sri_mechanism()
+    info = cb.validate(m)
+    assert info.n_reactions == m.R
+    bad = copy.deepcopy(m)
+    r = int(np.flatnonzero(bad.model == synthetic.SRI)[0])
+    bad.sri[r, 2] = 0.0
+    assert "SRI" in _rejects(bad, cb.CB_ERR_MECHANISM)
 
 
 def test_rejects_reversible_reaction_without_net_change():

@@ -15,7 +15,7 @@ import numpy_restatement as nr
 import oracle
 import util
 from combustion_gb300 import synthetic
-from mechanisms import branch_mechanism, cells_for
+from mechanisms import branch_mechanism, cells_for, sri_mechanism
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 # Fixtures were written on x86-64 glibc; another libm (e.g. aarch64) may differ by an ulp in exp/log.
@@ -42,10 +42,10 @@ def test_oracle_matches_golden_fixtures(name):
     assert util.cond_err(q, g["reaction_out"], g["reaction_scale"]).max() <= FIXTURE_TOL
 
 
-@pytest.mark.parametrize("name", ["k10", "branches"])
+@pytest.mark.parametrize("name", ["k10", "branches", "sri"])
 def test_oracle_matches_numpy_restatement(name):
-    m = branch_mechanism() if name == "branches" else util.mechanism(name)
-    cells = cells_for(m, 1024) if name == "branches" else synthetic.generate_cells(m.K, 1024, name, offset=777)
+    m = {"branches": branch_mechanism, "sri": sri_mechanism}.get(name, lambda: util.mechanism(name))()
+    cells = synthetic.generate_cells(m.K, 1024, name, offset=777) if name == "k10" else cells_for(m, 1024)
     o = oracle.Oracle(m)
     T0, mu0, l0 = synthetic.transport_scales(m)
     coefs = o.fit(T0)

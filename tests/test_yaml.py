@@ -200,14 +200,13 @@ def test_handwritten_file():
     assert m.active() == 7
 
 
-def test_sri_is_read_and_rejected_like_the_reference():
+def test_sri_is_read():
     import combustion_gb300 as cb
     m = _load(HANDWRITTEN + SRI_REACTION)
     assert m.model[-1] == synthetic.SRI
     assert list(m.sri[-1]) == [0.45, 797.0, 979.0, 1.0, 0.0]
-    with pytest.raises(cb.CombustionError) as e:
-        cb.validate(m)
-    assert e.value.code == cb.CB_ERR_UNSUPPORTED
+    assert m.k0[-1][0] == pytest.approx(4.0e22 * 1e-12, rel=1e-15)
+    assert cb.validate(m).n_reactions == 8
 
 
 @pytest.mark.parametrize("bad,code", [
