@@ -326,8 +326,27 @@ int ensure_inference(cb_surrogate* s, size_t rows) {
     return CB_OK;
 }
 
-// Inference forward over `rows` rows of Xi into Yi (FP32, normalised outputs).
+// Inference forward over `rows` rows of Xi into Yi (FP32, normalised outputs): the fused kernel for the
+// 64 -> 256 x n -> 64 shape, one GEMM per layer otherwise.
 int infer_rows(cb_surrogate* s, int rows, const CUtensorMap& mX, cudaStream_t st) {
+    if (mlp_fused_shape(s->dims, s->L)) {
+        FusedMaps maps;
+        std::memset(&maps, 0, sizeof maps);
+        FusedParams p;
+        std::memset(&p, 0, sizeof p);
+        p.rows = rows;
+        p.L = s->L;
+        for (int l = 0; l <= s->L; l++) p.dims[l] = s->dims[l];
+        for (int l = 0; l < s->L; l++) {
+            maps.w[l] = s->mW[l];
+            p.bias[l] = s->p + s->b_off[l];
+        }
+        p.Y = s->Yi;
+        p.ldY = s->n_out;
+        p.status = s->status;
+        SUR_CUDA(mlp_infer(mX, maps, p, st));
+        return CB_OK;
+    }
     for (int l = 0; l < s->L; l++) {
         GemmParams p = base_params(s);
         p.M = rows;

@@ -15,7 +15,18 @@
 namespace cbg {
 namespace sur {
 
-__device__ __forceinline__ float sigmoidf_(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
+// sigmoid(z) = (1 + tanh(z / 2)) / 2 on the hardware tanh (one SFU operation; its ~2^-11 relative
+// error stays below the BF16 rounding of the activations). Training and inference use the same form.
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
+__device__ __forceinline__ float siluf_(float z) {
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_approx(h), h);
+}
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -65,7 +76,7 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
             for (int j = 0; j < 32; j++) {
                 const float z = v[j] + p.bias[n + j];
                 v[j] = z;
-                a[j] = z * sigmoidf_(z);
+                a[j] = siluf_(z);
             }
             if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
             store_row_bf16(p.out2, p.ld_out2, row, n, a);
@@ -184,8 +195,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             }
             umma::mma_commit(smem_u32(&acc_full));  // every MMA issued above has completed
         }
-    } else {  // epilogue warps
-        ok = umma::mbar_wait(smem_u32(&acc_full), 0);
+    } else {  // epilogue warps (the wait's outcome made warp-uniform: tcgen05.ld needs the whole warp)
+        ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full), 0));
         umma::fence_after_sync();
         if (ok) epilogue<BN, EPI>(p, tmem, warp, lane, m0, n0);
     }
@@ -615,6 +626,226 @@ cudaError_t audit(const AuditArgs& a, size_t cap, cudaStream_t st) {
     size_t grid = (cap + 127) / 128;
     if (grid > 1024) grid = 1024;
     audit_kernel<<<(unsigned)grid, 128, 0, st>>>(a, cap);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Fused inference: the whole network for pairs of 128-row tiles in one persistent kernel. Activations
+// stay in shared memory between layers (written by the epilogue in the 128-byte-swizzled K-major layout
+// the next layer's MMAs read); weights stream through a two-stage ring by TMA; the accumulators of the
+// pair's two tiles live in the two halves of tensor memory, so that the epilogue of one tile overlaps
+// the MMAs of the other. Shape: 64 inputs, hidden width 256, 64 outputs (up to 62 species).
+//   warp 0: TMA producer (input tiles, weight chunks in the MMAs' order)
+//   warp 1: TMEM owner and MMA issuer
+//   warps 2-9: epilogue, two warps per TMEM lane quarter (columns 0-127 and 128-255)
+constexpr int kFusedThreads = 320;
+constexpr int kFusedWidth = 256;
+constexpr uint32_t kActChunk = kBM * 128;              // 16 KB: 128 rows x 64 BF16
+constexpr uint32_t kActBytes = 4 * kActChunk;           // one tile's activations (256 columns)
+constexpr uint32_t kWStage = kFusedWidth * 128;         // 32 KB: 256 weight rows x 64 BF16
+constexpr int kWStages = 2;
+constexpr int kFusedSmem = 2 * (int)kActBytes + kWStages * (int)kWStage + 1024;
+
+__device__ __forceinline__ void store_act_bf16(uint32_t chunk_base, int r, int c, const float* a) {
+    // 32 values of row r, columns [c, c + 32) of a 64-column chunk: four 16-byte pieces, swizzled
+    const uint32_t row = chunk_base + (uint32_t)r * 128u;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int piece = ((c & 63) >> 3) + j;
+        const uint32_t addr = row + (uint32_t)((piece ^ (r & 7)) << 4);
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(pack_bf16(a[8 * j], a[8 * j + 1])),
+                     "r"(pack_bf16(a[8 * j + 2], a[8 * j + 3])), "r"(pack_bf16(a[8 * j + 4], a[8 * j + 5])),
+                     "r"(pack_bf16(a[8 * j + 6], a[8 * j + 7]))
+                     : "memory");
+    }
+}
+
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    mlp_infer_kernel(const __grid_constant__ CUtensorMap tx, const __grid_constant__ FusedMaps maps, const FusedParams p) {
+    extern __shared__ uint8_t dsm[];
+    __shared__ uint64_t w_full[kWStages], w_empty[kWStages], x_full[2], acc_full[2], act_ready[2], act_free[2], fin;
+    __shared__ uint32_t tmem_s;
+    const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
+    const uint32_t act0 = base, wring = base + 2 * kActBytes;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int L = p.L;
+    const int tiles = p.rows / kBM;
+    const int pairs = (tiles + 1) / 2;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kWStages; s++) {
+            umma::mbar_init(smem_u32(&w_full[s]), 1);
+            umma::mbar_init(smem_u32(&w_empty[s]), 1);
+        }
+        for (int t = 0; t < 2; t++) {
+            umma::mbar_init(smem_u32(&x_full[t]), 1);
+            umma::mbar_init(smem_u32(&acc_full[t]), 1);
+            umma::mbar_init(smem_u32(&act_ready[t]), 8);
+            umma::mbar_init(smem_u32(&act_free[t]), 1);
+        }
+        umma::mbar_init(smem_u32(&fin), 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 1) {
+        umma::tmem_alloc(smem_u32(&tmem_s), 512);
+        umma::tmem_relinquish();
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = tmem_s;
+    bool ok = true;
+    // dims of layer l: K = p.dims[l], N = p.dims[l + 1]
+    if (warp == 0) {
+        if (lane == 0) {  // producer
+            int g = 0;    // weight chunks issued so far
+            int pi = 0;   // pairs done by this block
+            for (int pr = blockIdx.x; pr < pairs && ok; pr += gridDim.x, pi++) {
+                for (int t = 0; t < 2 && ok; t++) {
+                    const int tile = 2 * pr + t;
+                    if (tile >= tiles) break;
+                    if (pi > 0 && !umma::mbar_wait(smem_u32(&act_free[t]), (pi - 1) & 1)) { ok = false; break; }
+                    umma::mbar_expect_tx(smem_u32(&x_full[t]), kActChunk);
+                    umma::tma_load_2d(act0 + t * kActBytes, &tx, smem_u32(&x_full[t]), 0, tile * kBM);
+                }
+                for (int l = 0; l < L && ok; l++) {
+                    const int K = p.dims[l], N = p.dims[l + 1];
+                    for (int t = 0; t < 2 && ok; t++) {
+                        if (2 * pr + t >= tiles) break;
+                        for (int kc = 0; kc < K / kBK; kc++, g++) {
+                            const int s = g % kWStages;
+                            if (g >= kWStages && !umma::mbar_wait(smem_u32(&w_empty[s]), ((g / kWStages) & 1) ^ 1)) {
+                                ok = false;
+                                break;
+                            }
+                            umma::mbar_expect_tx(smem_u32(&w_full[s]), (uint32_t)N * 128u);
+                            umma::tma_load_2d(wring + s * kWStage, &maps.w[l], smem_u32(&w_full[s]), kc * kBK, 0);
+                        }
+                    }
+                }
+            }
+            if (!ok)  // let the weight copies already issued land before the block exits
+                for (int i = g > kWStages ? g - kWStages : 0; i < g; i++)
+                    umma::mbar_wait(smem_u32(&w_full[i % kWStages]), (i / kWStages) & 1);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            int g = 0, pi = 0;
+            for (int pr = blockIdx.x; pr < pairs && ok; pr += gridDim.x, pi++) {
+                for (int l = 0; l < L && ok; l++) {
+                    const int K = p.dims[l], N = p.dims[l + 1];
+                    const uint32_t idesc = umma::idesc_bf16_f32(kBM, N);
+                    for (int t = 0; t < 2 && ok; t++) {
+                        if (2 * pr + t >= tiles) break;
+                        const int use = pi * L + l;  // uses of this tile slot's barriers so far
+                        if (l == 0) {
+                            if (!umma::mbar_wait(smem_u32(&x_full[t]), pi & 1)) { ok = false; break; }
+                            // the slot's accumulator was read by the previous pair's last epilogue
+                            if (pi > 0 && !umma::mbar_wait(smem_u32(&act_ready[t]), (use - 1) & 1)) { ok = false; break; }
+                        } else if (!umma::mbar_wait(smem_u32(&act_ready[t]), (use - 1) & 1)) {
+                            ok = false;
+                            break;
+                        }
+                        umma::fence_after_sync();
+                        const uint32_t d = tmem + (uint32_t)(t * 256);
+                        const uint32_t a_base = act0 + t * kActBytes;
+                        for (int kc = 0; kc < K / kBK; kc++, g++) {
+                            const int s = g % kWStages;
+                            if (!umma::mbar_wait(smem_u32(&w_full[s]), (g / kWStages) & 1)) { ok = false; break; }
+                            umma::fence_after_sync();
+                            const uint32_t sa = a_base + kc * kActChunk, sb = wring + s * kWStage;
+#pragma unroll
+                            for (int k = 0; k < kBK / 16; k++)
+                                umma::mma_bf16(d, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k), idesc,
+                                               (kc | k) != 0);
+                            umma::mma_commit(smem_u32(&w_empty[s]));
+                        }
+                        umma::mma_commit(smem_u32(&acc_full[t]));
+                        if (l == L - 1) umma::mma_commit(smem_u32(&act_free[t]));
+                    }
+                }
+            }
+            umma::mma_commit(smem_u32(&fin));  // every MMA issued here has completed before TMEM is freed
+            umma::mbar_wait(smem_u32(&fin), 0);
+        }
+    } else {  // epilogue warps 2..9
+        const int e = warp - 2;
+        const int q = warp & 3;          // TMEM lane quarter
+        const int half = e >> 2;         // column half
+        const int r = q * 32 + lane;     // row within the tile
+        int pi = 0;
+        for (int pr = blockIdx.x; pr < pairs && ok; pr += gridDim.x, pi++) {
+            for (int l = 0; l < L && ok; l++) {
+                const int N = p.dims[l + 1];
+                const int cols = N / 2;  // this warp's columns: [half * cols, half * cols + cols)
+                const float* bias = p.bias[l];
+                for (int t = 0; t < 2 && ok; t++) {
+                    const int tile = 2 * pr + t;
+                    if (tile >= tiles) break;
+                    const int use = pi * L + l;
+                    if (!__all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full[t]), use & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const uint32_t acc = tmem + (uint32_t)(t * 256) + ((uint32_t)(q * 32) << 16);
+                    const uint32_t a_base = act0 + t * kActBytes;
+#pragma unroll 1
+                    for (int c = half * cols; c < half * cols + cols; c += 32) {
+                        float v[32];
+                        umma::tmem_ld32(acc + (uint32_t)c, v);
+                        if (l < L - 1) {
+#pragma unroll
+                            for (int j = 0; j < 32; j++) v[j] = siluf_(v[j] + bias[c + j]);
+                            store_act_bf16(a_base + (uint32_t)(c >> 6) * kActChunk, r, c, v);
+                        } else {
+                            float4* dst = reinterpret_cast<float4*>(p.Y + ((size_t)tile * kBM + r) * p.ldY + c);
+#pragma unroll
+                            for (int j = 0; j < 8; j++)
+                                dst[j] = make_float4(v[4 * j] + bias[c + 4 * j], v[4 * j + 1] + bias[c + 4 * j + 1],
+                                                     v[4 * j + 2] + bias[c + 4 * j + 2], v[4 * j + 3] + bias[c + 4 * j + 3]);
+                        }
+                    }
+                    // activations visible to the tensor core, accumulator reads complete: the MMAs of the
+                    // slot's next layer (or next tile) may start
+                    umma::fence_async_shared();
+                    umma::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) umma::mbar_arrive(smem_u32(&act_ready[t]));
+                }
+            }
+        }
+    }
+    if (!ok) atomicOr(p.status, kStatusGemmTimeout);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        umma::fence_after_sync();
+        umma::tmem_dealloc(tmem, 512);
+    }
+}
+
+bool mlp_fused_shape(const int* dims, int L) {
+    if (L < 2 || L > kMaxLayers || dims[0] != 64 || dims[L] != 64) return false;
+    for (int l = 1; l < L; l++)
+        if (dims[l] != kFusedWidth) return false;
+    return true;
+}
+
+cudaError_t mlp_infer(const CUtensorMap& tx, const FusedMaps& maps, const FusedParams& p, cudaStream_t st) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kFusedSmem);
+        if (e != cudaSuccess) return e;
+    }
+    if (p.rows % kBM || !mlp_fused_shape(p.dims, p.L)) return cudaErrorInvalidValue;
+    const int pairs = (p.rows / kBM + 1) / 2;
+    const int grid = pairs < sms ? pairs : sms;
+    if (grid == 0) return cudaSuccess;
+    mlp_infer_kernel<<<grid, kFusedThreads, kFusedSmem, st>>>(tx, maps, p);
     return cudaGetLastError();
 }
 

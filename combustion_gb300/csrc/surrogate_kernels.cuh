@@ -114,6 +114,21 @@ struct AdamArgs {
     float* p; const float* g; float* m; float* v;
 };
 
+// Fused inference (surrogate_kernels.cu): 64 -> 256 x (L - 1) -> 64, outputs FP32 [rows][ldY].
+struct FusedMaps {
+    CUtensorMap w[kMaxLayers];  // weights of layer l: [dims[l+1]][dims[l]], boxes of 64 columns x dims[l+1] rows
+};
+struct FusedParams {
+    int rows, L;
+    int dims[kMaxLayers + 1];
+    const float* bias[kMaxLayers];
+    float* Y;
+    int ldY;
+    int* status;
+};
+bool mlp_fused_shape(const int* dims, int L);
+cudaError_t mlp_infer(const CUtensorMap& tx, const FusedMaps& maps, const FusedParams& p, cudaStream_t st);
+
 // Launchers (surrogate_kernels.cu). gemm_setup() raises the GEMM's shared-memory limit on the current
 // device; it runs before the first GEMM (and outside any stream capture).
 cudaError_t gemm_setup();
