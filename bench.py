@@ -277,6 +277,80 @@ def run_reactors(args, rank):
     }
 
 
+def run_large(args):
+    """The large-mechanism configuration (K = 250, R = 1,500; opt-in with --large): plain FP64 and mixed
+    rates+transport on 2^20 device-generated cells, the width-512 surrogate (252 -> 512 x 4 -> 252) trained
+    on 2^23 plain-kernel cells and run gated on the same cells. Reactors at K = 250 are not supported
+    (their iteration matrix exceeds shared memory)."""
+    import torch
+    import combustion_gb300 as cb
+    import oracle
+    from combustion_gb300 import surrogate as S
+    from combustion_gb300 import synthetic
+    m = synthetic.generate_mechanism("k250")
+    scales = synthetic.transport_scales(m)
+    mech = cb.Mechanism(m)
+    mech.transport_setup(*scales)
+    n = 1 << 20
+    K, A = mech.K, mech.A
+    cells = S.generate_cells(mech, n, S.distribution("k250", seed=1))
+    r_out = torch.empty((A + 2, n), dtype=torch.float64, device="cuda")
+    t_out = torch.empty((K + 2, n), dtype=torch.float64, device="cuda")
+    m_r, m_t = torch.empty_like(r_out), torch.empty_like(t_out)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    plain_ms = timed(lambda: mech.rates_transport(cells, r_out, t_out), 2)
+    mixed_ms = timed(lambda: mech.rates_transport(cells, m_r, m_t, mixed=True), 2)
+    o = oracle.Oracle(m)
+    o.set_transport(*scales, *mech.transport_coefficients())
+    idx = torch.arange(0, n, n // 256, device="cuda")
+    host = cells.index_select(1, idx).cpu().numpy()
+    ins = [np.ascontiguousarray(r) for r in host]
+    rref, rsc = o.rates(ins, nthreads=os.cpu_count() or 1, scale=True)
+    tin = [(ins[0] * ins[3]) / ins[2], ins[2] / scales[0]] + ins[4:]
+    tref, tsc = o.transport(tin, nthreads=os.cpu_count() or 1, scale=True)
+
+    def cerr(x, ref, sc):
+        return float((np.abs(x.index_select(1, idx).cpu().numpy() - ref) / np.maximum(sc, 1e-300)).max())
+
+    sur = S.Surrogate(mech, width=512, hidden_layers=4, batch=65536, lr=1e-3, lr_final=1e-5, seed=3)
+    t = time.perf_counter()
+    sur.generate(1 << 23, S.distribution("k250", seed=2))
+    gen_s = time.perf_counter() - t
+    t = time.perf_counter()
+    losses = sur.train(args.large_steps)
+    train_s = time.perf_counter() - t
+    s_out = torch.empty_like(t_out)
+    st = sur.transport(cells, s_out, audit_stride=1024, timing=True)
+    sur_ms = timed(lambda: (mech.rates(cells, m_r, mixed=True), sur.transport(cells, s_out, audit_stride=1024)), 2)
+    return {
+        "workload": "K=250 / R=1500 (1200 reversible, 180 three-body, 120 Troe), 2^20 cells, T~U[300,3000] K, "
+                    "P log-uniform [0.1,40] atm, X~Dirichlet(0.3) (device generator)",
+        "plain_f64": {"cells_per_s": n / (plain_ms * 1e-3), "ms": plain_ms,
+                      "max_err": max(cerr(r_out, rref, rsc), cerr(t_out, tref, tsc))},
+        "mixed": {"cells_per_s": n / (mixed_ms * 1e-3), "ms": mixed_ms,
+                  "rates_max_err": cerr(m_r, rref, rsc), "transport_max_err": cerr(m_t, tref, tsc)},
+        "mixed_surrogate": {"cells_per_s": n / (sur_ms * 1e-3), "ms": sur_ms,
+                            "network": "252 -> 512 x 4 -> 252, BF16 tcgen05 (per-layer GEMMs)",
+                            "training": {"cells": 1 << 23, "steps": args.large_steps, "generate_s": gen_s,
+                                         "train_s": train_s, "loss_last": float(np.mean(losses[-20:]))},
+                            "error_network_vs_plain_f64": rel_err_groups(s_out, t_out), "gate": st},
+        "reactors": "not supported at K = 250 (iteration matrix beyond shared memory)",
+        "errors": "condition-scaled against the FP64 oracle on 256 sampled cells",
+    }
+
+
 def run_ours(args):
     world, rank, local = dist_setup("nccl")
     from combustion_gb300 import synthetic
@@ -379,6 +453,7 @@ def run_ours(args):
     reactors_form = None
     if not args.no_reactors and rank == 0:
         reactors_form = run_reactors(args, rank)
+    large_form = run_large(args) if (args.large and rank == 0) else None
 
     # Parity of this run's outputs on a sample of cells against the FP64 oracle.
     parity = None
@@ -467,6 +542,7 @@ def run_ours(args):
                 "mixed_surrogate": surrogate_form,
             },
             "reactors": reactors_form,
+            "large_mechanism": large_form,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -486,6 +562,8 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-reactors", action="store_true")
     ap.add_argument("--reactors", type=int, default=16384)
+    ap.add_argument("--large", action="store_true", help="also run the K = 250 configuration")
+    ap.add_argument("--large-steps", type=int, default=1500)
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
     ap.add_argument("--sur-steps", type=int, default=6000)
     ap.add_argument("--sur-batch", type=int, default=65536)
