@@ -21,10 +21,12 @@ struct cb_mech {
     uint8_t* d_rates_mixed = nullptr;      // tables of the mixed-precision form
     uint8_t* d_transport_mixed = nullptr;
     int* d_status = nullptr;         // kernel status bits
-    // Device staging for CB_HOST_MEMORY calls: two slots, each holding one chunk of inputs and outputs.
+    // Device staging for CB_HOST_MEMORY calls: two slots, each holding one chunk of inputs and outputs;
+    // streams for host->device copies, kernels and device->host copies, and per-slot events.
     double* d_stage = nullptr;
     size_t stage_doubles = 0;
-    cudaStream_t copy_stream[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream[3] = {nullptr, nullptr, nullptr};  // h2d, compute, d2h
+    cudaEvent_t slot_event[2][3] = {};                          // per slot: inputs in, kernels done, outputs out
 };
 
 namespace {
@@ -148,48 +150,67 @@ bool needs_transport(Path p) {
     return p == Path::Transport || p == Path::Fused || p == Path::TransportMixed || p == Path::FusedMixed;
 }
 
-// Host arrays: copy chunks through two device staging slots so that the copies of one chunk overlap
-// the kernel of the other (one cudaMemcpyAsync per array per chunk).
+// Host arrays: chunks through two device staging slots. Copies run on their own streams and kernels on
+// one compute stream (one chunk's kernels at a time: the kernels use persistent grids), so that the
+// copies of neighbouring chunks overlap the kernels: H2D(c+1) and D2H(c-1) run while chunk c computes.
+// One cudaMemcpyAsync per array per chunk.
 int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags) {
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
     const bool uniform = rates_layout(path) && (flags & CB_UNIFORM_PRESSURE);
-    size_t chunk = (size_t)1 << 20;
+    // chunks small enough that the first upload and the last download are short, large enough to fill
+    // the GPU: n / 16 cells, between 2^17 and 2^20
+    size_t chunk = n / 16;
+    if (chunk < ((size_t)1 << 17)) chunk = (size_t)1 << 17;
+    if (chunk > ((size_t)1 << 20)) chunk = (size_t)1 << 20;
     if (chunk > n) chunk = n;
     const size_t per_slot = (size_t)(ni + no) * chunk + 2;
     if (m->stage_doubles < 2 * per_slot) {
-        if (m->d_stage) cudaFree(m->d_stage);
+        if (m->d_stage) {
+            CB_CUDA(cudaDeviceSynchronize());
+            cudaFree(m->d_stage);
+        }
         m->d_stage = nullptr;
         m->stage_doubles = 0;
         CB_CUDA(cudaMalloc(&m->d_stage, 2 * per_slot * sizeof(double)));
         m->stage_doubles = 2 * per_slot;
     }
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < 3; s++)
         if (!m->copy_stream[s]) CB_CUDA(cudaStreamCreateWithFlags(&m->copy_stream[s], cudaStreamNonBlocking));
-    }
+    for (int s = 0; s < 2; s++)
+        for (int e = 0; e < 3; e++)
+            if (!m->slot_event[s][e]) CB_CUDA(cudaEventCreateWithFlags(&m->slot_event[s][e], cudaEventDisableTiming));
+    cudaStream_t h2d = m->copy_stream[0], comp = m->copy_stream[1], d2h = m->copy_stream[2];
     std::vector<const double*> din(ni);
     std::vector<double*> dout(no);
     size_t c = 0;
     for (size_t lo = 0; lo < n; lo += chunk, c++) {
         const size_t len = n - lo < chunk ? n - lo : chunk;
         const int s = (int)(c & 1);
-        cudaStream_t st = m->copy_stream[s];
+        cudaEvent_t* ev = m->slot_event[s];
         double* base = m->d_stage + s * per_slot;
+        if (c >= 2) CB_CUDA(cudaStreamWaitEvent(h2d, ev[1], 0));  // the slot's previous kernels read their inputs
         for (int q = 0; q < ni; q++) {
             double* dst = base + (size_t)q * chunk;
             if (uniform && q < 2) {
-                CB_CUDA(cudaMemcpyAsync(dst, in[q], sizeof(double), cudaMemcpyHostToDevice, st));
+                CB_CUDA(cudaMemcpyAsync(dst, in[q], sizeof(double), cudaMemcpyHostToDevice, h2d));
             } else {
-                CB_CUDA(cudaMemcpyAsync(dst, in[q] + lo, len * sizeof(double), cudaMemcpyHostToDevice, st));
+                CB_CUDA(cudaMemcpyAsync(dst, in[q] + lo, len * sizeof(double), cudaMemcpyHostToDevice, h2d));
             }
             din[q] = dst;
         }
+        CB_CUDA(cudaEventRecord(ev[0], h2d));
         for (int q = 0; q < no; q++) dout[q] = base + (size_t)(ni + q) * chunk;
-        int rc = launch_path(m, path, len, din.data(), dout.data(), flags & ~CB_HOST_MEMORY, st);
+        CB_CUDA(cudaStreamWaitEvent(comp, ev[0], 0));
+        if (c >= 2) CB_CUDA(cudaStreamWaitEvent(comp, ev[2], 0));  // the slot's previous outputs are copied out
+        int rc = launch_path(m, path, len, din.data(), dout.data(), flags & ~CB_HOST_MEMORY, comp);
         if (rc) return rc;
+        CB_CUDA(cudaEventRecord(ev[1], comp));
+        CB_CUDA(cudaStreamWaitEvent(d2h, ev[1], 0));
         for (int q = 0; q < no; q++)
-            CB_CUDA(cudaMemcpyAsync(out[q] + lo, dout[q], len * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CB_CUDA(cudaMemcpyAsync(out[q] + lo, dout[q], len * sizeof(double), cudaMemcpyDeviceToHost, d2h));
+        CB_CUDA(cudaEventRecord(ev[2], d2h));
     }
-    for (int s = 0; s < 2; s++) CB_CUDA(cudaStreamSynchronize(m->copy_stream[s]));
+    CB_CUDA(cudaStreamSynchronize(d2h));
     return check_status(m);
 }
 
@@ -312,9 +333,12 @@ int cb_transport_fit(const cb_mech_desc* desc, double T0, double* cond, double* 
 int cb_mech_destroy(cb_mech* m) {
     if (!m) return CB_OK;
     cudaSetDevice(m->device);
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < 3; s++) {
         if (m->copy_stream[s]) { cudaStreamSynchronize(m->copy_stream[s]); cudaStreamDestroy(m->copy_stream[s]); }
     }
+    for (int s = 0; s < 2; s++)
+        for (int e = 0; e < 3; e++)
+            if (m->slot_event[s][e]) cudaEventDestroy(m->slot_event[s][e]);
     cudaFree(m->d_rates);
     cudaFree(m->d_transport);
     cudaFree(m->d_rates_mixed);
