@@ -182,6 +182,32 @@ __global__ void __launch_bounds__(kBlock) reaction_rates_kernel(const uint8_t* _
 }
 
 // ---------------------------------------------------------------------------------------------------
+// Pieces shared by the thread-per-cell and warp-per-cell transport kernels, so that both evaluate the
+// same expressions: a cell's sum n, T/T0 and amount arrays (transport.rs:179-190), the conductivity of
+// its two mixing sums (transport.rs:141-146) and one species' mixture diffusion (transport.rs:176).
+template <class Args>
+__device__ __forceinline__ const double* const* transport_inputs(const TransportHeader& H, const Args& io,
+                                                                 size_t i, double& N, double& Tn) {
+    if (io.flags & kFromRates) {  // sum n = (P/R V) / T and T/T0 of a rates-layout cell
+        const double pressure_R = (io.flags & kUniformPressure) ? io.in[0][0] : io.in[0][i];
+        const double T = io.in[2][i];
+        N = div64(pressure_R * io.in[3][i], T);
+        Tn = div64(T, H.T0);
+        return io.in + 4;
+    }
+    N = io.in[0][i];
+    Tn = io.in[1][i];
+    return io.in + 2;
+}
+// Products here are rounded on their own (never fused into the next add, as in the reference's own
+// arithmetic), so that the two kernels cannot differ by where the compiler contracts.
+__device__ __forceinline__ double conductivity_of(double Ac, double Bc, double N, double VT) {
+    return __dmul_rn(__dadd_rn(div64(Ac, N), div64(N, Bc)), VT);
+}
+__device__ __forceinline__ double diffusion_of(double MVTN, double VT, double W, double X, double S) {
+    return div64(__dsub_rn(MVTN, __dmul_rn(__dmul_rn(VT, W), X)), S);
+}
+
 template <int KMAX>
 __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i, size_t o) {
     // i: the cell's index in the inputs, o: in the outputs (they differ for gathered cells)
@@ -195,18 +221,7 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
     const double* B2 = reinterpret_cast<const double*>(tab + H.off_B2);
     const int K = H.K;
     double N, Tn;
-    const double* const* amounts;
-    if (io.flags & kFromRates) {  // sum n = (P/R V) / T and T/T0 of a rates-layout cell
-        const double pressure_R = (io.flags & kUniformPressure) ? io.in[0][0] : io.in[0][i];
-        const double T = io.in[2][i];
-        N = div64(pressure_R * io.in[3][i], T);
-        Tn = div64(T, H.T0);
-        amounts = io.in + 4;
-    } else {
-        N = io.in[0][i];
-        Tn = io.in[1][i];
-        amounts = io.in + 2;
-    }
+    const double* const* amounts = transport_inputs(H, io, i, N, Tn);
     const double L1 = log64(Tn), L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
     auto poly = [&](const double* P) { return fma(P[4], L4, fma(P[3], L3, fma(P[2], L2, fma(P[1], L1, P[0])))); };
 
@@ -229,7 +244,7 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         Ac = fma(X[k], c, Ac);
         Bc = fma(X[k], rcp64(c), Bc);
     }
-    io.out[0][o] = (div64(Ac, N) + div64(N, Bc)) * VT;
+    io.out[0][o] = conductivity_of(Ac, Bc, N, VT);
 
     // Viscosity, Wilke mixing (transport.rs:148-158) with the square expanded:
     // sum_j X_j (a + b v_k/v_j)^2 = sum_j a^2 X_j + v_k sum_j 2ab X_j/v_j + v_k^2 sum_j b^2 X_j/v_j^2.
@@ -291,7 +306,7 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         }
         S[k] += sa + sb;
     }
-    for (int k = 0; k < K; k++) io.out[2 + k][o] = div64(MVTN - (VT * W[k]) * X[k], S[k]);
+    for (int k = 0; k < K; k++) io.out[2 + k][o] = diffusion_of(MVTN, VT, W[k], X[k], S[k]);
 }
 
 template <int KMAX, bool SMEM>
@@ -310,6 +325,180 @@ __global__ void __launch_bounds__(kTransportBlock) transport_kernel(const uint8_
     for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
         const size_t i = io.index ? (size_t)(io.index[j] & kIndexMask) : j;
         transport_cell<KMAX>(tab, io, i, (io.flags & kCompactOut) ? j : i);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Warp-per-cell transport for small gathered launches (the surrogate gate's fallback and audit cells):
+// the 32 lanes share one cell's species rows, so a few hundred cells still spread over every SM. Each
+// sum is evaluated in the order transport_cell uses, which makes the two kernels' outputs identical bit
+// for bit:
+//  - per-species terms (polynomials, reciprocals) and the per-row viscosity sums run lane-parallel;
+//  - the chains over species (sum n, mean molar mass, conductivity sums, viscosity) run on one lane each;
+//  - the diffusion pair matrix goes by blocks of 32 rows: lane q walks the pairs of row 32b+q left to
+//    right (its even/odd-column sums, as transport_cell's two chains) and leaves the reciprocals of
+//    each 32-column chunk in a shared tile; lane c then adds that chunk's rows, in row order, to column
+//    sum S[32t+c], which is first seeded with its row's own sum, exactly when transport_cell does.
+constexpr int kWarpCellWarps = 8;  // cells (warps) per block
+// Shared memory ahead of the warps' scratch: the staged blob or the math tables, rounded to 16 bytes.
+__host__ __device__ __forceinline__ size_t warp_table_bytes(bool staged, uint32_t tab_bytes) {
+    return ((staged ? (size_t)tab_bytes : (size_t)kMathBytes) + 15) & ~(size_t)15;
+}
+template <int KMAX>
+constexpr int kWarpScratch = 4 * KMAX + 32 * 33;  // doubles per warp: X, v, Y, Z and a 32 x 33 tile
+
+template <int KMAX>
+__device__ void transport_cell_warp(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i, size_t o,
+                                    double* sh) {
+    static_assert(2 * KMAX <= 32 * 33, "the viscosity terms reuse the tile");
+    const int lane = threadIdx.x & 31;
+    const TransportHeader& H = *reinterpret_cast<const TransportHeader*>(tab + kMathBytes);
+    const double* cond = reinterpret_cast<const double*>(tab + H.off_cond);
+    const double* visc = reinterpret_cast<const double*>(tab + H.off_visc);
+    const double* W = reinterpret_cast<const double*>(tab + H.off_W);
+    const double* diff = reinterpret_cast<const double*>(tab + H.off_diff);
+    const double* A2 = reinterpret_cast<const double*>(tab + H.off_A2);
+    const double* AB = reinterpret_cast<const double*>(tab + H.off_AB);
+    const double* B2 = reinterpret_cast<const double*>(tab + H.off_B2);
+    const int K = H.K;
+    double N, Tn;
+    const double* const* amounts = transport_inputs(H, io, i, N, Tn);
+    const double L1 = log64(Tn), L2 = L1 * L1, L3 = L2 * L1, L4 = L3 * L1;
+    auto poly = [&](const double* P) { return fma(P[4], L4, fma(P[3], L3, fma(P[2], L2, fma(P[1], L1, P[0])))); };
+    double* X = sh;
+    double* v = sh + KMAX;
+    double* Y = sh + 2 * KMAX;
+    double* Z = sh + 3 * KMAX;
+    double* T = sh + 4 * KMAX;
+
+    for (int k = lane; k < K - 1; k += 32) X[k] = amounts[k][i];
+    __syncwarp();
+    if (lane == 0) {
+        double s = 0.0;
+        for (int k = 0; k < K - 1; k++) s += X[k];
+        X[K - 1] = N - s;
+    }
+    __syncwarp();
+    const double VT = sqrt(Tn);
+
+    // Conductivity: species polynomials and reciprocals lane-parallel (in v, Y), then three chains on
+    // lanes 0-2: the mean molar mass and the two mixing sums.
+    for (int k = lane; k < K; k += 32) {
+        const double c = poly(cond + 5 * k);
+        v[k] = c;
+        Y[k] = rcp64(c);
+    }
+    __syncwarp();
+    double acc = 0.0;
+    if (lane < 3) {
+        const double* src = lane == 0 ? W : lane == 1 ? v : Y;
+#pragma unroll 1
+        for (int k = 0; k < K; k++) acc = fma(src[k], X[k], acc);
+    }
+    const double MN = __shfl_sync(0xffffffffu, acc, 0);
+    const double Ac = __shfl_sync(0xffffffffu, acc, 1);
+    const double Bc = __shfl_sync(0xffffffffu, acc, 2);
+    __syncwarp();  // lanes 0-2 are done with v and Y
+    if (lane == 0) io.out[0][o] = conductivity_of(Ac, Bc, N, VT);
+    const double MVTN = MN * VT;
+
+    // Viscosity: one row of the expanded Wilke sums per lane, each over j in order; the products and
+    // reciprocals of the rows go to the tile, the sum over rows to lane 0.
+    for (int k = lane; k < K; k += 32) {
+        v[k] = poly(visc + 5 * k);
+        const double r = rcp64(v[k]);
+        Y[k] = X[k] * r;
+        Z[k] = Y[k] * r;
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int k = lane; k < K; k += 32) {
+        const double* a2 = A2 + (size_t)k * K;
+        const double* ab = AB + (size_t)k * K;
+        const double* b2 = B2 + (size_t)k * K;
+        double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+#pragma unroll 4
+        for (int j = 0; j < K; j++) {
+            s1 = fma(a2[j], X[j], s1);
+            s2 = fma(ab[j], Y[j], s2);
+            s3 = fma(b2[j], Z[j], s3);
+        }
+        const double den = fma(v[k], fma(v[k], s3, s2), s1);
+        T[2 * k] = X[k] * (v[k] * v[k]);
+        T[2 * k + 1] = rcp64(den);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        double mu = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < K; k++) mu = fma(T[2 * k], T[2 * k + 1], mu);
+        io.out[1][o] = VT * mu;
+    }
+    __syncwarp();
+
+    // Mixture-averaged diffusion; S reuses Y.
+    double* S = Y;
+#pragma unroll 1
+    for (int b = 0; 32 * b < K; b++) {
+        const int r = 32 * b + lane;
+        const double* P = diff + 5 * ((size_t)r * (size_t)(r > 0 ? r - 1 : 0) / 2);  // pair (r, 0)
+        const int rows = min(32, K - 32 * b);
+        double sa = 0.0, sb = 0.0;
+#pragma unroll 1
+        for (int t = 0; t <= b; t++) {
+            const int j0 = 32 * t;
+            const int j1 = r < K ? min(j0 + 32, r) : j0;
+            int j = j0;
+            double* Trow = T + 33 * lane;  // this row's reciprocals, column j at Trow[j - j0]
+#pragma unroll 1
+            for (; j + 1 < j1; j += 2) {  // j0 is even: sa takes the even columns, sb the odd ones
+                const double Ra = rcp64(poly(P + 5 * j)), Rb = rcp64(poly(P + 5 * (j + 1)));
+                sa = fma(X[j], Ra, sa);
+                sb = fma(X[j + 1], Rb, sb);
+                Trow[j - j0] = Ra;
+                Trow[j + 1 - j0] = Rb;
+            }
+            if (j < j1) {
+                const double R = rcp64(poly(P + 5 * j));
+                sa = fma(X[j], R, sa);
+                Trow[j - j0] = R;
+            }
+            if (t == b && r < K) S[r] = 0.0 + (sa + sb);
+            __syncwarp();
+            const int jc = j0 + lane;
+            if (jc < K) {
+                double s = S[jc];
+#pragma unroll 1
+                for (int q = t == b ? lane + 1 : 0; q < rows; q++) s = fma(X[32 * b + q], T[33 * q + lane], s);
+                S[jc] = s;
+            }
+            __syncwarp();
+        }
+    }
+    for (int k = lane; k < K; k += 32) io.out[2 + k][o] = diffusion_of(MVTN, VT, W[k], X[k], S[k]);
+    __syncwarp();  // the scratch is reused by the warp's next cell
+}
+
+template <int KMAX, bool SMEM>
+__global__ void __launch_bounds__(32 * kWarpCellWarps) transport_warp_kernel(const uint8_t* __restrict__ gtab,
+                                                                           uint32_t tab_bytes,
+                                                                           const __grid_constant__ TransportArgs<KMAX> io,
+                                                                           size_t n, int* status) {
+    __shared__ uint64_t bar;
+    const uint8_t* tab = gtab;
+    if (SMEM) {
+        if (!stage_to_shared(cb_dsmem, gtab, tab_bytes, &bar, status)) return;
+        tab = cb_dsmem;
+    } else {
+        load_math(gtab);
+    }
+    const size_t table_bytes = warp_table_bytes(SMEM, tab_bytes);
+    double* sh = reinterpret_cast<double*>(cb_dsmem + table_bytes) + (size_t)(threadIdx.x >> 5) * kWarpScratch<KMAX>;
+    if (io.count) n = min(n, (size_t)*io.count);
+    const size_t warps = (size_t)gridDim.x * kWarpCellWarps;
+    for (size_t j = (size_t)blockIdx.x * kWarpCellWarps + (threadIdx.x >> 5); j < n; j += warps) {
+        const size_t i = io.index[j] & kIndexMask;
+        transport_cell_warp<KMAX>(tab, io, i, (io.flags & kCompactOut) ? j : i, sh);
     }
 }
 
@@ -403,7 +592,49 @@ int max_table_smem() {
     }
 CB_DISPATCH(launch_rates, rates_kernel, RatesArgs, kBlock)
 CB_DISPATCH(launch_reaction_rates, reaction_rates_kernel, ReactionRatesArgs, kBlock)
-CB_DISPATCH(launch_transport, transport_kernel, TransportArgs, kTransportBlock)
 #undef CB_DISPATCH
+
+namespace {
+// Gathered launches of up to this many cells per SM go warp-per-cell (above 16 species): one cell per
+// thread would leave most SMs idle and the rest latency-bound; beyond it, one per thread keeps every
+// lane busy without the warp form's serial chains.
+constexpr size_t kWarpCellsPerSm = 128;
+
+template <int KMAX>
+cudaError_t launch_transport_k(const uint8_t* tab, uint32_t tab_bytes, const TransportArgs<KMAX>& io, size_t n,
+                               cudaStream_t st, int* status) {
+    if constexpr (KMAX >= 64) {
+        if (io.index && n <= (size_t)sm_count() * kWarpCellsPerSm) {
+            const size_t scratch = (size_t)kWarpCellWarps * kWarpScratch<KMAX> * sizeof(double);
+            const bool smem = warp_table_bytes(true, tab_bytes) + scratch <= (size_t)max_table_smem();
+            const size_t bytes = warp_table_bytes(smem, tab_bytes) + scratch;
+            auto kern = smem ? transport_warp_kernel<KMAX, true> : transport_warp_kernel<KMAX, false>;
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+            if (e != cudaSuccess) return e;
+            int per_sm = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kWarpCellWarps, bytes);
+            if (per_sm < 1) per_sm = 1;
+            size_t grid = (size_t)sm_count() * per_sm;
+            const size_t want = (n + kWarpCellWarps - 1) / kWarpCellWarps;
+            if (want < grid) grid = want ? want : 1;
+            kern<<<(unsigned)grid, 32 * kWarpCellWarps, bytes, st>>>(tab, tab_bytes, io, n, status);
+            return cudaGetLastError();
+        }
+    }
+    return launch_table_kernel<kTransportBlock>(transport_kernel<KMAX, true>, transport_kernel<KMAX, false>, tab,
+                                                tab_bytes, io, n, st, status);
+}
+}  // namespace
+
+cudaError_t launch_transport(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,
+                             cudaStream_t st, int* status) {
+    switch (kmax) {
+    case 16: return launch_transport_k<16>(tab, tab_bytes, *static_cast<const TransportArgs<16>*>(args), n, st, status);
+    case 64: return launch_transport_k<64>(tab, tab_bytes, *static_cast<const TransportArgs<64>*>(args), n, st, status);
+    case 256:
+        return launch_transport_k<256>(tab, tab_bytes, *static_cast<const TransportArgs<256>*>(args), n, st, status);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 }  // namespace cbg

@@ -143,6 +143,38 @@ def test_training_gate_and_audit():
     assert int(same.sum()) >= st["fallback_cells"] + st["audited_cells"]
 
 
+@pytest.mark.parametrize("config,width", [("k53", 256), ("k250", 512)])
+def test_gate_fallback_warp_per_cell_matches_plain_kernel(config, width):
+    """Above 16 species the gate's few fallback and audit cells run one cell per warp; those cells equal
+    the one-cell-per-thread kernel's outputs bit for bit, and so do the plain values of audited cells."""
+    import torch
+    from combustion_gb300 import surrogate as S
+    mech = _mech(config)
+    s = S.Surrogate(mech, width=width, hidden_layers=2, batch=1024, seed=3)
+    s.generate(1 << 13, S.distribution(config, seed=2))
+    n = 4096
+    cells = S.generate_cells(mech, n, S.distribution(config, seed=7))
+    cells[2, : n // 8] = 3500.0  # above the training temperatures
+    cells[2, n // 8 : n // 8 + 3] = 250.0  # below them
+    plain = _plain_transport(mech, cells)  # not gathered: one cell per thread
+    out = torch.empty_like(plain)
+    st = s.transport(cells, out, audit_stride=16)
+    print(config, st)
+    assert n // 8 + 3 <= st["fallback_cells"] <= n // 4  # a small gathered launch: warp per cell
+    assert torch.equal(out[:, : n // 8 + 3], plain[:, : n // 8 + 3])
+    # audited cells get their plain values from the warp-per-cell kernel in compact order: equal too
+    same = (out == plain).all(dim=0)
+    assert st["audited_cells"] > 0
+    assert int(same.sum()) >= st["fallback_cells"] + st["audited_cells"]
+    # the audit's error is the network's against those values: bounded by the error over every cell
+    # that holds a plain value outside the forced fallbacks (the audited ones and any natural fallback)
+    net = torch.empty_like(plain)
+    s.transport(cells, net, gate=False)
+    idx = torch.nonzero(same[n // 8 + 3 :]).squeeze(1) + n // 8 + 3
+    err = (net[:, idx] - plain[:, idx]).abs() / plain[:, idx].abs()
+    assert st["audit_max_rel_err"][2] <= float(err[2:].max()) * (1 + 1e-6)
+
+
 def test_trained_network_gain_over_plain_kernel():
     """What the trained network gains: transport cells/s through the gated surrogate against the plain
     FP64 kernel on the same cells (53 species), at the error the audit reports."""
