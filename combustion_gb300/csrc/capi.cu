@@ -1,6 +1,7 @@
 // extern "C" entry points declared in include/combustion_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -150,6 +151,33 @@ bool needs_transport(Path p) {
     return p == Path::Transport || p == Path::Fused || p == Path::TransportMixed || p == Path::FusedMixed;
 }
 
+// Cells of one wave of every kernel on the path (the least common multiple of their waves, or the
+// largest wave when that multiple would exceed a chunk): a chunk of whole waves gives every thread of
+// each persistent grid the same number of cells, so no SM idles through a chunk's last partial wave.
+size_t path_wave(const cb_mech* m, Path path) {
+    const uint32_t rb = (uint32_t)m->host.rates_blob.size(), tb = (uint32_t)m->host.transport_blob.size();
+    const uint32_t rmb = (uint32_t)m->host.rates_mixed_blob.size();
+    const uint32_t tmb = (uint32_t)m->host.transport_mixed_blob.size();
+    size_t w[2] = {0, 0};
+    switch (path) {
+    case Path::Rates: w[0] = cbg::wave_rates(m->kmax, rb); break;
+    case Path::ReactionRates: w[0] = cbg::wave_reaction_rates(m->kmax, rb); break;
+    case Path::Transport: w[0] = cbg::wave_transport(m->kmax, tb); break;
+    case Path::Fused: w[0] = cbg::wave_rates(m->kmax, rb); w[1] = cbg::wave_transport(m->kmax, tb); break;
+    case Path::RatesMixed: w[0] = cbg::wave_rates_mixed(m->kmax, rmb); break;
+    case Path::TransportMixed: w[0] = cbg::wave_transport_mixed(m->kmax, tmb); break;
+    case Path::FusedMixed:
+        w[0] = cbg::wave_rates_mixed(m->kmax, rmb);
+        w[1] = cbg::wave_transport_mixed(m->kmax, tmb);
+        break;
+    }
+    if (!w[0] || !w[1]) return w[0] ? w[0] : w[1];
+    size_t a = w[0], b = w[1];
+    while (b) { const size_t t = a % b; a = b; b = t; }
+    const size_t lcm = w[0] / a * w[1];
+    return lcm <= ((size_t)1 << 20) ? lcm : std::max(w[0], w[1]);
+}
+
 // Host arrays: chunks through two device staging slots. Copies run on their own streams and kernels on
 // one compute stream (one chunk's kernels at a time: the kernels use persistent grids), so that the
 // copies of neighbouring chunks overlap the kernels: H2D(c+1) and D2H(c-1) run while chunk c computes.
@@ -158,10 +186,12 @@ int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* 
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
     const bool uniform = rates_layout(path) && (flags & CB_UNIFORM_PRESSURE);
     // chunks small enough that the first upload and the last download are short, large enough to fill
-    // the GPU: n / 16 cells, between 2^17 and 2^20
+    // the GPU: about n / 16 cells, between 2^17 and 2^20, rounded to whole waves of the path's kernels
     size_t chunk = n / 16;
     if (chunk < ((size_t)1 << 17)) chunk = (size_t)1 << 17;
     if (chunk > ((size_t)1 << 20)) chunk = (size_t)1 << 20;
+    const size_t wave = path_wave(m, path);
+    if (wave) chunk = std::max<size_t>(1, (chunk + wave / 2) / wave) * wave;
     if (chunk > n) chunk = n;
     const size_t per_slot = (size_t)(ni + no) * chunk + 2;
     if (m->stage_doubles < 2 * per_slot) {

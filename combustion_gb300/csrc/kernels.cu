@@ -531,19 +531,21 @@ cudaError_t launch_table_kernel(KS ksmem, KG kglobal, const uint8_t* tab, uint32
     const int block = gathered(io) ? 32 : BLOCK;
     int per_sm = 1;
     const size_t want = (n + block - 1) / block;
-    if (smem) {
-        cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, block, tab_bytes);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, block, kMathBytes);
-    }
-    if (per_sm < 1) per_sm = 1;
+    cudaError_t e = table_kernel_occupancy(ksmem, kglobal, block, tab_bytes, kMathBytes, smem, &per_sm);
+    if (e != cudaSuccess) return e;
     size_t grid = (size_t)sm_count() * per_sm;
     if (want < grid) grid = want ? want : 1;
     if (smem) ksmem<<<(unsigned)grid, block, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
     else kglobal<<<(unsigned)grid, block, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
+}
+template <int BLOCK, class KS, class KG>
+size_t wave_of(KS ksmem, KG kglobal, uint32_t tab_bytes) {
+    int per_sm = 1;
+    if (table_kernel_occupancy(ksmem, kglobal, BLOCK, tab_bytes, kMathBytes, (int)tab_bytes <= max_table_smem(),
+                               &per_sm) != cudaSuccess)
+        return 0;
+    return (size_t)sm_count() * per_sm * BLOCK;
 }
 }  // namespace
 
@@ -593,6 +595,20 @@ int max_table_smem() {
 CB_DISPATCH(launch_rates, rates_kernel, RatesArgs, kBlock)
 CB_DISPATCH(launch_reaction_rates, reaction_rates_kernel, ReactionRatesArgs, kBlock)
 #undef CB_DISPATCH
+
+#define CB_WAVE(FN, KERNEL, BLOCK)                                                     \
+    size_t FN(int kmax, uint32_t tab_bytes) {                                          \
+        switch (kmax) {                                                                \
+        case 16: return wave_of<BLOCK>(KERNEL<16, true>, KERNEL<16, false>, tab_bytes);    \
+        case 64: return wave_of<BLOCK>(KERNEL<64, true>, KERNEL<64, false>, tab_bytes);    \
+        case 256: return wave_of<BLOCK>(KERNEL<256, true>, KERNEL<256, false>, tab_bytes); \
+        default: return 0;                                                             \
+        }                                                                              \
+    }
+CB_WAVE(wave_rates, rates_kernel, kBlock)
+CB_WAVE(wave_reaction_rates, reaction_rates_kernel, kBlock)
+CB_WAVE(wave_transport, transport_kernel, kTransportBlock)
+#undef CB_WAVE
 
 namespace {
 // Gathered launches of up to this many cells per SM go warp-per-cell (above 16 species): one cell per

@@ -55,6 +55,33 @@ inline int kmax_for(int K, int n_eff) {
 }
 
 int max_table_smem();
+
+// Blocks of a persistent table kernel resident per SM, the tables in shared memory (smem: the variant
+// ksmem, whose dynamic shared memory limit is raised first) or read from global memory (kglobal, only
+// the math tables in shared memory).
+template <class KS, class KG>
+cudaError_t table_kernel_occupancy(KS ksmem, KG kglobal, int block, uint32_t tab_bytes, uint32_t math_bytes,
+                                   bool smem, int* per_sm) {
+    *per_sm = 1;
+    if (smem) {
+        cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
+        if (e != cudaSuccess) return e;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, ksmem, block, tab_bytes);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kglobal, block, math_bytes);
+    }
+    if (*per_sm < 1) *per_sm = 1;
+    return cudaSuccess;
+}
+
+// Cells one wave of a kernel's persistent grid covers (its threads resident on the whole GPU): every
+// thread of a launch over a multiple of it gets the same number of cells. Host arrays go through the
+// GPU in chunks of whole waves.
+size_t wave_rates(int kmax, uint32_t tab_bytes);
+size_t wave_reaction_rates(int kmax, uint32_t tab_bytes);
+size_t wave_transport(int kmax, uint32_t tab_bytes);
+size_t wave_rates_mixed(int kmax, uint32_t tab_bytes);
+size_t wave_transport_mixed(int kmax, uint32_t tab_bytes);
 cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, double* y, size_t n,
                               cudaStream_t st);
 cudaError_t launch_rates(int kmax, const uint8_t* tab, uint32_t tab_bytes, const void* args, size_t n,

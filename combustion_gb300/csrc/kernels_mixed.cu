@@ -387,23 +387,31 @@ __global__ void __launch_bounds__(kTransportBlock) transport_mixed_kernel(const 
 
 // ---------------------------------------------------------------------------------------------------
 namespace {
+int sm_count_m() {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+template <int BLOCK, class KS, class KG>
+size_t wave_of_m(KS ksmem, KG kglobal, uint32_t tab_bytes) {
+    int per_sm = 1;
+    if (table_kernel_occupancy(ksmem, kglobal, BLOCK, tab_bytes, kMathBytes, (int)tab_bytes <= max_table_smem(),
+                               &per_sm) != cudaSuccess)
+        return 0;
+    return (size_t)sm_count_m() * per_sm * BLOCK;
+}
+
 template <int BLOCK, class Args, class KS, class KG>
 cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io, size_t n,
                          cudaStream_t st, int* status) {
     const bool smem = (int)tab_bytes <= max_table_smem();
-    int per_sm = 1, dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int per_sm = 1;
     const size_t want = (n + BLOCK - 1) / BLOCK;
-    if (smem) {
-        cudaError_t e = cudaFuncSetAttribute(ksmem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tab_bytes);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksmem, BLOCK, tab_bytes);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kglobal, BLOCK, kMathBytes);
-    }
-    if (per_sm < 1) per_sm = 1;
-    size_t grid = (size_t)sms * per_sm;
+    cudaError_t e = table_kernel_occupancy(ksmem, kglobal, BLOCK, tab_bytes, kMathBytes, smem, &per_sm);
+    if (e != cudaSuccess) return e;
+    size_t grid = (size_t)sm_count_m() * per_sm;
     if (want < grid) grid = want ? want : 1;
     if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
     else kglobal<<<(unsigned)grid, BLOCK, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
@@ -427,5 +435,18 @@ cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_
 CB_DISPATCH_M(launch_rates_mixed, rates_mixed_kernel, RatesArgs, kBlock)
 CB_DISPATCH_M(launch_transport_mixed, transport_mixed_kernel, TransportArgs, kTransportBlock)
 #undef CB_DISPATCH_M
+
+#define CB_WAVE_M(FN, KERNEL, BLOCK)                                                        \
+    size_t FN(int kmax, uint32_t tab_bytes) {                                               \
+        switch (kmax) {                                                                     \
+        case 16: return wave_of_m<BLOCK>(KERNEL<16, true>, KERNEL<16, false>, tab_bytes);    \
+        case 64: return wave_of_m<BLOCK>(KERNEL<64, true>, KERNEL<64, false>, tab_bytes);    \
+        case 256: return wave_of_m<BLOCK>(KERNEL<256, true>, KERNEL<256, false>, tab_bytes); \
+        default: return 0;                                                                  \
+        }                                                                                   \
+    }
+CB_WAVE_M(wave_rates_mixed, rates_mixed_kernel, kBlock)
+CB_WAVE_M(wave_transport_mixed, transport_mixed_kernel, kTransportBlock)
+#undef CB_WAVE_M
 
 }  // namespace cbg
