@@ -5,7 +5,9 @@
 // rates function's outputs, reaction.rs:356-391) and the cvode crate's BDF (cvode/lib.rs:17-47: CV_BDF,
 // dense linear solver, difference-quotient Jacobian). Here many reactors advance together: each warp
 // owns one reactor at a time, taken from a work queue, and keeps its iteration matrix (LU with partial
-// pivoting), difference array and rates scratch in shared memory; the rates program runs
+// pivoting), difference array and rates scratch in shared memory (in global memory when they do not fit,
+// for large mechanisms: then each reactor keeps its own factorisation, made by panels, with a
+// transposed copy for coalesced triangular solves); the rates program runs
 // warp-cooperatively (lanes split species, third-body rows and reactions; per-species sums in the
 // reactions' order). Launches are slices of at most `slice_steps` steps per reactor so that reactors of
 // uneven stiffness rebalance between launches; a CUDA graph replays the slice sequence.
@@ -36,7 +38,9 @@
 #include "device_common.cuh"
 #include "device_math.cuh"
 #include "rates_core.cuh"
+#include "rates_mixed_core.cuh"
 #include "tables.h"
+#include "tables_mixed.h"
 
 namespace cbg {
 namespace bdf {
@@ -45,15 +49,19 @@ constexpr int kMaxOrder = 5;
 constexpr int kDRows = kMaxOrder + 3;
 constexpr int kNewtonMaxIter = 4;
 constexpr double kMinFactor = 0.2, kMaxFactor = 10.0;
-constexpr int kMaxN = 66;  // state size limit: the iteration matrix stays in shared memory
+constexpr int kPanel = 8;  // columns per panel of the blocked factorisation (global-memory matrices)
+constexpr double kReuseSpread = 0.3;  // CB_BDF_REUSE_LU: largest |c / c_lu - 1| of a kept factorisation
+constexpr int kReuseSteps = 20;       // CB_BDF_REUSE_LU: steps a factorisation is kept at most
 
 enum State : int { kNew = 0, kRunning = 1, kDone = 2, kFailStep = 3, kFailSteps = 4, kFailLU = 5 };
 
 struct Head {
     double t, h;
     double ign_t, ign_g, ta, ga, tc, gc, tp, gp;  // max dT/dt, its neighbours, the previous sample
+    double c_lu;                                  // c of the factorisation kept between launches
     int q, n_equal, state, jac_current;
-    int steps, rhs, jacs, lus, newton_fail, err_fail, need_next, pad;
+    int steps, rhs, jacs, lus, newton_fail, err_fail, need_next, since_lu;
+    int lu_have, lu_refresh;  // a kept factorisation exists; c changed since it was made
 };
 
 struct Params {
@@ -77,6 +85,15 @@ struct Params {
     const double* eval_y;
     double* eval_f;
     double* eval_J;
+    const uint8_t* tab_m;  // mixed-precision rates tables (global memory): f(u) with CB_BDF_MIXED_RHS
+    int mixed, reuse_lu;
+    // Large states: per-warp workspaces in global memory (null: in shared memory), and per reactor its
+    // factorisation [n][N][LD], the factors' transpose (coalesced triangular solves), pivots, 1 / U_kk.
+    uint8_t* ws_global;
+    double* LUr;
+    double* LUt;
+    double* rdiag_r;
+    int* piv_r;
 };
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -266,6 +283,113 @@ __device__ RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double
     return o;
 }
 
+// The warp's cell for the mixed-precision rates program (reaction_rate_m).
+struct WarpCellM {
+    const double* C;
+    const double* ex;
+    const double* exn;
+    const float* Mf;
+    double C0, rcpC0, rcpC0sq;
+    float Ctotf, Tf, lnTf, rcpTf;
+};
+
+// du/dt by the mixed-precision rates program (the arithmetic of kernels_mixed.cu's rates_mixed_cell,
+// warp-cooperative as rhs_warp): FP64 concentrations, Gibbs polynomials and exponentials, rates of
+// progress, accumulation and energy sums; FP32 Arrhenius terms, third-body sums, falloff blending and
+// h/RT, cp/R polynomials. w.M holds the FP32 third-body sums.
+__device__ void rhs_warp_mixed(const Params& p, const Mech& m, const RatesMixedTables& tm, const Work& w, double pR,
+                               double rP, const double* y, double* f, int lane) {
+    const RatesMixedHeader& H = *tm.H;
+    const int K = p.K, A = p.A, R = p.R;
+    const double T = y[0], V = y[1];
+    const double rcpT = rcp64(T), lnT = log64(T);
+    const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
+    const double md = rcp64(V);
+    double s = 0.0;
+    for (int k = lane; k < K - 1; k += 32) {
+        const double ck = md * max0(y[2 + k]);
+        w.C[k] = ck;
+        s += ck;
+    }
+    s = warp_sum(s);
+    const double Ctot = pR * rcpT;
+    if (lane == 0) w.C[K - 1] = Ctot - s;
+    WarpCellM c;
+    c.C0 = H.C0 * rcpT;
+    c.rcpC0 = H.rcp_C0 * T;
+    c.rcpC0sq = c.rcpC0 * c.rcpC0;
+    c.Ctotf = dbl_to_flt(Ctot);
+    c.Tf = dbl_to_flt(T);
+    c.lnTf = dbl_to_flt(lnT);
+    c.rcpTf = dbl_to_flt(rcpT);
+    const float Tf = c.Tf, rcpTf = c.rcpTf;
+    for (int k = lane; k < K; k += 32) {
+        const SpeciesF& sp = tm.species[k];
+        const int pc = piece_of_m(sp.split, T);
+        const float* cp = sp.cp[pc];
+        const float ck = fmaf(cp[4], Tf, cp[3]);
+        w.cpk[k] = flt_to_dbl(fmaf(fmaf(fmaf(ck, Tf, cp[2]), Tf, cp[1]), Tf, cp[0]));
+        if (k < A) {
+            const float* h = sp.h[pc];
+            w.hk[k] = flt_to_dbl(fmaf(h[5], rcpTf, fmaf(fmaf(fmaf(fmaf(h[4], Tf, h[3]), Tf, h[2]), Tf, h[1]), Tf, h[0])));
+            if (sp.need_exp | sp.need_exp_neg) {
+                const double* g = sp.g[pc];
+                const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
+                if (sp.need_exp) w.ex[k] = min_pos(H.M3, exp64(x));
+                if (sp.need_exp_neg) w.exn[k] = min_pos(H.cbrt_max, exp64(-x));
+            }
+        }
+    }
+    __syncwarp();
+    float* Mf = reinterpret_cast<float*>(w.M);
+    for (int e = lane; e < H.n_eff; e += 32) {
+        const float* E = tm.eff + (size_t)e * K;
+        float sum = 0.f;
+        for (int k = 0; k < K; k++) sum = fmaf(E[k], dbl_to_flt(w.C[k]), sum);
+        Mf[e] = c.Ctotf + sum;
+    }
+    __syncwarp();
+    c.C = w.C;
+    c.ex = w.ex;
+    c.exn = w.exn;
+    c.Mf = Mf;
+    for (int r = lane; r < R; r += 32) {
+        const ReactionF& x = tm.reactions[r];
+        double cR;
+        switch (x.model) {
+        case 0: cR = reaction_rate_m<0>(tm, x, c); break;
+        case 1: cR = reaction_rate_m<1>(tm, x, c); break;
+        case 2: cR = reaction_rate_m<2>(tm, x, c); break;
+        case 3: cR = reaction_rate_m<3>(tm, x, c); break;
+        case 4: cR = reaction_rate_m<4>(tm, x, c); break;
+        default: cR = reaction_rate_m<5>(tm, x, c); break;
+        }
+        w.cR[r] = cR;
+    }
+    __syncwarp();
+    double E = 0.0, dtE = 0.0, Cp = 0.0;
+    for (int k = lane; k < A; k += 32) {
+        double wk = 0.0;
+        for (int q = m.csr_start[k]; q < m.csr_start[k + 1]; q++) {
+            const int e = m.csr[q];
+            wk = fma(small_int_to_double((int)(int8_t)(e & 0xff)), w.cR[e >> 8], wk);
+        }
+        f[2 + k] = wk;
+        E = fma(wk, w.hk[k], E);
+        dtE = fma(tm.species[k].dtE, wk, dtE);
+    }
+    for (int k = lane; k < K; k += 32) Cp = fma(w.cpk[k], w.C[k], Cp);
+    E = warp_sum(E);
+    dtE = warp_sum(dtE);
+    Cp = warp_sum(Cp);
+    const double dtT_T = -E * rcp64(Cp);
+    if (lane == 0) {
+        f[0] = T * dtT_T;
+        f[1] = V * fma(rP * T, dtE, dtT_T);
+    }
+    __syncwarp();
+}
+
 // d/dC_{ks[i]} of prod_q C_{ks[q]}^{ns[q]}: one factor of species ks[i] removed, times its multiplicity.
 __device__ __forceinline__ double deriv_product(const double* C, const uint16_t* ks, const int8_t* ns, int n, int i) {
     double p = small_int_to_double(ns[i]);
@@ -431,8 +555,133 @@ __device__ void lu_solve_warp(const double* A, int N, int LD, const int* piv, co
     }
 }
 
-// I - c J (J in w.LU already when `fresh`, else from global) factorised in w.LU.
-__device__ bool build_lu(const Params& p, const Work& w, const double* Jg, double c, bool fresh, int lane) {
+// lu_warp by panels of kPanel columns, for matrices in global memory: inside a panel the pivot search,
+// row swap (whole rows), scaling and update of the panel's own columns go column by column; then the
+// panel's U rows right of it by forward substitution, and one rank-kPanel update of the trailing matrix,
+// which so is read and written once per panel instead of once per column. Every element receives the
+// same FMAs in the same order as in lu_warp.
+__device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdiag, int lane) {
+    for (int kb = 0; kb < N; kb += kPanel) {
+        const int ke = min(kb + kPanel, N);
+        for (int k = kb; k < ke; k++) {
+            double best = -1.0;
+            int bi = k;
+            for (int i = k + lane; i < N; i += 32) {
+                const double v = fabs(A[(size_t)i * LD + k]);
+                if (v > best) {
+                    best = v;
+                    bi = i;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > best || (ov == best && oi < bi)) {
+                    best = ov;
+                    bi = oi;
+                }
+            }
+            best = __shfl_sync(0xffffffffu, best, 0);
+            bi = __shfl_sync(0xffffffffu, bi, 0);
+            if (!(best > 0.0) || !(best < 1e300)) return false;
+            if (lane == 0) piv[k] = bi;
+            if (bi != k)
+                for (int j = lane; j < N; j += 32) {
+                    const double t = A[(size_t)k * LD + j];
+                    A[(size_t)k * LD + j] = A[(size_t)bi * LD + j];
+                    A[(size_t)bi * LD + j] = t;
+                }
+            __syncwarp();
+            const double rp = 1.0 / A[(size_t)k * LD + k];
+            if (lane == 0) rdiag[k] = rp;
+            for (int i = k + 1 + lane; i < N; i += 32) {
+                double* Ai = A + (size_t)i * LD;
+                const double l = Ai[k] * rp;
+                Ai[k] = l;
+                for (int j = k + 1; j < ke; j++) Ai[j] = fma(-l, A[(size_t)k * LD + j], Ai[j]);
+            }
+            __syncwarp();
+        }
+        if (ke == N) break;
+        const int nb = ke - kb;
+        // U rows of the panel, columns ke..N-1: forward substitution with the panel's unit lower L
+        for (int j = ke + lane; j < N; j += 32) {
+            double u[kPanel];
+#pragma unroll
+            for (int r = 0; r < kPanel; r++) {
+                if (r < nb) {
+                    double a = A[(size_t)(kb + r) * LD + j];
+#pragma unroll
+                    for (int t = 0; t < r; t++) a = fma(-A[(size_t)(kb + r) * LD + kb + t], u[t], a);
+                    u[r] = a;
+                    A[(size_t)(kb + r) * LD + j] = a;
+                }
+            }
+        }
+        __syncwarp();
+        // trailing matrix: A[i][j] -= sum_t L[i][kb+t] U[kb+t][j], t in panel order
+        for (int j = ke + lane; j < N; j += 32) {
+            double u[kPanel];
+#pragma unroll
+            for (int t = 0; t < kPanel; t++) u[t] = t < nb ? A[(size_t)(kb + t) * LD + j] : 0.0;
+#pragma unroll 2
+            for (int i = ke; i < N; i++) {
+                const double* Li = A + (size_t)i * LD + kb;
+                double a = A[(size_t)i * LD + j];
+#pragma unroll
+                for (int t = 0; t < kPanel; t++)
+                    if (t < nb) a = fma(-Li[t], u[t], a);
+                A[(size_t)i * LD + j] = a;
+            }
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+// At = A^T (both N x N with rows of LD), for the triangular solves below.
+__device__ void transpose_warp(const double* A, double* At, int N, int LD, int lane) {
+    for (int i = 0; i < N; i++)
+        for (int j = lane; j < N; j += 32) At[(size_t)j * LD + i] = A[(size_t)i * LD + j];
+    __syncwarp();
+}
+
+// lu_solve_warp on the transposed factors: column k of L and U is row k of At, so every lane's reads of
+// one elimination step fall in one contiguous row (global-memory matrices). Same operations and order.
+__device__ void lu_solve_t_warp(const double* At, int N, int LD, const int* piv, const double* rdiag, double* b,
+                                int lane) {
+    if (lane == 0)
+        for (int k = 0; k < N; k++) {
+            const int pk = piv[k];
+            if (pk != k) {
+                const double t = b[k];
+                b[k] = b[pk];
+                b[pk] = t;
+            }
+        }
+    __syncwarp();
+    for (int k = 0; k < N; k++) {
+        const double bk = b[k];
+        const double* col = At + (size_t)k * LD;
+        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-col[i], bk, b[i]);
+        __syncwarp();
+    }
+    for (int k = N - 1; k >= 0; k--) {
+        const double bk = b[k] * rdiag[k];
+        __syncwarp();
+        if (lane == 0) b[k] = bk;
+        const double* col = At + (size_t)k * LD;
+        for (int i = lane; i < k; i += 32) b[i] = fma(-col[i], bk, b[i]);
+        __syncwarp();
+    }
+}
+
+// I - c J (J in w.LU already when `fresh`, else from global) factorised in w.LU; with per-reactor
+// factorisations in global memory (GLOBAL), by panels, and its transpose into `LUt` for the solves.
+template <bool GLOBAL>
+__device__ bool build_lu(const Params& p, const Work& w, const double* Jg, double c, bool fresh, double* LUt,
+                         int lane) {
     const int N = p.N, LD = p.LD;
     for (int idx = lane; idx < N * N; idx += 32) {
         const int i = idx / N, j = idx % N;
@@ -440,7 +689,13 @@ __device__ bool build_lu(const Params& p, const Work& w, const double* Jg, doubl
         w.LU[(size_t)i * LD + j] = (i == j ? 1.0 : 0.0) - c * Jij;
     }
     __syncwarp();
-    return lu_warp(w.LU, N, LD, w.piv, w.rdiag, lane);
+    if constexpr (!GLOBAL) {
+        return lu_warp(w.LU, N, LD, w.piv, w.rdiag, lane);
+    } else {
+        if (!lu_warp_blocked(w.LU, N, LD, w.piv, w.rdiag, lane)) return false;
+        transpose_warp(w.LU, LUt, N, LD, lane);
+        return true;
+    }
 }
 
 __device__ __forceinline__ double rms_scaled(const double* x, const double* scale, int N, int lane) {
@@ -491,7 +746,10 @@ __device__ __forceinline__ double gamma_k(int k) {  // sum_{i=1..k} 1/i
     return g;
 }
 
-// One reactor for at most `budget` steps (warp-uniform control flow).
+// One reactor for at most `budget` steps (warp-uniform control flow). MIXED: the first Newton iteration
+// of each step on the mixed-precision f(u); GLOBAL: workspaces and per-reactor factorisations in global
+// memory (w.LU, w.piv, w.rdiag are the reactor's own).
+template <bool MIXED, bool GLOBAL>
 __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, int lane) {
     const int N = p.N;
     Head hd = p.head[r];
@@ -499,9 +757,24 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
     double* Dg = p.D + (size_t)r * kDRows * N;
     double* Jg = p.J + (size_t)r * N * N;
     const double pR = p.pR[r], rP = 1.0 / pR;
+    double* LUt = GLOBAL ? p.LUt + (size_t)r * N * p.LD : nullptr;
     for (int i = lane; i < kDRows * N; i += 32) w.D[i] = Dg[i];
     __syncwarp();
-    bool lu_valid = false;
+    // lu_have: w.LU holds the factorisation of I - c_lu J; lu_refresh: c changed since (a step size or
+    // order change), so it is made again before the next Newton iteration unless CB_BDF_REUSE_LU keeps
+    // it. A launch starts with a fresh factorisation, except that with CB_BDF_REUSE_LU a reactor's own
+    // (global memory) carries over.
+    const bool carry = GLOBAL && p.reuse_lu;
+    bool lu_have = carry ? hd.lu_have != 0 : false;
+    bool lu_refresh = carry ? hd.lu_refresh != 0 : true;
+    double c_lu = hd.c_lu;
+    auto factorise = [&](double c, bool fresh) {
+        lu_have = build_lu<GLOBAL>(p, w, Jg, c, fresh, LUt, lane);
+        c_lu = c;
+        lu_refresh = false;
+        hd.lus++;
+        hd.since_lu = 0;
+    };
     if (hd.state == kNew) {
         // f(y0), initial step (Hairer, Norsett and Wanner, Solving ODEs I, II.4), D_1 = h f(y0), J(y0)
         for (int i = lane; i < N; i += 32) w.y[i] = w.D[i];
@@ -542,8 +815,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         hd.jacs++;
         hd.rhs += 2;
         hd.jac_current = 1;
-        lu_valid = build_lu(p, w, Jg, h / gamma_k(1), true, lane);
-        hd.lus++;
+        factorise(h / gamma_k(1), true);
         hd.state = kRunning;
     }
     const double newton_tol = fmax(10.0 * 2.220446049250313e-16 / p.rtol, fmin(0.03, sqrt(p.rtol)));
@@ -562,7 +834,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
             change_D(w.D, N, q, hn / h, lane);
             h = hn;
             hd.n_equal = 0;
-            lu_valid = false;
+            lu_refresh = true;
         }
         if (!(h >= p.h_min)) {
             hd.state = kFailStep;
@@ -582,17 +854,21 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
             w.d[i] = 0.0;
         }
         __syncwarp();
-        if (!lu_valid) {
-            lu_valid = build_lu(p, w, Jg, c, false, lane);
-            hd.lus++;
-        }
+        if (lu_have && lu_refresh && p.reuse_lu && fabs(c / c_lu - 1.0) <= kReuseSpread && hd.since_lu < kReuseSteps)
+            lu_refresh = false;  // kept: the correction is scaled below
+        if (!lu_have || lu_refresh) factorise(c, false);
+        // a kept factorisation of I - c_lu J: Newton corrections scaled by 2 / (1 + c / c_lu)
+        const double corr = (p.reuse_lu && c != c_lu) ? 2.0 / (1.0 + c / c_lu) : 1.0;
         // Newton iterations on d - c f(t_new, ypred + d) + psi = 0
         bool converged = false;
         int n_iter = 0;
         double dy_norm_old = -1.0;
-        if (lu_valid) {
+        if (lu_have) {
             for (int k = 0; k < kNewtonMaxIter; k++) {
-                rhs_warp<false>(p, m, w, pR, rP, w.y, w.f, lane);
+                // MIXED: the first iteration (the correction from the predictor) on the mixed-precision
+                // f; the later ones, whose corrections decide convergence, in FP64
+                if (MIXED && k == 0) rhs_warp_mixed(p, m, RatesMixedTables(p.tab_m), w, pR, rP, w.y, w.f, lane);
+                else rhs_warp<false>(p, m, w, pR, rP, w.y, w.f, lane);
                 hd.rhs++;
                 n_iter = k + 1;
                 bool finite = true;
@@ -603,7 +879,12 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
                 }
                 if (!__all_sync(0xffffffffu, finite)) break;
                 __syncwarp();
-                lu_solve_warp(w.LU, N, p.LD, w.piv, w.rdiag, w.b, lane);
+                if constexpr (GLOBAL) lu_solve_t_warp(LUt, N, p.LD, w.piv, w.rdiag, w.b, lane);
+                else lu_solve_warp(w.LU, N, p.LD, w.piv, w.rdiag, w.b, lane);
+                if (corr != 1.0) {
+                    for (int i = lane; i < N; i += 32) w.b[i] *= corr;
+                    __syncwarp();
+                }
                 const double dy_norm = rms_scaled(w.b, w.scale, N, lane);
                 const double rate = dy_norm_old >= 0.0 ? dy_norm / dy_norm_old : -1.0;
                 if (rate >= 0.0 && (rate >= 1.0 || pow(rate, (double)(kNewtonMaxIter - k)) / (1.0 - rate) * dy_norm > newton_tol))
@@ -613,11 +894,15 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
                     w.d[i] += w.b[i];
                 }
                 __syncwarp();
-                if (dy_norm == 0.0 || (rate >= 0.0 && rate / (1.0 - rate) * dy_norm < newton_tol)) {
+                // MIXED: the first FP64 correction follows the mixed one, whose size says nothing about
+                // the FP64 iteration's rate; it is accepted when it is below the tolerance itself (the
+                // first-iteration test of CVODE), and the rate is measured from it on.
+                if (dy_norm == 0.0 || (rate >= 0.0 && rate / (1.0 - rate) * dy_norm < newton_tol) ||
+                    (MIXED && k == 1 && dy_norm <= newton_tol)) {
                     converged = true;
                     break;
                 }
-                dy_norm_old = dy_norm;
+                dy_norm_old = (MIXED && k == 0) ? -1.0 : dy_norm;
             }
         }
         if (!converged) {
@@ -627,15 +912,14 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
                 hd.jacs++;
                 hd.rhs += 2;
                 hd.jac_current = 1;
-                lu_valid = build_lu(p, w, Jg, c, true, lane);
-                hd.lus++;
+                factorise(c, true);
                 hd.h = h;
                 continue;
             }
             change_D(w.D, N, q, 0.5, lane);
             hd.h = 0.5 * h;
             hd.n_equal = 0;
-            lu_valid = false;
+            lu_refresh = true;
             continue;
         }
         const double safety = 0.9 * (2 * kNewtonMaxIter + 1) / (2 * kNewtonMaxIter + n_iter);
@@ -655,6 +939,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         }
         // accepted
         hd.steps++;
+        hd.since_lu++;
         budget--;
         hd.t = t_new;
         hd.jac_current = 0;
@@ -725,9 +1010,12 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         hd.q = q;
         hd.h = h * factor;
         hd.n_equal = 0;
-        lu_valid = false;
+        lu_refresh = true;
     }
     for (int i = lane; i < kDRows * N; i += 32) Dg[i] = w.D[i];
+    hd.lu_have = lu_have ? 1 : 0;
+    hd.lu_refresh = lu_refresh ? 1 : 0;
+    hd.c_lu = c_lu;
     if (lane == 0) {
         p.head[r] = hd;
         if (hd.state != kRunning) atomicAdd(p.done, 1);
@@ -735,6 +1023,14 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
     __syncwarp();
 }
 
+// This warp's workspace: after the tables in shared memory, or its slot of the global workspaces.
+__device__ __forceinline__ uint8_t* workspace_of(const Params& p, int warp) {
+    if (p.ws_global) return p.ws_global + ((size_t)blockIdx.x * (blockDim.x >> 5) + warp) * p.ws_bytes;
+    const size_t tab_smem = p.smem_tables ? ((p.tab_bytes + 127) & ~127u) : (size_t)kMathBytes;
+    return cb_dsmem + tab_smem + (size_t)warp * p.ws_bytes;
+}
+
+template <bool MIXED, bool GLOBAL>
 __global__ void slice_kernel(const Params p) {
     __shared__ uint64_t bar;
     const uint8_t* tab = p.tab;
@@ -745,15 +1041,22 @@ __global__ void slice_kernel(const Params p) {
         load_math(p.tab);
     }
     const Mech m(tab, p);
-    const size_t tab_smem = p.smem_tables ? ((p.tab_bytes + 127) & ~127u) : (size_t)kMathBytes;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Work w = carve(p, cb_dsmem + tab_smem + (size_t)warp * p.ws_bytes);
+    const Work w = carve(p, workspace_of(p, warp));
     for (;;) {
         int r = 0;
         if (lane == 0) r = atomicAdd(p.queue, 1);
         r = __shfl_sync(0xffffffffu, r, 0);
         if (r >= p.n) break;
-        integrate(p, m, w, r, lane);
+        if constexpr (GLOBAL) {  // the reactor's own factorisation
+            Work wr = w;
+            wr.LU = p.LUr + (size_t)r * p.N * p.LD;
+            wr.piv = p.piv_r + (size_t)r * p.N;
+            wr.rdiag = p.rdiag_r + (size_t)r * p.N;
+            integrate<MIXED, GLOBAL>(p, m, wr, r, lane);
+        } else {
+            integrate<MIXED, GLOBAL>(p, m, w, r, lane);
+        }
     }
 }
 
@@ -768,14 +1071,14 @@ __global__ void eval_kernel(const Params p, int count) {
         load_math(p.tab);
     }
     const Mech m(tab, p);
-    const size_t tab_smem = p.smem_tables ? ((p.tab_bytes + 127) & ~127u) : (size_t)kMathBytes;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Work w = carve(p, cb_dsmem + tab_smem + (size_t)warp * p.ws_bytes);
+    const Work w = carve(p, workspace_of(p, warp));
     const int N = p.N;
     for (int s = blockIdx.x * (blockDim.x >> 5) + warp; s < count; s += gridDim.x * (blockDim.x >> 5)) {
         for (int i = lane; i < N; i += 32) w.y[i] = p.eval_y[(size_t)s * N + i];
         __syncwarp();
         jacobian_warp(p, m, w, p.pR[s], 1.0 / p.pR[s], w.y, p.eval_J + (size_t)s * N * N, lane);
+        if (p.mixed) rhs_warp_mixed(p, m, RatesMixedTables(p.tab_m), w, p.pR[s], 1.0 / p.pR[s], w.y, w.f, lane);
         for (int i = lane; i < N; i += 32) p.eval_f[(size_t)s * N + i] = w.f[i];
         __syncwarp();
     }
@@ -803,6 +1106,14 @@ struct cb_reactors {
     int warps = 0, smem_tables = -1;  // launch shape (0 / -1: autotune)
     bool have_state = false;
     cudaStream_t stream = nullptr;
+    uint8_t* d_tab_m = nullptr;  // mixed-precision rates tables (CB_BDF_MIXED_RHS)
+    // Workspaces in global memory when one warp's does not fit in shared memory (large mechanisms):
+    // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, pivots and 1 / U_kk.
+    bool global = false;
+    uint8_t* ws = nullptr;
+    size_t ws_slots = 0;
+    double *LUr = nullptr, *LUt = nullptr, *rdiag_r = nullptr;
+    int* piv_r = nullptr;
 };
 
 namespace {
@@ -820,7 +1131,7 @@ uint32_t ws_bytes(const cb_reactors* s) {
 
 size_t smem_bytes(const cb_reactors* s, int warps, int tables) {
     const size_t tab = tables ? ((s->blob.size() + 127) & ~(size_t)127) : (size_t)cbg::kMathBytes;
-    return tab + (size_t)warps * ws_bytes(s);
+    return tab + (s->global ? 0 : (size_t)warps * ws_bytes(s));
 }
 
 int max_smem() {
@@ -866,23 +1177,58 @@ Params params(cb_reactors* s, int tables) {
     p.queue = s->counters;
     p.done = s->counters + 1;
     p.status = s->counters + 2;
+    p.tab_m = s->d_tab_m;
+    p.mixed = (s->opt.flags & CB_BDF_MIXED_RHS) ? 1 : 0;
+    p.reuse_lu = (s->opt.flags & CB_BDF_REUSE_LU) ? 1 : 0;
+    if (s->global) {
+        p.ws_global = s->ws;
+        p.LUr = s->LUr;
+        p.LUt = s->LUt;
+        p.rdiag_r = s->rdiag_r;
+        p.piv_r = s->piv_r;
+    }
     return p;
+}
+
+// Global workspaces for at least `slots` warps in flight (outside any stream capture).
+cudaError_t ensure_slots(cb_reactors* s, size_t slots) {
+    if (!s->global || slots <= s->ws_slots) return cudaSuccess;
+    if (s->ws) {
+        cudaError_t e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) return e;
+        cudaFree(s->ws);
+        s->ws = nullptr;
+        s->ws_slots = 0;
+    }
+    cudaError_t e = cudaMalloc(&s->ws, slots * ws_bytes(s));
+    if (e == cudaSuccess) s->ws_slots = slots;
+    return e;
+}
+
+// The slice kernel of the batch's variant: FP64 or mixed-precision first Newton iterations, workspaces
+// in shared or global memory.
+using SliceFn = void (*)(Params);
+SliceFn slice_fn(const cb_reactors* s) {
+    const bool mixed = (s->opt.flags & CB_BDF_MIXED_RHS) != 0;
+    if (s->global) return mixed ? slice_kernel<true, true> : slice_kernel<false, true>;
+    return mixed ? slice_kernel<true, false> : slice_kernel<false, false>;
 }
 
 // Shared-memory limit and grid of a launch shape (outside any stream capture).
 cudaError_t prepare_slice(cb_reactors* s, int warps, int tables, int* grid) {
     const size_t smem = smem_bytes(s, warps, tables);
-    cudaError_t e = cudaFuncSetAttribute(slice_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const SliceFn fn = slice_fn(s);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 1;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, slice_kernel, 32 * warps, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * warps, smem);
     if (e != cudaSuccess) return e;
     *grid = sm_count() * (per_sm < 1 ? 1 : per_sm);
-    return cudaSuccess;
+    return ensure_slots(s, (size_t)*grid * warps);
 }
 
 cudaError_t launch_slice(cb_reactors* s, int warps, int tables, int grid, cudaStream_t st) {
-    slice_kernel<<<grid, 32 * warps, smem_bytes(s, warps, tables), st>>>(params(s, tables));
+    slice_fn(s)<<<grid, 32 * warps, smem_bytes(s, warps, tables), st>>>(params(s, tables));
     return cudaGetLastError();
 }
 
@@ -913,7 +1259,8 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     if (v.A != v.K - 1)
         return cbi::fail(CB_ERR_UNSUPPORTED, "reactors need every non-bulk species active (inert non-bulk species "
                                              "would be parameters, not state)");
-    if (v.K + 1 > kMaxN) return cbi::fail(CB_ERR_UNSUPPORTED, "at most 65 species for the batched integrator");
+    if (opt->flags & ~(CB_BDF_MIXED_RHS | CB_BDF_REUSE_LU | CB_BDF_GLOBAL_MEMORY))
+        return cbi::fail(CB_ERR_INVALID, "unknown integrator flag");
     cb_reactors* s = new cb_reactors();
     s->mech = mech;
     s->device = v.device;
@@ -969,8 +1316,23 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     if (e == cudaSuccess) e = cudaMalloc(&s->J, n * (size_t)s->N * s->N * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&s->counters, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(s->counters, 0, 4 * sizeof(int));
+    if (e == cudaSuccess && (s->opt.flags & CB_BDF_MIXED_RHS)) {
+        const std::vector<uint8_t>& mb = *v.rates_mixed_blob;
+        e = cudaMalloc(&s->d_tab_m, mb.size());
+        if (e == cudaSuccess) e = cudaMemcpy(s->d_tab_m, mb.data(), mb.size(), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor batch allocation"));
-    if (!shape_fits(s, 1, 0)) return fail_free(cbi::fail(CB_ERR_UNSUPPORTED, "reactor workspace exceeds shared memory"));
+    // one warp's workspace beside the math tables in shared memory, or all of them in global memory
+    s->global = (s->opt.flags & CB_BDF_GLOBAL_MEMORY) || !shape_fits(s, 1, 0);
+    if (s->global) {
+        const size_t per = (size_t)s->N * s->LD;
+        e = cudaMalloc(&s->LUr, n * per * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->LUt, n * per * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->rdiag_r, n * (size_t)s->N * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->piv_r, n * (size_t)s->N * sizeof(int));
+        if (e == cudaSuccess) e = ensure_slots(s, (size_t)sm_count());  // the evaluation hook's warps
+        if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor workspaces in global memory"));
+    }
     *out = s;
     return CB_OK;
 }
@@ -988,6 +1350,12 @@ int cb_reactors_destroy(cb_reactors* s) {
     cudaFree(s->D);
     cudaFree(s->J);
     cudaFree(s->counters);
+    cudaFree(s->d_tab_m);
+    cudaFree(s->ws);
+    cudaFree(s->LUr);
+    cudaFree(s->LUt);
+    cudaFree(s->rdiag_r);
+    cudaFree(s->piv_r);
     delete s;
     return CB_OK;
 }
@@ -1023,10 +1391,11 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     std::vector<Cand> cands;
     for (int tables = 1; tables >= 0; tables--)
         for (int w = 1; w <= 8; w++)
-            if (shape_fits(s, w, tables)) cands.push_back({w, tables});
+            if (shape_fits(s, w, tables) && (!s->global || (w & (w - 1)) == 0)) cands.push_back({w, tables});
     if (cands.empty()) return cbi::fail(CB_ERR_UNSUPPORTED, "no launch shape fits");
     // calibrate on copies of the state: a few slices of the first reactors, then restore the state
-    const size_t n_cal = std::min<size_t>(s->n, calib_reactors > 0 ? (size_t)calib_reactors : 4096);
+    const size_t n_def = s->global ? 512 : 4096;
+    const size_t n_cal = std::min<size_t>(s->n, calib_reactors > 0 ? (size_t)calib_reactors : n_def);
     const size_t hb = s->n * sizeof(Head), db = s->n * kDRows * (size_t)s->N * sizeof(double);
     std::vector<uint8_t> h0(hb), d0(db);
     BDF_CUDA(cudaMemcpy(h0.data(), s->head, hb, cudaMemcpyDeviceToHost));

@@ -287,7 +287,8 @@ namespace cbi {
 int fail(int code, const std::string& msg) { return ::fail(code, msg); }
 int cuda_fail(cudaError_t e, const char* what) { return ::cuda_fail(e, what); }
 MechView view(const cb_mech* m) {
-    return MechView{m->host.K, m->host.A, m->device, m->host.transport_ready ? 1 : 0, m->host.T0, &m->host.rates_blob};
+    return MechView{m->host.K, m->host.A, m->device, m->host.transport_ready ? 1 : 0, m->host.T0, &m->host.rates_blob,
+                    &m->host.rates_mixed_blob};
 }
 int transport_gather(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
                      const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st) {

@@ -18,7 +18,8 @@ struct MechView {
     int K, A, device;
     int transport_ready;
     double T0;
-    const std::vector<uint8_t>* rates_blob;  // host copy of the rates tables
+    const std::vector<uint8_t>* rates_blob;        // host copy of the rates tables
+    const std::vector<uint8_t>* rates_mixed_blob;  // host copy of the mixed-precision rates tables
 };
 MechView view(const cb_mech* m);
 

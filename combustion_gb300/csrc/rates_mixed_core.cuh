@@ -1,0 +1,143 @@
+// Mixed-precision rate of progress of one reaction (reaction.rs:113-309 with FP32 Arrhenius exponentials,
+// third-body sums and falloff blending; FP64 equilibrium constant, forward-minus-reverse rate and the
+// product with the forward coefficient), shared by the per-cell kernels (kernels_mixed.cu) and the
+// batched reactors' mixed right-hand side (bdf.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "device_math.cuh"
+#include "tables_mixed.h"
+
+namespace cbg {
+
+struct RatesMixedTables {
+    const RatesMixedHeader* H;
+    const SpeciesF* species;
+    const ReactionF* reactions;
+    const FalloffF* falloff;
+    const float* eff;
+    __device__ explicit RatesMixedTables(const uint8_t* tab)
+        : H(reinterpret_cast<const RatesMixedHeader*>(tab + kMathBytes)),
+          species(reinterpret_cast<const SpeciesF*>(tab + H->off_species)),
+          reactions(reinterpret_cast<const ReactionF*>(tab + H->off_reactions)),
+          falloff(reinterpret_cast<const FalloffF*>(tab + H->off_falloff)),
+          eff(reinterpret_cast<const float*>(tab + H->off_eff)) {}
+};
+
+__device__ __forceinline__ int piece_of_m(double split, double T) {
+    return __double_as_longlong(T) <= __double_as_longlong(split) ? 0 : 1;
+}
+
+// min(f32::MAX, k) of reaction.rs:138 with k = exp(b lnT - Ea/T + ln A) evaluated in FP32.
+__device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, float rcpT) {
+    if (!a.has_x) return min_pos(kF32Max, a.A);
+    return min_pos(kF32Max, exp_f32x(fmaf(a.b, lnT, fmaf(a.mEa, rcpT, a.lnA))));
+}
+
+__device__ __forceinline__ double conc_product_m(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
+    double p = C[ks[0]];
+#pragma unroll 1
+    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+#pragma unroll 1
+    for (int q = 1; q < n; q++)
+#pragma unroll 1
+        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
+    return p;
+}
+
+__device__ __forceinline__ double int_to_double_small(int v) {
+    if (v == 0) return 0.0;
+    const unsigned a = v < 0 ? (unsigned)(-v) : (unsigned)v;
+    const int e = 31 - __clz(a);
+    const unsigned long long mant = (unsigned long long)(a ^ (1u << e)) << (52 - e);
+    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
+}
+
+// cR of one reaction. MODEL is a compile-time constant (reactions are grouped by model), so no
+// predicated FP64 instruction of another model's branch is executed.
+// CellT: any cell view with C, ex, exn (FP64, indexable), Mf (FP32 third-body sums), C0, rcpC0,
+// rcpC0sq and the FP32 temperatures Ctotf, Tf, lnTf, rcpTf (one thread's cell here, one warp's cell in
+// the batched reactors).
+template <int MODEL, class CellT>
+__device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, const ReactionF& x, const CellT& c) {
+    const RatesMixedHeader& H = *tb.H;
+    double kf;  // forward rate coefficient including third body and falloff
+    if constexpr (MODEL == 4) {  // Troe, blending in FP32 (reaction.rs:160-193)
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double Md = flt_to_dbl(c.Mf[x.eff_row]);
+        double Pr, kinf;
+        if (f.flags & kKinfConst) {
+            Pr = Md * k0;
+            kinf = f.ainf;
+        } else {
+            const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+            Pr = (Md * k0) * rcp64(ki + kF32MinPos);
+            kinf = f.ainf * ki;
+        }
+        float lnF;
+        if (f.flags & kFcentConst) {
+            lnF = f.ln_fcent;
+        } else {
+            float F = 0.f;
+            if (f.flags & kTermT3) F = f.c1mA * expf(c.Tf * f.c3);
+            if (f.flags & kTermT1) F += f.cA * expf(c.Tf * f.c1);
+            if (f.flags & kTermAConst) F += f.cA;
+            if (f.flags & kTermT2) F += expf(f.cmT2 * c.rcpTf);
+            lnF = logf(F);
+        }
+        const float Cc = fmaf(-0.67f, lnF, -H.ln10_04);
+        const float Nn = fmaf(-1.27f, lnF, H.ln10_075);
+        const float lnPrC = log_dbl_f32(Pr + kF32MinPos) + Cc;
+        const float f1 = __fdividef(lnPrC, fmaf(-0.14f, lnPrC, Nn));
+        const float Fb = expf(__fdividef(lnF, fmaf(f1, f1, 1.f)));
+        kf = (flt_to_dbl(Fb) * kinf) * (Pr * rcp64(Pr + 1.0));
+    } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double Ck0 = flt_to_dbl(c.Mf[x.eff_row]) * arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+        kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
+    } else if constexpr (MODEL == 5) {  // SRI (reaction.rs:194-203, commented formula), blending in FP32
+        const FalloffF& f = tb.falloff[x.falloff];
+        const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+        const double Pr = (flt_to_dbl(c.Mf[x.eff_row]) * k0) * rcp64(ki + kF32MinPos);
+        const float lP = log_dbl_f32(Pr + kF32MinPos);
+        float base = expf(f.smrC * c.Tf);
+        if (f.sri_flags & kSriA) base = fmaf(f.sA, expf(f.smB * c.rcpTf), base);
+        float F = expf(__fdividef(logf(base), fmaf(lP, lP, 1.f)));
+        if (f.sri_flags & kSriD) F *= f.sD;
+        if (f.sri_flags & kSriE) F *= expf(f.sE * c.lnTf);
+        kf = (flt_to_dbl(F) * ki) * (Pr * rcp64(Pr + 1.0));
+    } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
+        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf) * flt_to_dbl(c.Mf[x.eff_row]);
+    } else {
+        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf);
+    }
+    // FP64 rate of progress (reaction.rs:269-306).
+    const double Rf = conc_product_m(c.C, x.r_k, x.r_n, x.n_r);
+    double Rnet = Rf;
+    if constexpr (MODEL != 1) {
+        const int nu0 = x.net_n[0];
+        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
+        double p = t0;
+#pragma unroll 1
+        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
+#pragma unroll 1
+        for (int q = 1; q < x.n_net; q++) {
+            const int nu = x.net_n[q], k = x.net_k[q];
+            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
+#pragma unroll 1
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
+        }
+        const int msn = x.minus_sigma_net;  // (P0/RT)^(-sum nu) chosen by integer selects
+        p *= msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
+        Rnet = fma(-p, conc_product_m(c.C, x.p_k, x.p_n, x.n_p), Rf);
+    }
+    return kf * Rnet;
+}
+
+}  // namespace cbg

@@ -17,7 +17,13 @@ from .synthetic import R, uniform
 
 class cb_bdf_options(C.Structure):
     _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("t_end", C.c_double), ("max_steps", C.c_int32),
-                ("slice_steps", C.c_int32), ("warps_per_block", C.c_int32), ("tables_in_shared", C.c_int32)]
+                ("slice_steps", C.c_int32), ("warps_per_block", C.c_int32), ("tables_in_shared", C.c_int32),
+                ("flags", C.c_int32)]
+
+
+MIXED_RHS = 1  # CB_BDF_MIXED_RHS: first Newton iteration per step on the mixed-precision f; the rest FP64
+REUSE_LU = 2   # CB_BDF_REUSE_LU: keep the factorisation while h / gamma_q changes by at most 30 %
+GLOBAL_MEMORY = 4  # CB_BDF_GLOBAL_MEMORY: workspaces in global memory even when they fit in shared memory
 
 
 class cb_reactor_stats(C.Structure):
@@ -91,11 +97,11 @@ class Reactors:
     """A batch of reactors on the current CUDA device."""
 
     def __init__(self, mech: Mechanism, n: int, rtol=1e-6, atol=1e-12, t_end=1e-3, max_steps=200000,
-                 slice_steps=0, warps_per_block=0, tables_in_shared=-1):
+                 slice_steps=0, warps_per_block=0, tables_in_shared=-1, flags=0):
         L = _bind()
         self.mech, self.n = mech, n
         self.N = mech.A + 2
-        o = cb_bdf_options(rtol, atol, t_end, max_steps, slice_steps, warps_per_block, tables_in_shared)
+        o = cb_bdf_options(rtol, atol, t_end, max_steps, slice_steps, warps_per_block, tables_in_shared, flags)
         h = C.c_void_p()
         _check(L.cb_reactors_create(mech.h, n, C.byref(o), C.byref(h)))
         self.h = h

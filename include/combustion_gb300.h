@@ -257,7 +257,9 @@ int cb_yaml_free(cb_yaml_mech* mech);
 /* ---- Batched constant-pressure reactors (variable-order BDF) ----------------------------------------
  * Replaces the reactor loop of plot.rs:32-118 with the cvode crate's role (cvode/lib.rs:17-47: BDF,
  * dense Newton): state u = [T, V, n_0 .. n_{A-1}] at fixed P/R, du/dt = the outputs of cb_rates_f64 for
- * that state (reaction.rs:356-391). Needs every non-bulk species active (A = K - 1) and K <= 65.
+ * that state (reaction.rs:356-391). Needs every non-bulk species active (A = K - 1). Up to 65 species a
+ * reactor's workspace sits in shared memory; above, in global memory (24 (K + 1)^2 bytes per reactor
+ * for its Jacobian and factorisation, plus about 0.6 MB per reactor in flight at 250 species).
  * Every reactor is integrated from t = 0 to t_end with its own step size and order (1-5) against
  * atol + rtol |u_i| for every component; its ignition delay is the time of the largest dT/dt (the
  * vertex of a parabola through the samples around it). The host side is synchronous. */
@@ -269,7 +271,22 @@ typedef struct cb_bdf_options {
     int32_t slice_steps;        /* steps per reactor per kernel launch (0: 256) */
     int32_t warps_per_block;    /* reactors in flight per block (0: autotuned) */
     int32_t tables_in_shared;   /* 1: mechanism tables in shared memory, 0: through L1, -1: autotuned */
+    int32_t flags;              /* CB_BDF_* below (0: FP64 right-hand side, factorisation at every change) */
 } cb_bdf_options;
+/* The first Newton iteration of every step (the correction from the predictor) evaluates f(u) by the
+ * mixed-precision rates program (FP32 Arrhenius, third-body and falloff terms; FP64 equilibrium
+ * constants, rates of progress and accumulation); the later iterations, which decide convergence (the
+ * FP64 Newton correction), the initial step's f, the Jacobian and the factorisation stay FP64. Newton on
+ * the mixed f alone cannot meet an absolute tolerance below its rounding noise. */
+#define CB_BDF_MIXED_RHS 1u
+/* Keep the factorisation of I - c J while c = h / gamma_q stays within 30 % of the factorised value and
+ * for at most 20 steps (the Newton correction is then scaled by 2 / (1 + c / c_lu), as in CVODE); the
+ * factorisation also carries over between launches when it lives in global memory. */
+#define CB_BDF_REUSE_LU 2u
+/* Workspaces and factorisations in global memory even when one reactor's fit in shared memory (they go
+ * there by themselves for large mechanisms; without CB_BDF_REUSE_LU the integration takes the same
+ * steps either way). */
+#define CB_BDF_GLOBAL_MEMORY 4u
 typedef struct cb_reactor_stats {
     uint64_t steps, rhs_evals, jacobians, factorizations, newton_failures, error_failures;
     uint64_t finished, failed;

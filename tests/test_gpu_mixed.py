@@ -13,7 +13,7 @@ from mechanisms import branch_mechanism, cells_for, sri_mechanism
 
 pytestmark = pytest.mark.gpu
 NTHREADS = os.cpu_count() or 4
-MIXED_TOL = 1e-4
+MIXED_TOL = util.MIXED_TOL
 
 
 def _setup(m):

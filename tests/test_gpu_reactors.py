@@ -99,3 +99,83 @@ def test_autotune_graph_replays_and_tolerance_convergence():
     rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
     print("ignition delay vs rtol 1e-10: max rel diff %.2e, median %.2e" % (rel.max(), np.median(rel)))
     assert np.median(rel) <= 1e-3 and rel.max() <= 5e-3
+
+
+def test_global_memory_workspaces_match_shared_memory():
+    """CB_BDF_GLOBAL_MEMORY, the placement large mechanisms get by themselves: the factorisation by
+    panels (the same FMAs in the same order), the solves on its transpose and the workspaces in global
+    memory take the shared-memory path's steps (53 species, 64 reactors, 64-step launches); the two
+    kernels are compiled apart, so values may differ in the last bits."""
+    from combustion_gb300 import reactors as RX
+    n = 64
+    kw = dict(slice_steps=64, warps_per_block=2, tables_in_shared=0)
+    m, mech, R, state = _setup("k53", n, **kw)
+    st = R.integrate()
+    res = R.results()
+    Rg = RX.Reactors(mech, n, flags=RX.GLOBAL_MEMORY, **kw)
+    Rg.set_state(*state)
+    stg = Rg.integrate()
+    resg = Rg.results()
+    print(st, stg, sep="\n")
+    assert st["finished"] == n and stg["finished"] == n and st["slices"] >= 8
+    for key in ("steps", "rhs_evals", "jacobians", "factorizations"):
+        assert st[key] == stg[key], key
+    assert np.max(np.abs(res["ignition_delay"] / resg["ignition_delay"] - 1)) <= 1e-9
+    assert np.max(np.abs(res["state"] - resg["state"]) / (np.abs(res["state"]) + 1e-12)) <= 1e-9
+
+
+@pytest.mark.parametrize("flags", ["mixed", "reuse", "mixed+reuse"])
+def test_mixed_rhs_and_kept_factorisations(flags):
+    """Ignition delays with the mixed-precision first Newton iterations, the kept factorisations, or
+    both, within 0.1 % of the FP64 integration (53 species, 256 reactors); the mixed f(u) itself within
+    the mixed form's bar of the FP64 oracle (condition-scaled)."""
+    from combustion_gb300 import reactors as RX
+    from combustion_gb300 import synthetic
+    bits = {"mixed": RX.MIXED_RHS, "reuse": RX.REUSE_LU, "mixed+reuse": RX.MIXED_RHS | RX.REUSE_LU}[flags]
+    n = 256
+    m, mech, R, state = _setup("k53", n)
+    st = R.integrate()
+    ref = R.results()
+    Rv = RX.Reactors(mech, n, flags=bits)
+    Rv.set_state(*state)
+    stv = Rv.integrate()
+    res = Rv.results()
+    print(st, stv, sep="\n")
+    assert stv["finished"] == n
+    rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
+    dT = np.abs(res["state"][0] - ref["state"][0]) / ref["state"][0]
+    print(f"{flags}: ignition delay rel diff max {rel.max():.2e} median {np.median(rel):.2e}; final T {dT.max():.2e}; "
+          f"factorisations {stv['factorizations']} vs {st['factorizations']}, rhs {stv['rhs_evals']} vs {st['rhs_evals']}")
+    assert rel.max() <= 1e-3 and dT.max() <= 1e-5
+    if bits & RX.REUSE_LU:
+        assert stv["factorizations"] < st["factorizations"]
+    if bits & RX.MIXED_RHS:
+        o = oracle.Oracle(m)
+        cells = synthetic.generate_cells(m.K, 16, "k53", seed=5)
+        Y = np.vstack([cells.temperature, cells.volume, cells.amounts]).T.copy()
+        f, _ = Rv.eval(cells.pressure_R, Y)
+        ref_f, sc = o.rates(o.rates_inputs(cells), scale=True)
+        err = util.cond_err(f.T, ref_f, sc)
+        print("mixed du/dt max cond err %.2e" % err.max())
+        assert err.max() <= util.MIXED_TOL
+
+
+def test_large_mechanism_reactors():
+    """250 species (251 states): the iteration matrix leaves shared memory, so workspaces and
+    factorisations go to global memory by themselves; the mixed-precision first Newton iterations with
+    kept factorisations (the large configuration's form) against the FP64 integration: ignition delays
+    within 0.1 %."""
+    from combustion_gb300 import reactors as RX
+    n = 32
+    m, mech, R, state = _setup("k250", n)
+    st = R.integrate()
+    ref = R.results()
+    Rv = RX.Reactors(mech, n, flags=RX.MIXED_RHS | RX.REUSE_LU)
+    Rv.set_state(*state)
+    stv = Rv.integrate()
+    res = Rv.results()
+    print(st, stv, sep="\n")
+    assert st["finished"] == n and stv["finished"] == n
+    rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
+    print(f"k250 mixed+reuse: ignition delay rel diff max {rel.max():.2e} median {np.median(rel):.2e}")
+    assert rel.max() <= 1e-3
