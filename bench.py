@@ -280,8 +280,9 @@ def run_reactors(args, rank):
 def run_large(args):
     """The large-mechanism configuration (K = 250, R = 1,500; opt-in with --large): plain FP64 and mixed
     rates+transport on 2^20 device-generated cells, the width-512 surrogate (252 -> 512 x 4 -> 252) trained
-    on 2^23 plain-kernel cells and run gated on the same cells. Reactors at K = 250 are not supported
-    (their iteration matrix exceeds shared memory)."""
+    on 2^23 plain-kernel cells and run gated on the same cells, and args.large_reactors constant-pressure
+    reactors of the 250-species reactor variant to 1 ms (workspaces in global memory), in the mixed form
+    (mixed-precision first Newton iterations, kept factorisations) and in plain FP64."""
     import torch
     import combustion_gb300 as cb
     import oracle
@@ -346,9 +347,43 @@ def run_large(args):
                             "training": {"cells": 1 << 23, "steps": args.large_steps, "generate_s": gen_s,
                                          "train_s": train_s, "loss_last": float(np.mean(losses[-20:]))},
                             "error_network_vs_plain_f64": rel_err_groups(s_out, t_out), "gate": st},
-        "reactors": "not supported at K = 250 (iteration matrix beyond shared memory)",
+        "reactors": large_reactors(args) if args.large_reactors > 0 else None,
         "errors": "condition-scaled against the FP64 oracle on 256 sampled cells",
     }
+
+
+def large_reactors(args):
+    """args.large_reactors reactors of the 250-species reactor variant (251 states), rtol 1e-6 / atol
+    1e-12 to 1 ms: the large configuration's form (CB_BDF_MIXED_RHS | CB_BDF_REUSE_LU) and plain FP64,
+    each autotuned, with the ignition-delay difference between the two."""
+    import combustion_gb300 as cb
+    from combustion_gb300 import reactors as RX
+    from combustion_gb300 import synthetic
+    m = synthetic.generate_reactor_mechanism("k250")
+    mech = cb.Mechanism(m)
+    n = args.large_reactors
+    state = RX.initial_states(m.K, n, seed=4)
+    out = {"workload": "%d constant-pressure reactors, 250-species reactor variant of the generator, "
+                       "T0~U[1000,1600] K, P log-uniform [1,40] atm, phi~U[0.5,2] in 79%% diluent, to 1 ms, "
+                       "rtol 1e-6, atol 1e-12" % n}
+    res = {}
+    for name, flags in (("mixed_reuse", RX.MIXED_RHS | RX.REUSE_LU), ("plain_f64", 0)):
+        R = RX.Reactors(mech, n, rtol=1e-6, atol=1e-12, t_end=1e-3, flags=flags)
+        R.set_state(*state)
+        tune = R.autotune(0)
+        st = R.integrate()
+        res[name] = R.results()
+        out[name] = {"reactors_per_s": n / (st["ms"] * 1e-3), "ms": st["ms"], "steps": st["steps"],
+                     "rhs_evals": st["rhs_evals"], "factorizations": st["factorizations"],
+                     "jacobians": st["jacobians"], "finished": st["finished"], "failed": st["failed"],
+                     "warps_per_block": tune["warps_per_block"]}
+        R.close()
+    ok = (res["plain_f64"]["status"] == 2) & (res["mixed_reuse"]["status"] == 2)
+    a, b = res["mixed_reuse"]["ignition_delay"][ok], res["plain_f64"]["ignition_delay"][ok]
+    rel = np.abs(a - b) / b
+    out["ignition_delay_mixed_vs_plain"] = {"reactors": int(ok.sum()), "max_rel": float(rel.max()) if rel.size else None,
+                                            "median_rel": float(np.median(rel)) if rel.size else None}
+    return out
 
 
 def run_ours(args):
@@ -564,6 +599,7 @@ def main():
     ap.add_argument("--reactors", type=int, default=16384)
     ap.add_argument("--large", action="store_true", help="also run the K = 250 configuration")
     ap.add_argument("--large-steps", type=int, default=1500)
+    ap.add_argument("--large-reactors", type=int, default=4096, help="K = 250 reactors in --large (0: none)")
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
     ap.add_argument("--sur-steps", type=int, default=6000)
     ap.add_argument("--sur-batch", type=int, default=65536)
