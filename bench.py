@@ -282,7 +282,7 @@ def run_large(args):
     rates+transport on 2^20 device-generated cells, the width-512 surrogate (252 -> 512 x 4 -> 252) trained
     on 2^23 plain-kernel cells and run gated on the same cells, and args.large_reactors constant-pressure
     reactors of the 250-species reactor variant to 1 ms (workspaces in global memory), in the mixed form
-    (mixed-precision first Newton iterations, kept factorisations) and in plain FP64."""
+    (mixed-precision first Newton iterations, FP32 factorisation, kept factorisations) and in plain FP64."""
     import torch
     import combustion_gb300 as cb
     import oracle
@@ -354,8 +354,9 @@ def run_large(args):
 
 def large_reactors(args):
     """args.large_reactors reactors of the 250-species reactor variant (251 states), rtol 1e-6 / atol
-    1e-12 to 1 ms: the large configuration's form (CB_BDF_MIXED_RHS | CB_BDF_REUSE_LU) and plain FP64,
-    each autotuned, with the ignition-delay difference between the two."""
+    1e-12 to 1 ms: the large configuration's form (mixed-precision first Newton iterations, FP32
+    factorisation with FP64 residuals and corrections, kept factorisations), the FP32 factorisation alone,
+    and plain FP64, each autotuned, with the ignition-delay differences from plain FP64."""
     import combustion_gb300 as cb
     from combustion_gb300 import reactors as RX
     from combustion_gb300 import synthetic
@@ -367,7 +368,8 @@ def large_reactors(args):
                        "T0~U[1000,1600] K, P log-uniform [1,40] atm, phi~U[0.5,2] in 79%% diluent, to 1 ms, "
                        "rtol 1e-6, atol 1e-12" % n}
     res = {}
-    for name, flags in (("mixed_reuse", RX.MIXED_RHS | RX.REUSE_LU), ("plain_f64", 0)):
+    for name, flags in (("mixed_lu32_reuse", RX.MIXED_RHS | RX.LU32 | RX.REUSE_LU), ("lu32", RX.LU32),
+                        ("plain_f64", 0)):
         R = RX.Reactors(mech, n, rtol=1e-6, atol=1e-12, t_end=1e-3, flags=flags)
         R.set_state(*state)
         tune = R.autotune(0)
@@ -378,11 +380,13 @@ def large_reactors(args):
                      "jacobians": st["jacobians"], "finished": st["finished"], "failed": st["failed"],
                      "warps_per_block": tune["warps_per_block"]}
         R.close()
-    ok = (res["plain_f64"]["status"] == 2) & (res["mixed_reuse"]["status"] == 2)
-    a, b = res["mixed_reuse"]["ignition_delay"][ok], res["plain_f64"]["ignition_delay"][ok]
-    rel = np.abs(a - b) / b
-    out["ignition_delay_mixed_vs_plain"] = {"reactors": int(ok.sum()), "max_rel": float(rel.max()) if rel.size else None,
-                                            "median_rel": float(np.median(rel)) if rel.size else None}
+    for name in ("mixed_lu32_reuse", "lu32"):
+        ok = (res["plain_f64"]["status"] == 2) & (res[name]["status"] == 2)
+        a, b = res[name]["ignition_delay"][ok], res["plain_f64"]["ignition_delay"][ok]
+        rel = np.abs(a - b) / b
+        out[name]["ignition_delay_vs_plain_f64"] = {"reactors": int(ok.sum()),
+                                                    "max_rel": float(rel.max()) if rel.size else None,
+                                                    "median_rel": float(np.median(rel)) if rel.size else None}
     return out
 
 

@@ -86,7 +86,7 @@ struct Params {
     double* eval_f;
     double* eval_J;
     const uint8_t* tab_m;  // mixed-precision rates tables (global memory): f(u) with CB_BDF_MIXED_RHS
-    int mixed, reuse_lu;
+    int mixed, reuse_lu, lu32;
     // Large states: per-warp workspaces in global memory (null: in shared memory), and per reactor its
     // factorisation [n][N][LD], the factors' transpose (coalesced triangular solves), pivots, 1 / U_kk.
     uint8_t* ws_global;
@@ -400,12 +400,11 @@ __device__ __forceinline__ double deriv_product(const double* C, const uint16_t*
     return p;
 }
 
-// Jacobian of du/dt at y into w.LU (rows of LD), also stored to Jg [N][N]; w.f receives f(y).
+// Jacobian of du/dt at y into Jm (N rows of LD), also stored to Jg [N][N]; w.f receives f(y).
 __device__ void jacobian_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
-                              double* Jg, int lane) {
+                              double* Jg, double* Jm, int lane) {
     const int K = p.K, A = p.A, N = p.N, LD = p.LD;
     const RhsOut o = rhs_warp<true>(p, m, w, pR, rP, y, w.f, lane);
-    double* Jm = w.LU;
     // species rows: G[k][j] = d wdot_k / d C_j (bulk column kept in column 0 for now)
     for (int k = lane; k < A; k += 32) {
         double* row = Jm + (size_t)(2 + k) * LD;
@@ -559,15 +558,17 @@ __device__ void lu_solve_warp(const double* A, int N, int LD, const int* piv, co
 // row swap (whole rows), scaling and update of the panel's own columns go column by column; then the
 // panel's U rows right of it by forward substitution, and one rank-kPanel update of the trailing matrix,
 // which so is read and written once per panel instead of once per column. Every element receives the
-// same FMAs in the same order as in lu_warp.
-__device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdiag, int lane) {
+// same FMAs in the same order as in lu_warp. T = float: the FP32 factorisation of CB_BDF_LU32 (1 / U_kk
+// still stored as a double).
+template <class T>
+__device__ bool lu_warp_blocked(T* A, int N, int LD, int* piv, double* rdiag, int lane) {
     for (int kb = 0; kb < N; kb += kPanel) {
         const int ke = min(kb + kPanel, N);
         for (int k = kb; k < ke; k++) {
-            double best = -1.0;
+            T best = -1;
             int bi = k;
             for (int i = k + lane; i < N; i += 32) {
-                const double v = fabs(A[(size_t)i * LD + k]);
+                const T v = fabs(A[(size_t)i * LD + k]);
                 if (v > best) {
                     best = v;
                     bi = i;
@@ -575,7 +576,7 @@ __device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdia
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+                const T ov = __shfl_xor_sync(0xffffffffu, best, o);
                 const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ov > best || (ov == best && oi < bi)) {
                     best = ov;
@@ -584,20 +585,20 @@ __device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdia
             }
             best = __shfl_sync(0xffffffffu, best, 0);
             bi = __shfl_sync(0xffffffffu, bi, 0);
-            if (!(best > 0.0) || !(best < 1e300)) return false;
+            if (!(best > (T)0) || !(best < (sizeof(T) == 8 ? (T)1e300 : (T)1e38))) return false;
             if (lane == 0) piv[k] = bi;
             if (bi != k)
                 for (int j = lane; j < N; j += 32) {
-                    const double t = A[(size_t)k * LD + j];
+                    const T t = A[(size_t)k * LD + j];
                     A[(size_t)k * LD + j] = A[(size_t)bi * LD + j];
                     A[(size_t)bi * LD + j] = t;
                 }
             __syncwarp();
-            const double rp = 1.0 / A[(size_t)k * LD + k];
-            if (lane == 0) rdiag[k] = rp;
+            const T rp = (T)1 / A[(size_t)k * LD + k];
+            if (lane == 0) rdiag[k] = (double)rp;
             for (int i = k + 1 + lane; i < N; i += 32) {
-                double* Ai = A + (size_t)i * LD;
-                const double l = Ai[k] * rp;
+                T* Ai = A + (size_t)i * LD;
+                const T l = Ai[k] * rp;
                 Ai[k] = l;
                 for (int j = k + 1; j < ke; j++) Ai[j] = fma(-l, A[(size_t)k * LD + j], Ai[j]);
             }
@@ -607,11 +608,11 @@ __device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdia
         const int nb = ke - kb;
         // U rows of the panel, columns ke..N-1: forward substitution with the panel's unit lower L
         for (int j = ke + lane; j < N; j += 32) {
-            double u[kPanel];
+            T u[kPanel];
 #pragma unroll
             for (int r = 0; r < kPanel; r++) {
                 if (r < nb) {
-                    double a = A[(size_t)(kb + r) * LD + j];
+                    T a = A[(size_t)(kb + r) * LD + j];
 #pragma unroll
                     for (int t = 0; t < r; t++) a = fma(-A[(size_t)(kb + r) * LD + kb + t], u[t], a);
                     u[r] = a;
@@ -622,13 +623,13 @@ __device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdia
         __syncwarp();
         // trailing matrix: A[i][j] -= sum_t L[i][kb+t] U[kb+t][j], t in panel order
         for (int j = ke + lane; j < N; j += 32) {
-            double u[kPanel];
+            T u[kPanel];
 #pragma unroll
-            for (int t = 0; t < kPanel; t++) u[t] = t < nb ? A[(size_t)(kb + t) * LD + j] : 0.0;
+            for (int t = 0; t < kPanel; t++) u[t] = t < nb ? A[(size_t)(kb + t) * LD + j] : (T)0;
 #pragma unroll 2
             for (int i = ke; i < N; i++) {
-                const double* Li = A + (size_t)i * LD + kb;
-                double a = A[(size_t)i * LD + j];
+                const T* Li = A + (size_t)i * LD + kb;
+                T a = A[(size_t)i * LD + j];
 #pragma unroll
                 for (int t = 0; t < kPanel; t++)
                     if (t < nb) a = fma(-Li[t], u[t], a);
@@ -641,15 +642,18 @@ __device__ bool lu_warp_blocked(double* A, int N, int LD, int* piv, double* rdia
 }
 
 // At = A^T (both N x N with rows of LD), for the triangular solves below.
-__device__ void transpose_warp(const double* A, double* At, int N, int LD, int lane) {
+template <class T>
+__device__ void transpose_warp(const T* A, T* At, int N, int LD, int lane) {
     for (int i = 0; i < N; i++)
         for (int j = lane; j < N; j += 32) At[(size_t)j * LD + i] = A[(size_t)i * LD + j];
     __syncwarp();
 }
 
 // lu_solve_warp on the transposed factors: column k of L and U is row k of At, so every lane's reads of
-// one elimination step fall in one contiguous row (global-memory matrices). Same operations and order.
-__device__ void lu_solve_t_warp(const double* At, int N, int LD, const int* piv, const double* rdiag, double* b,
+// one elimination step fall in one contiguous row (global-memory matrices). Same operations and order;
+// with FP32 factors (T = float) the right-hand side and its updates stay FP64.
+template <class T>
+__device__ void lu_solve_t_warp(const T* At, int N, int LD, const int* piv, const double* rdiag, double* b,
                                 int lane) {
     if (lane == 0)
         for (int k = 0; k < N; k++) {
@@ -663,37 +667,50 @@ __device__ void lu_solve_t_warp(const double* At, int N, int LD, const int* piv,
     __syncwarp();
     for (int k = 0; k < N; k++) {
         const double bk = b[k];
-        const double* col = At + (size_t)k * LD;
-        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-col[i], bk, b[i]);
+        const T* col = At + (size_t)k * LD;
+        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-(double)col[i], bk, b[i]);
         __syncwarp();
     }
     for (int k = N - 1; k >= 0; k--) {
         const double bk = b[k] * rdiag[k];
         __syncwarp();
         if (lane == 0) b[k] = bk;
-        const double* col = At + (size_t)k * LD;
-        for (int i = lane; i < k; i += 32) b[i] = fma(-col[i], bk, b[i]);
+        const T* col = At + (size_t)k * LD;
+        for (int i = lane; i < k; i += 32) b[i] = fma(-(double)col[i], bk, b[i]);
         __syncwarp();
     }
 }
 
-// I - c J (J in w.LU already when `fresh`, else from global) factorised in w.LU; with per-reactor
-// factorisations in global memory (GLOBAL), by panels, and its transpose into `LUt` for the solves.
+// I - c J (J in LU already when `fresh`, else from global) factorised in LU (pivots, 1 / U_kk); with
+// per-reactor factorisations in global memory (GLOBAL), by panels, and its transpose into `LUt` for the
+// solves. With CB_BDF_LU32 (GLOBAL only) the factors are FP32 and both they and their transpose live in
+// LUt's bytes (LU stays the FP64 Jacobian scratch).
 template <bool GLOBAL>
-__device__ bool build_lu(const Params& p, const Work& w, const double* Jg, double c, bool fresh, double* LUt,
-                         int lane) {
+__device__ bool build_lu(const Params& p, double* LU, int* piv, double* rdiag, const double* Jg, double c, bool fresh,
+                         double* LUt, int lane) {
     const int N = p.N, LD = p.LD;
     for (int idx = lane; idx < N * N; idx += 32) {
         const int i = idx / N, j = idx % N;
-        const double Jij = fresh ? w.LU[(size_t)i * LD + j] : Jg[idx];
-        w.LU[(size_t)i * LD + j] = (i == j ? 1.0 : 0.0) - c * Jij;
+        const double Jij = fresh ? LU[(size_t)i * LD + j] : Jg[idx];
+        LU[(size_t)i * LD + j] = (i == j ? 1.0 : 0.0) - c * Jij;
     }
     __syncwarp();
     if constexpr (!GLOBAL) {
-        return lu_warp(w.LU, N, LD, w.piv, w.rdiag, lane);
+        return lu_warp(LU, N, LD, piv, rdiag, lane);
     } else {
-        if (!lu_warp_blocked(w.LU, N, LD, w.piv, w.rdiag, lane)) return false;
-        transpose_warp(w.LU, LUt, N, LD, lane);
+        if (p.lu32) {
+            float* F = reinterpret_cast<float*>(LUt);
+            for (int idx = lane; idx < N * N; idx += 32) {
+                const int i = idx / N, j = idx % N;
+                F[(size_t)i * LD + j] = (float)LU[(size_t)i * LD + j];
+            }
+            __syncwarp();
+            if (!lu_warp_blocked(F, N, LD, piv, rdiag, lane)) return false;
+            transpose_warp(F, F + (size_t)N * LD, N, LD, lane);
+            return true;
+        }
+        if (!lu_warp_blocked(LU, N, LD, piv, rdiag, lane)) return false;
+        transpose_warp(LU, LUt, N, LD, lane);
         return true;
     }
 }
@@ -748,7 +765,7 @@ __device__ __forceinline__ double gamma_k(int k) {  // sum_{i=1..k} 1/i
 
 // One reactor for at most `budget` steps (warp-uniform control flow). MIXED: the first Newton iteration
 // of each step on the mixed-precision f(u); GLOBAL: workspaces and per-reactor factorisations in global
-// memory (w.LU, w.piv, w.rdiag are the reactor's own).
+// memory.
 template <bool MIXED, bool GLOBAL>
 __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, int lane) {
     const int N = p.N;
@@ -757,10 +774,14 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
     double* Dg = p.D + (size_t)r * kDRows * N;
     double* Jg = p.J + (size_t)r * N * N;
     const double pR = p.pR[r], rP = 1.0 / pR;
+    // the factorisation: the warp's workspace, or (GLOBAL) the reactor's own with its transpose
+    double* LU = GLOBAL ? p.LUr + (size_t)r * N * p.LD : w.LU;
+    int* piv = GLOBAL ? p.piv_r + (size_t)r * N : w.piv;
+    double* rdiag = GLOBAL ? p.rdiag_r + (size_t)r * N : w.rdiag;
     double* LUt = GLOBAL ? p.LUt + (size_t)r * N * p.LD : nullptr;
     for (int i = lane; i < kDRows * N; i += 32) w.D[i] = Dg[i];
     __syncwarp();
-    // lu_have: w.LU holds the factorisation of I - c_lu J; lu_refresh: c changed since (a step size or
+    // lu_have: LU holds the factorisation of I - c_lu J; lu_refresh: c changed since (a step size or
     // order change), so it is made again before the next Newton iteration unless CB_BDF_REUSE_LU keeps
     // it. A launch starts with a fresh factorisation, except that with CB_BDF_REUSE_LU a reactor's own
     // (global memory) carries over.
@@ -769,7 +790,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
     bool lu_refresh = carry ? hd.lu_refresh != 0 : true;
     double c_lu = hd.c_lu;
     auto factorise = [&](double c, bool fresh) {
-        lu_have = build_lu<GLOBAL>(p, w, Jg, c, fresh, LUt, lane);
+        lu_have = build_lu<GLOBAL>(p, LU, piv, rdiag, Jg, c, fresh, LUt, lane);
         c_lu = c;
         lu_refresh = false;
         hd.lus++;
@@ -811,7 +832,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         hd.tp = 0.0;
         hd.gp = g0;
         hd.need_next = 1;
-        jacobian_warp(p, m, w, pR, rP, w.y, Jg, lane);
+        jacobian_warp(p, m, w, pR, rP, w.y, Jg, LU, lane);
         hd.jacs++;
         hd.rhs += 2;
         hd.jac_current = 1;
@@ -879,8 +900,16 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
                 }
                 if (!__all_sync(0xffffffffu, finite)) break;
                 __syncwarp();
-                if constexpr (GLOBAL) lu_solve_t_warp(LUt, N, p.LD, w.piv, w.rdiag, w.b, lane);
-                else lu_solve_warp(w.LU, N, p.LD, w.piv, w.rdiag, w.b, lane);
+                if constexpr (GLOBAL) {
+                    if (p.lu32) {
+                        const float* F = reinterpret_cast<const float*>(LUt);
+                        lu_solve_t_warp(F + (size_t)N * p.LD, N, p.LD, piv, rdiag, w.b, lane);
+                    } else {
+                        lu_solve_t_warp(LUt, N, p.LD, piv, rdiag, w.b, lane);
+                    }
+                } else {
+                    lu_solve_warp(LU, N, p.LD, piv, rdiag, w.b, lane);
+                }
                 if (corr != 1.0) {
                     for (int i = lane; i < N; i += 32) w.b[i] *= corr;
                     __syncwarp();
@@ -908,7 +937,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         if (!converged) {
             hd.newton_fail++;
             if (!hd.jac_current) {  // a fresh Jacobian at the predicted state, same step
-                jacobian_warp(p, m, w, pR, rP, w.ypred, Jg, lane);
+                jacobian_warp(p, m, w, pR, rP, w.ypred, Jg, LU, lane);
                 hd.jacs++;
                 hd.rhs += 2;
                 hd.jac_current = 1;
@@ -1031,7 +1060,7 @@ __device__ __forceinline__ uint8_t* workspace_of(const Params& p, int warp) {
 }
 
 template <bool MIXED, bool GLOBAL>
-__global__ void slice_kernel(const Params p) {
+__device__ __forceinline__ void slice_body(const Params& p) {
     __shared__ uint64_t bar;
     const uint8_t* tab = p.tab;
     if (p.smem_tables) {
@@ -1048,16 +1077,20 @@ __global__ void slice_kernel(const Params p) {
         if (lane == 0) r = atomicAdd(p.queue, 1);
         r = __shfl_sync(0xffffffffu, r, 0);
         if (r >= p.n) break;
-        if constexpr (GLOBAL) {  // the reactor's own factorisation
-            Work wr = w;
-            wr.LU = p.LUr + (size_t)r * p.N * p.LD;
-            wr.piv = p.piv_r + (size_t)r * p.N;
-            wr.rdiag = p.rdiag_r + (size_t)r * p.N;
-            integrate<MIXED, GLOBAL>(p, m, wr, r, lane);
-        } else {
-            integrate<MIXED, GLOBAL>(p, m, w, r, lane);
-        }
+        integrate<MIXED, GLOBAL>(p, m, w, r, lane);
     }
+}
+
+template <bool MIXED>
+__global__ void slice_kernel(const Params p) {
+    slice_body<MIXED, false>(p);
+}
+
+// Global-memory workspaces: at least two 256-thread blocks per SM (16 warps to hide the latency of
+// workspaces that live in L2 and HBM).
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 2) slice_kernel_global(const Params p) {
+    slice_body<MIXED, true>(p);
 }
 
 // Evaluation hook: f and J at given states, one warp per state.
@@ -1077,7 +1110,7 @@ __global__ void eval_kernel(const Params p, int count) {
     for (int s = blockIdx.x * (blockDim.x >> 5) + warp; s < count; s += gridDim.x * (blockDim.x >> 5)) {
         for (int i = lane; i < N; i += 32) w.y[i] = p.eval_y[(size_t)s * N + i];
         __syncwarp();
-        jacobian_warp(p, m, w, p.pR[s], 1.0 / p.pR[s], w.y, p.eval_J + (size_t)s * N * N, lane);
+        jacobian_warp(p, m, w, p.pR[s], 1.0 / p.pR[s], w.y, p.eval_J + (size_t)s * N * N, w.LU, lane);
         if (p.mixed) rhs_warp_mixed(p, m, RatesMixedTables(p.tab_m), w, p.pR[s], 1.0 / p.pR[s], w.y, w.f, lane);
         for (int i = lane; i < N; i += 32) p.eval_f[(size_t)s * N + i] = w.f[i];
         __syncwarp();
@@ -1180,6 +1213,7 @@ Params params(cb_reactors* s, int tables) {
     p.tab_m = s->d_tab_m;
     p.mixed = (s->opt.flags & CB_BDF_MIXED_RHS) ? 1 : 0;
     p.reuse_lu = (s->opt.flags & CB_BDF_REUSE_LU) ? 1 : 0;
+    p.lu32 = (s->global && (s->opt.flags & CB_BDF_LU32)) ? 1 : 0;
     if (s->global) {
         p.ws_global = s->ws;
         p.LUr = s->LUr;
@@ -1210,8 +1244,8 @@ cudaError_t ensure_slots(cb_reactors* s, size_t slots) {
 using SliceFn = void (*)(Params);
 SliceFn slice_fn(const cb_reactors* s) {
     const bool mixed = (s->opt.flags & CB_BDF_MIXED_RHS) != 0;
-    if (s->global) return mixed ? slice_kernel<true, true> : slice_kernel<false, true>;
-    return mixed ? slice_kernel<true, false> : slice_kernel<false, false>;
+    if (s->global) return mixed ? slice_kernel_global<true> : slice_kernel_global<false>;
+    return mixed ? slice_kernel<true> : slice_kernel<false>;
 }
 
 // Shared-memory limit and grid of a launch shape (outside any stream capture).
@@ -1259,7 +1293,7 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     if (v.A != v.K - 1)
         return cbi::fail(CB_ERR_UNSUPPORTED, "reactors need every non-bulk species active (inert non-bulk species "
                                              "would be parameters, not state)");
-    if (opt->flags & ~(CB_BDF_MIXED_RHS | CB_BDF_REUSE_LU | CB_BDF_GLOBAL_MEMORY))
+    if (opt->flags & ~(CB_BDF_MIXED_RHS | CB_BDF_REUSE_LU | CB_BDF_GLOBAL_MEMORY | CB_BDF_LU32))
         return cbi::fail(CB_ERR_INVALID, "unknown integrator flag");
     cb_reactors* s = new cb_reactors();
     s->mech = mech;

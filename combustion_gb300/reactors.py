@@ -24,6 +24,7 @@ class cb_bdf_options(C.Structure):
 MIXED_RHS = 1  # CB_BDF_MIXED_RHS: first Newton iteration per step on the mixed-precision f; the rest FP64
 REUSE_LU = 2   # CB_BDF_REUSE_LU: keep the factorisation while h / gamma_q changes by at most 30 %
 GLOBAL_MEMORY = 4  # CB_BDF_GLOBAL_MEMORY: workspaces in global memory even when they fit in shared memory
+LU32 = 8  # CB_BDF_LU32: FP32 factorisation (global-memory workspaces); residuals and corrections FP64
 
 
 class cb_reactor_stats(C.Structure):

@@ -287,6 +287,11 @@ typedef struct cb_bdf_options {
  * there by themselves for large mechanisms; without CB_BDF_REUSE_LU the integration takes the same
  * steps either way). */
 #define CB_BDF_GLOBAL_MEMORY 4u
+/* With workspaces in global memory: factorise I - c J in FP32 (the FP32 pipe is many times the FP64 one
+ * on this GPU). The Newton residuals, corrections and triangular-solve accumulations stay FP64, so a
+ * converged step meets the same tolerances; only the convergence rate depends on the factorisation's
+ * accuracy. Ignored when the workspaces are in shared memory. */
+#define CB_BDF_LU32 8u
 typedef struct cb_reactor_stats {
     uint64_t steps, rhs_evals, jacobians, factorizations, newton_failures, error_failures;
     uint64_t finished, failed;

@@ -126,14 +126,16 @@ def test_global_memory_workspaces_match_shared_memory():
     assert np.max(np.abs(res["state"] - resg["state"]) / (1e-12 + 1e-6 * np.abs(res["state"]))) <= 5e-2
 
 
-@pytest.mark.parametrize("flags", ["mixed", "reuse", "mixed+reuse"])
+@pytest.mark.parametrize("flags", ["mixed", "reuse", "mixed+reuse", "lu32"])
 def test_mixed_rhs_and_kept_factorisations(flags):
-    """Ignition delays with the mixed-precision first Newton iterations, the kept factorisations, or
-    both, within 0.1 % of the FP64 integration (53 species, 256 reactors); the mixed f(u) itself within
-    the mixed form's bar of the FP64 oracle (condition-scaled)."""
+    """Ignition delays with the mixed-precision first Newton iterations, the kept factorisations, both,
+    or the FP32 factorisation (global-memory placement), within 0.1 % of the FP64 integration (53
+    species, 256 reactors); the mixed f(u) itself within the mixed form's bar of the FP64 oracle
+    (condition-scaled)."""
     from combustion_gb300 import reactors as RX
     from combustion_gb300 import synthetic
-    bits = {"mixed": RX.MIXED_RHS, "reuse": RX.REUSE_LU, "mixed+reuse": RX.MIXED_RHS | RX.REUSE_LU}[flags]
+    bits = {"mixed": RX.MIXED_RHS, "reuse": RX.REUSE_LU, "mixed+reuse": RX.MIXED_RHS | RX.REUSE_LU,
+            "lu32": RX.GLOBAL_MEMORY | RX.LU32}[flags]
     n = 256
     m, mech, R, state = _setup("k53", n)
     st = R.integrate()
@@ -165,19 +167,22 @@ def test_mixed_rhs_and_kept_factorisations(flags):
 def test_large_mechanism_reactors():
     """250 species (251 states): the iteration matrix leaves shared memory, so workspaces and
     factorisations go to global memory by themselves; the mixed-precision first Newton iterations with
-    kept factorisations (the large configuration's form) against the FP64 integration: ignition delays
-    within 0.1 %."""
+    kept factorisations, with FP64 or FP32 factors (the large configuration's form), against the FP64
+    integration: ignition delays within 0.1 %."""
     from combustion_gb300 import reactors as RX
     n = 32
     m, mech, R, state = _setup("k250", n)
     st = R.integrate()
     ref = R.results()
-    Rv = RX.Reactors(mech, n, flags=RX.MIXED_RHS | RX.REUSE_LU)
-    Rv.set_state(*state)
-    stv = Rv.integrate()
-    res = Rv.results()
-    print(st, stv, sep="\n")
-    assert st["finished"] == n and stv["finished"] == n
-    rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
-    print(f"k250 mixed+reuse: ignition delay rel diff max {rel.max():.2e} median {np.median(rel):.2e}")
-    assert rel.max() <= 1e-3
+    assert st["finished"] == n
+    for name, bits in (("mixed+reuse", RX.MIXED_RHS | RX.REUSE_LU),
+                       ("mixed+reuse+lu32", RX.MIXED_RHS | RX.REUSE_LU | RX.LU32)):
+        Rv = RX.Reactors(mech, n, flags=bits)
+        Rv.set_state(*state)
+        stv = Rv.integrate()
+        res = Rv.results()
+        print(st, stv, sep="\n")
+        assert stv["finished"] == n
+        rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
+        print(f"k250 {name}: ignition delay rel diff max {rel.max():.2e} median {np.median(rel):.2e}")
+        assert rel.max() <= 1e-3
