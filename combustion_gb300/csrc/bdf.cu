@@ -335,8 +335,7 @@ __device__ void rhs_warp_mixed(const Params& p, const Mech& m, const RatesMixedT
             if (sp.need_exp | sp.need_exp_neg) {
                 const double* g = sp.g[pc];
                 const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
-                if (sp.need_exp) w.ex[k] = min_pos(H.M3, exp64(x));
-                if (sp.need_exp_neg) w.exn[k] = min_pos(H.cbrt_max, exp64(-x));
+                gibbs_exps(x, sp.need_exp, sp.need_exp_neg, H.M3, H.cbrt_max, c.C0, c.rcpC0, w.ex[k], w.exn[k]);
             }
         }
     }

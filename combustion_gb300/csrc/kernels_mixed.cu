@@ -74,8 +74,7 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
         if (!(s.need_exp | s.need_exp_neg)) continue;
         const double* g = s.g[piece_of_m(s.split, T)];
         const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
-        if (s.need_exp) c.ex[k] = min_pos(H.M3, exp64(x));
-        if (s.need_exp_neg) c.exn[k] = min_pos(H.cbrt_max, exp64(-x));
+        gibbs_exps(x, s.need_exp, s.need_exp_neg, H.M3, H.cbrt_max, c.C0, c.rcpC0, c.ex[k], c.exn[k]);
     }
     // FP32 third-body sums, four rows per pass.
     for (int e0 = 0; e0 < H.n_eff; e0 += 4) {

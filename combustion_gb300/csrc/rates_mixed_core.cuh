@@ -58,7 +58,19 @@ __device__ __forceinline__ double int_to_double_small(int v) {
 
 // cR of one reaction. MODEL is a compile-time constant (reactions are grouped by model), so no
 // predicated FP64 instruction of another model's branch is executed.
-// CellT: any cell view with C, ex, exn (FP64, indexable), Mf (FP32 third-body sums), C0, rcpC0,
+// The cached Gibbs exponentials of the mixed program for exponent x (reaction.rs:234-263), with the
+// standard-state factor of the equilibrium constant folded in: ex = min(M3, e^x) RT/P0 and
+// exn = min(cbrt(f32::MAX), e^-x) P0/RT, so that a reaction's product of |nu| factors per net species
+// carries (P0/RT)^(-sum nu) without a multiply per reaction; e^-x is the FP64 reciprocal of e^x (3 FP64
+// operations instead of an exponential's 9; its zero and infinity meet the same clamps).
+__device__ __forceinline__ void gibbs_exps(double x, bool need_exp, bool need_exp_neg, double M3, double cbrt_max,
+                                           double C0, double rcpC0, double& ex, double& exn) {
+    const double e = exp64(x);
+    if (need_exp) ex = min_pos(M3, e) * rcpC0;
+    if (need_exp_neg) exn = min_pos(cbrt_max, rcp64(e)) * C0;
+}
+
+// CellT: any cell view with C, ex, exn (FP64, indexable, from gibbs_exps), Mf (FP32 third-body sums), C0, rcpC0,
 // rcpC0sq and the FP32 temperatures Ctotf, Tf, lnTf, rcpTf (one thread's cell here, one warp's cell in
 // the batched reactors).
 template <int MODEL, class CellT>
@@ -133,8 +145,7 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
 #pragma unroll 1
             for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
         }
-        const int msn = x.minus_sigma_net;  // (P0/RT)^(-sum nu) chosen by integer selects
-        p *= msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
+        // (P0/RT)^(-sum nu) is folded into the cell's exponentials (gibbs_exps), one factor per use
         Rnet = fma(-p, conc_product_m(c.C, x.p_k, x.p_n, x.n_p), Rf);
     }
     return kf * Rnet;
