@@ -9,6 +9,7 @@
 #include <cuda_bf16.h>
 
 #include "device_common.cuh"
+#include "device_math.cuh"
 #include "surrogate_kernels.cuh"
 #include "umma.cuh"
 
@@ -457,13 +458,15 @@ __device__ __forceinline__ int ordered(float f) {
 }
 
 // Network inputs of one cell (rates layout): log(T/T0), log(P / 1 atm), mole fractions X_0 .. X_{K-1}
-// with the bulk fraction from the total amount (P/R V) / T like the transport kernel's.
-__device__ __forceinline__ float raw_feature(const FeatureArgs& a, size_t c, int j, double logT, double logP,
-                                             double rN, double bulk) {
-    if (j == 0) return (float)logT;
-    if (j == 1) return (float)logP;
+// with the bulk fraction from the total amount (P/R V) / T like the transport kernel's. FP32 throughout
+// (the inputs converted with integer instructions): the features end as BF16, and FP64 arithmetic here
+// would make the kernel FP64-pipe bound.
+__device__ __forceinline__ float raw_feature(const FeatureArgs& a, size_t c, int j, float logT, float logP,
+                                             float rN, float bulk) {
+    if (j == 0) return logT;
+    if (j == 1) return logP;
     const int k = j - 2;
-    return (float)((k < a.K - 1 ? a.in[4 + k][c] : bulk) * rN);
+    return (k < a.K - 1 ? dbl_to_flt(a.in[4 + k][c]) : bulk) * rN;
 }
 
 __global__ void features_kernel(const FeatureArgs a) {
@@ -484,13 +487,13 @@ __global__ void features_kernel(const FeatureArgs a) {
                 for (int j = 0; j < a.n_in; j++) a.XT[(size_t)j * a.ldXT + a.row0 + c] = __float2bfloat16_rn(0.f);
             continue;
         }
-        const double pR = a.uniform_pressure ? a.in[0][0] : a.in[0][c];
-        const double T = a.in[2][c], V = a.in[3][c];
-        const double N = pR * V / T;
-        double s = 0.0;
-        for (int k = 0; k < a.K - 1; k++) s += a.in[4 + k][c];
-        const double bulk = N - s, rN = 1.0 / N;
-        const double logT = log(T / a.T0), logP = log(pR * a.R_over_P0);
+        const float pR = dbl_to_flt(a.uniform_pressure ? a.in[0][0] : a.in[0][c]);
+        const float T = dbl_to_flt(a.in[2][c]), V = dbl_to_flt(a.in[3][c]);
+        const float N = pR * V / T;
+        float s = 0.f;
+        for (int k = 0; k < a.K - 1; k++) s += dbl_to_flt(a.in[4 + k][c]);
+        const float bulk = N - s, rN = 1.f / N;
+        const float logT = logf(T / (float)a.T0), logP = logf(pR * (float)a.R_over_P0);
         bool inside = true;
         for (int j0 = 0; j0 < a.n_in; j0 += 8) {
             float x[8];
