@@ -59,9 +59,11 @@ struct Head {
     double t, h;
     double ign_t, ign_g, ta, ga, tc, gc, tp, gp;  // max dT/dt, its neighbours, the previous sample
     double c_lu;                                  // c of the factorisation kept between launches
+    double peak_t, peak_x;                        // largest mole fraction of the peak species, its time
     int q, n_equal, state, jac_current;
     int steps, rhs, jacs, lus, newton_fail, err_fail, need_next, since_lu;
     int lu_have, lu_refresh;  // a kept factorisation exists; c changed since it was made
+    int next_out, pad_out;    // next trajectory point to write
 };
 
 struct Params {
@@ -94,7 +96,14 @@ struct Params {
     double* LUt;
     double* rdiag_r;
     int* piv_r;
+    // Outputs (cb_reactors_set_outputs): states at n_points uniform times [n][n_points][N] (null: none),
+    // and the state where species peak_k's mole fraction among the active species peaks [n][N] (k < 0:
+    // none).
+    double* traj;
+    int n_points, peak_k;
+    double* peak_state;
 };
+
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -105,6 +114,44 @@ __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// After an accepted step to t_new of size h at order q (backward differences D at t_new): the
+// trajectory points in (t_new - h, t_new] from the interpolating polynomial through the last q + 1
+// points (Newton's backward-difference form, y(t) = sum_j D_j prod_{m<j} (t - t_new + m h) / ((m+1) h),
+// the dense output of the BDF method), and the peak of the chosen species' mole fraction.
+__device__ void record_outputs(const Params& p, Head& hd, int r, const double* D, double t_new, double h, int q,
+                               int lane) {
+    const int N = p.N;
+    if (p.traj) {
+        const double dt = p.t_end / (p.n_points - 1);
+        while (hd.next_out < p.n_points) {
+            const double tj = hd.next_out == p.n_points - 1 ? p.t_end : hd.next_out * dt;
+            if (tj > t_new) break;
+            double* out = p.traj + ((size_t)r * p.n_points + hd.next_out) * N;
+            for (int i = lane; i < N; i += 32) {
+                double y = D[i], pj = 1.0;
+                for (int j = 1; j <= q; j++) {
+                    pj *= (tj - t_new + (j - 1) * h) / (j * h);
+                    y = fma(D[(size_t)j * N + i], pj, y);
+                }
+                out[i] = y;
+            }
+            hd.next_out++;
+        }
+    }
+    if (p.peak_k >= 0) {  // mole fraction among the active species (the reference's plotted fractions)
+        double s = 0.0;
+        for (int i = 2 + lane; i < N; i += 32) s += D[i];
+        s = warp_sum(s);
+        const double x = D[2 + p.peak_k] / s;
+        if (x > hd.peak_x) {
+            hd.peak_x = x;
+            hd.peak_t = t_new;
+            for (int i = lane; i < N; i += 32) p.peak_state[(size_t)r * N + i] = D[i];
+        }
+    }
+    __syncwarp();
 }
 
 // Concentrations, Gibbs exponentials and third-body sums in shared memory, viewed as a rates "cell".
@@ -831,6 +878,9 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         hd.tp = 0.0;
         hd.gp = g0;
         hd.need_next = 1;
+        hd.next_out = 0;
+        hd.peak_x = -1.0;
+        record_outputs(p, hd, r, w.D, 0.0, h, 0, lane);  // the initial state: trajectory point 0
         jacobian_warp(p, m, w, pR, rP, w.y, Jg, LU, lane);
         hd.jacs++;
         hd.rhs += 2;
@@ -979,6 +1029,7 @@ __device__ void integrate(const Params& p, const Mech& m, const Work& w, int r, 
         }
         __syncwarp();
         hd.n_equal++;
+        if (p.traj || p.peak_k >= 0) record_outputs(p, hd, r, w.D, t_new, h, q, lane);
         // dT/dt at the new point from the backward differences: h y' = sum_{j=1..q} D_j / j
         double g = 0.0;
         for (int j = 1; j <= q; j++) g += w.D[(size_t)j * N] / j;
@@ -1147,6 +1198,10 @@ struct cb_reactors {
     size_t ws_slots = 0;
     double *LUr = nullptr, *LUt = nullptr, *rdiag_r = nullptr;
     int* piv_r = nullptr;
+    // cb_reactors_set_outputs: trajectory [n][n_points][N] and the peak species' state [n][N]
+    double* traj = nullptr;
+    int n_points = 0, peak_k = -1;
+    double* peak_state = nullptr;
 };
 
 namespace {
@@ -1211,6 +1266,10 @@ Params params(cb_reactors* s, int tables) {
     p.done = s->counters + 1;
     p.status = s->counters + 2;
     p.tab_m = s->d_tab_m;
+    p.traj = s->traj;
+    p.n_points = s->n_points;
+    p.peak_k = s->peak_k;
+    p.peak_state = s->peak_state;
     p.mixed = (s->opt.flags & CB_BDF_MIXED_RHS) ? 1 : 0;
     p.reuse_lu = (s->opt.flags & CB_BDF_REUSE_LU) ? 1 : 0;
     p.lu32 = (s->global && (s->opt.flags & CB_BDF_LU32)) ? 1 : 0;
@@ -1390,6 +1449,8 @@ int cb_reactors_destroy(cb_reactors* s) {
     cudaFree(s->LUt);
     cudaFree(s->rdiag_r);
     cudaFree(s->piv_r);
+    cudaFree(s->traj);
+    cudaFree(s->peak_state);
     delete s;
     return CB_OK;
 }
@@ -1412,7 +1473,70 @@ int cb_reactors_set_state(cb_reactors* s, const double* pressure_R, const double
     BDF_CUDA(cudaMemcpy(s->pR, pressure_R, n * sizeof(double), cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->head, 0, n * sizeof(Head)));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
+    // outputs not reached (a reactor that fails) read as NaN (all bits set)
+    if (s->traj) BDF_CUDA(cudaMemset(s->traj, 0xff, n * (size_t)s->n_points * N * sizeof(double)));
+    if (s->peak_state) BDF_CUDA(cudaMemset(s->peak_state, 0xff, n * (size_t)N * sizeof(double)));
     s->have_state = true;
+    return CB_OK;
+}
+
+int cb_reactors_set_outputs(cb_reactors* s, int32_t n_points, int32_t peak_species) {
+    if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
+    if (n_points == 1 || n_points < 0) return cbi::fail(CB_ERR_INVALID, "n_points must be 0 (none) or at least 2");
+    if (peak_species < -1 || peak_species >= s->A) return cbi::fail(CB_ERR_INVALID, "peak species out of range");
+    BDF_CUDA(cudaSetDevice(s->device));
+    BDF_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(s->traj);
+    cudaFree(s->peak_state);
+    s->traj = nullptr;
+    s->peak_state = nullptr;
+    s->n_points = 0;
+    s->peak_k = -1;
+    const size_t N = (size_t)s->N;
+    if (n_points) {
+        BDF_CUDA(cudaMalloc(&s->traj, s->n * (size_t)n_points * N * sizeof(double)));
+        BDF_CUDA(cudaMemset(s->traj, 0xff, s->n * (size_t)n_points * N * sizeof(double)));
+        s->n_points = n_points;
+    }
+    if (peak_species >= 0) {
+        BDF_CUDA(cudaMalloc(&s->peak_state, s->n * N * sizeof(double)));
+        BDF_CUDA(cudaMemset(s->peak_state, 0xff, s->n * N * sizeof(double)));
+        s->peak_k = peak_species;
+    }
+    return CB_OK;
+}
+
+int cb_reactors_outputs(cb_reactors* s, double* times, double* trajectory, double* peak_time, double* peak_fraction,
+                        double* peak_state) {
+    if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
+    if ((times || trajectory) && !s->traj) return cbi::fail(CB_ERR_NOT_READY, "no trajectory requested");
+    if ((peak_time || peak_fraction || peak_state) && s->peak_k < 0)
+        return cbi::fail(CB_ERR_NOT_READY, "no peak species requested");
+    BDF_CUDA(cudaSetDevice(s->device));
+    const size_t n = s->n, N = (size_t)s->N, P = (size_t)s->n_points;
+    if (times)
+        for (size_t j = 0; j < P; j++) times[j] = j == P - 1 ? s->opt.t_end : (double)j * (s->opt.t_end / (P - 1));
+    if (trajectory) {  // device [n][P][N] -> host [P][N][n]
+        std::vector<double> h(n * P * N);
+        BDF_CUDA(cudaMemcpy(h.data(), s->traj, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < n; r++)
+            for (size_t j = 0; j < P; j++)
+                for (size_t i = 0; i < N; i++) trajectory[(j * N + i) * n + r] = h[(r * P + j) * N + i];
+    }
+    if (peak_time || peak_fraction) {
+        std::vector<Head> h(n);
+        BDF_CUDA(cudaMemcpy(h.data(), s->head, n * sizeof(Head), cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < n; r++) {
+            if (peak_time) peak_time[r] = h[r].peak_x >= 0.0 ? h[r].peak_t : NAN;
+            if (peak_fraction) peak_fraction[r] = h[r].peak_x >= 0.0 ? h[r].peak_x : NAN;
+        }
+    }
+    if (peak_state) {  // device [n][N] -> host [N][n]
+        std::vector<double> h(n * N);
+        BDF_CUDA(cudaMemcpy(h.data(), s->peak_state, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (size_t r = 0; r < n; r++)
+            for (size_t i = 0; i < N; i++) peak_state[i * n + r] = h[r * N + i];
+    }
     return CB_OK;
 }
 
@@ -1436,6 +1560,10 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     BDF_CUDA(cudaMemcpy(d0.data(), s->D, db, cudaMemcpyDeviceToHost));
     const size_t n_save = s->n;
     const int steps_save = s->opt.slice_steps;
+    double* const traj_save = s->traj;  // calibration slices write no outputs
+    const int peak_save = s->peak_k;
+    s->traj = nullptr;
+    s->peak_k = -1;
     s->n = n_cal;
     s->opt.slice_steps = 16;
     double best = 1e300;
@@ -1474,6 +1602,8 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     cudaEventDestroy(b);
     s->n = n_save;
     s->opt.slice_steps = steps_save;
+    s->traj = traj_save;
+    s->peak_k = peak_save;
     BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));

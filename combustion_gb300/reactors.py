@@ -68,6 +68,8 @@ def _bind():
         L.cb_reactors_integrate.argtypes = [vp, C.POINTER(cb_reactor_stats)]
         L.cb_reactors_results.argtypes = [vp, vp, vp, vp, vp]
         L.cb_reactors_eval.argtypes = [vp, C.c_int32, vp, vp, vp, vp]
+        L.cb_reactors_set_outputs.argtypes = [vp, C.c_int32, C.c_int32]
+        L.cb_reactors_outputs.argtypes = [vp, vp, vp, vp, vp, vp]
         _bound = True
     return L
 
@@ -138,6 +140,28 @@ class Reactors:
         _check(lib().cb_reactors_results(self.h, ign.ctypes.data, state.ctypes.data, status.ctypes.data,
                                          steps.ctypes.data))
         return {"ignition_delay": ign, "state": state, "status": status, "steps": steps}
+
+    def set_outputs(self, n_points=0, peak_species=-1):
+        """Trajectory points (uniform times over [0, t_end]) and the peak of one active species' mole
+        fraction, recorded by the following integrations (the role of plot.rs:76-138)."""
+        _check(lib().cb_reactors_set_outputs(self.h, n_points, peak_species))
+        self.n_points, self.peak_species = n_points, peak_species
+
+    def outputs(self):
+        """{times [P], trajectory [P, N, n], peak_time [n], peak_fraction [n], peak_state [N, n]} (the
+        entries that were requested)."""
+        P, n, N = getattr(self, "n_points", 0), self.n, self.N
+        out = {}
+        t = traj = pt = pf = ps = None
+        if P:
+            t, traj = np.zeros(P), np.zeros((P, N, n))
+            out.update(times=t, trajectory=traj)
+        if getattr(self, "peak_species", -1) >= 0:
+            pt, pf, ps = np.zeros(n), np.zeros(n), np.zeros((N, n))
+            out.update(peak_time=pt, peak_fraction=pf, peak_state=ps)
+        ptr = lambda a: None if a is None else a.ctypes.data
+        _check(lib().cb_reactors_outputs(self.h, ptr(t), ptr(traj), ptr(pt), ptr(pf), ptr(ps)))
+        return out
 
     def eval(self, pressure_R, states):
         """(f [m, N], J [m, N, N]) of the integrator at the given states [m, N]."""

@@ -316,6 +316,17 @@ int cb_reactors_integrate(cb_reactors* batch, cb_reactor_stats* stats);
  * status [n] (2 done, 3 step size underflow, 4 step limit, 1 unfinished), accepted steps [n]. */
 int cb_reactors_results(cb_reactors* batch, double* ignition_delay, double* state, int32_t* status,
                         int32_t* steps);
+/* Outputs of the following integrations, headless (the role of plot.rs:76-138, which samples the state
+ * at uniform times and reports where the OH mole fraction peaks): n_points states per reactor at
+ * t_j = j t_end / (n_points - 1), from the integrator's interpolating polynomial (0: none, else >= 2),
+ * and for active species peak_species (-1: none) the largest mole fraction among the active species
+ * over the accepted steps, its time and the state there. Allocates device memory; call before
+ * cb_reactors_integrate (cb_reactors_set_state resets the outputs). */
+int cb_reactors_set_outputs(cb_reactors* batch, int32_t n_points, int32_t peak_species);
+/* Host arrays, any may be NULL: times [n_points], trajectory [n_points][A+2][n], peak_time [n],
+ * peak_fraction [n], peak_state [A+2][n]. Points a failed reactor did not reach are NaN. */
+int cb_reactors_outputs(cb_reactors* batch, double* times, double* trajectory, double* peak_time,
+                        double* peak_fraction, double* peak_state);
 /* The integrator's du/dt and Jacobian at m given states (host): pressure_R [m], states [m][A+2] ->
  * f [m][A+2], J [m][A+2][A+2] (row i: d f_i / d u_j). Synchronous. */
 int cb_reactors_eval(cb_reactors* batch, int32_t m, const double* pressure_R, const double* states, double* f,

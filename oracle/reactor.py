@@ -37,6 +37,19 @@ def ignition_time(t, g):
     return float(t[i])
 
 
+def trajectory(o, pressure_R, y0, t_end, times, peak_species, rtol=1e-9, atol=1e-14):
+    """States at `times` (dense output) and, over the accepted steps, the largest mole fraction among the
+    active species of `peak_species` with its time: the CPU check of the GPU integrator's outputs."""
+    from scipy.integrate import solve_ivp
+    sol = solve_ivp(lambda t, y: rhs(o, pressure_R, y), (0.0, t_end), np.asarray(y0, dtype=np.float64),
+                    method="BDF", rtol=rtol, atol=atol, dense_output=True)
+    if sol.status != 0:
+        raise RuntimeError(sol.message)
+    x = sol.y[2 + peak_species] / sol.y[2:].sum(axis=0)
+    i = int(np.argmax(x))
+    return sol.sol(np.asarray(times)), float(sol.t[i]), float(x[i])
+
+
 def integrate(o, pressure_R, y0, t_end, rtol=1e-9, atol=1e-14):
     """(ignition delay, final state, number of steps) of one reactor."""
     from scipy.integrate import solve_ivp

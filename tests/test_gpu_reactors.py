@@ -186,3 +186,39 @@ def test_large_mechanism_reactors():
         rel = np.abs(res["ignition_delay"] - ref["ignition_delay"]) / ref["ignition_delay"]
         print(f"k250 {name}: ignition delay rel diff max {rel.max():.2e} median {np.median(rel):.2e}")
         assert rel.max() <= 1e-3
+
+
+def test_trajectory_and_species_peak_against_cpu_bdf():
+    """Headless trajectory and species peak (the role of plot.rs:76-138): 21 states per reactor at
+    uniform times from the integrator's interpolating polynomial against scipy's BDF dense output on the
+    oracle at rtol 1e-9 (temperature within 1e-4, amounts within 1e-3 of each species' largest amount);
+    the first and last points equal to the initial and final states; the largest mole fraction of one
+    species among the active ones within 1 % of the CPU integration's, the state there consistent with
+    it and no trajectory sample above it."""
+    n, P, k_peak = 6, 21, 3
+    m, mech, R, (pR, T, V, am) = _setup("k10", n, rtol=1e-6, atol=1e-12, t_end=1e-3)
+    R.set_outputs(P, k_peak)
+    st = R.integrate()
+    res = R.results()
+    out = R.outputs()
+    assert st["finished"] == n
+    traj, times = out["trajectory"], out["times"]
+    assert traj.shape == (P, m.K + 1, n) and times[0] == 0.0 and times[-1] == 1e-3
+    y0 = np.vstack([T, V, am])
+    assert np.array_equal(traj[0], y0)
+    assert np.array_equal(traj[-1], res["state"])
+    ps, pf = out["peak_state"], out["peak_fraction"]
+    assert np.allclose(ps[2 + k_peak] / ps[2:].sum(axis=0), pf, rtol=1e-12, atol=0)
+    x_samples = traj[:, 2 + k_peak, :] / traj[:, 2:, :].sum(axis=1)
+    assert np.all(x_samples.max(axis=0) <= pf * (1 + 1e-3))
+    o = oracle.Oracle(m)
+    for i in range(n):
+        Y, t_pk, x_pk = reactor.trajectory(o, pR[i], y0[:, i], 1e-3, times, k_peak)
+        g = traj[:, :, i].T
+        relT = float(np.max(np.abs(g[0] - Y[0]) / Y[0]))
+        scale = np.abs(Y[2:]).max(axis=1, keepdims=True)
+        rel_n = float(np.max(np.abs(g[2:] - Y[2:]) / (1e-3 * scale + 1e-30)))
+        print(f"  reactor {i}: T max rel {relT:.1e}, amounts {rel_n * 1e-3:.1e} of max; peak x {pf[i]:.6e} at "
+              f"{out['peak_time'][i]:.4e} s, CPU {x_pk:.6e} at {t_pk:.4e} s")
+        assert relT <= 1e-4 and rel_n <= 1.0
+        assert abs(pf[i] - x_pk) <= 1e-2 * x_pk
