@@ -550,6 +550,12 @@ def run_ours(args):
         o.fused(ins, nthreads=threads)
         cpu = {"value": ns / (time.perf_counter() - t), "unit": "cells/s", "cores": threads, "kind": "port",
                "sample": f"first {ns} cells of the benchmark batch, fused rates+transport, {threads} threads"}
+        # one thread, as the reference's own CPU path runs (a per-state loop on one thread)
+        n1 = max(1024, ns // 16)
+        t = time.perf_counter()
+        o.fused([a[:n1] for a in ins], nthreads=1)
+        cpu["single_thread"] = {"value": n1 / (time.perf_counter() - t), "unit": "cells/s",
+                                "sample": f"first {n1} cells, 1 thread"}
 
     if rank == 0:
         clk = clocks.summary()
