@@ -5,11 +5,14 @@
 
 namespace cbg {
 
-// Threads per block. The rates tables (94 KB at K = 53) fit twice per SM: 2 x 256 threads give four
-// warps per SM sub-partition to hide the latency of the thread-local arrays. The transport tables
-// (135 KB) fit once, so that kernel runs 256-thread blocks as well.
-constexpr int kBlock = 256;
-constexpr int kTransportBlock = 256;
+// Threads per block: one 768-thread block per SM. Each block stages its own copy of the tables in
+// shared memory, which shares the SM's 256 KB with the L1 cache that holds the thread-local arrays
+// (concentrations, Gibbs exponentials, accumulators). One copy per SM instead of two or three leaves L1
+// that room: measured at K = 53, 2^22 cells, the mixed rates kernel 54.2 -> 38.1 ms (three 256-thread
+// blocks before; 1024-thread blocks 45.5 ms), the plain rates kernel 119.6 -> 117.0 ms, transport the
+// same or slightly faster.
+constexpr int kBlock = 768;
+constexpr int kTransportBlock = 768;
 
 // One pointer per input / output array (struct of arrays), passed by value as a kernel parameter.
 template <int KMAX>
