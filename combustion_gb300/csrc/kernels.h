@@ -5,14 +5,17 @@
 
 namespace cbg {
 
-// Threads per block: one 768-thread block per SM. Each block stages its own copy of the tables in
-// shared memory, which shares the SM's 256 KB with the L1 cache that holds the thread-local arrays
-// (concentrations, Gibbs exponentials, accumulators). One copy per SM instead of two or three leaves L1
-// that room: measured at K = 53, 2^22 cells, the mixed rates kernel 54.2 -> 38.1 ms (three 256-thread
-// blocks before; 1024-thread blocks 45.5 ms), the plain rates kernel 119.6 -> 117.0 ms, transport the
-// same or slightly faster.
+// Threads per block. Each block stages its own copy of the tables in shared memory, which shares the
+// SM's 256 KB with the L1 cache that holds the thread-local arrays (concentrations, Gibbs exponentials,
+// accumulators); 768-thread blocks keep one or two copies per SM instead of two or three and leave L1
+// that room: measured at K = 53, 2^22 cells, the mixed rates kernel 54.2 -> 38.1 ms (256-thread blocks
+// before; 1024-thread blocks 45.5 ms), the plain rates kernel 119.6 -> 117.0 ms, mixed transport
+// 1 ms faster. Plain transport (tables of 135 KB, one block per SM) keeps 256 threads: 768 ran no
+// faster (the FP64 pipe is 97 % busy either way) and its per-thread arrays then spilled past L1 into
+// DRAM (24 KB per cell instead of 2 KB).
 constexpr int kBlock = 768;
-constexpr int kTransportBlock = 768;
+constexpr int kTransportBlock = 256;
+constexpr int kTransportMixedBlock = 768;
 
 // One pointer per input / output array (struct of arrays), passed by value as a kernel parameter.
 template <int KMAX>

@@ -244,7 +244,7 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
 }
 
 template <int KMAX, bool SMEM>
-__global__ void __launch_bounds__(kTransportBlock) transport_mixed_kernel(const uint8_t* __restrict__ gtab,
+__global__ void __launch_bounds__(kTransportMixedBlock) transport_mixed_kernel(const uint8_t* __restrict__ gtab,
                                                                          uint32_t tab_bytes,
                                                                          const __grid_constant__ TransportArgs<KMAX> io,
                                                                          size_t n, int* status) {
@@ -308,7 +308,7 @@ cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_
         }                                                                                                  \
     }
 CB_DISPATCH_M(launch_rates_mixed, rates_mixed_kernel, RatesArgs, kBlock)
-CB_DISPATCH_M(launch_transport_mixed, transport_mixed_kernel, TransportArgs, kTransportBlock)
+CB_DISPATCH_M(launch_transport_mixed, transport_mixed_kernel, TransportArgs, kTransportMixedBlock)
 #undef CB_DISPATCH_M
 
 #define CB_WAVE_M(FN, KERNEL, BLOCK)                                                        \
@@ -321,7 +321,7 @@ CB_DISPATCH_M(launch_transport_mixed, transport_mixed_kernel, TransportArgs, kTr
         }                                                                                   \
     }
 CB_WAVE_M(wave_rates_mixed, rates_mixed_kernel, kBlock)
-CB_WAVE_M(wave_transport_mixed, transport_mixed_kernel, kTransportBlock)
+CB_WAVE_M(wave_transport_mixed, transport_mixed_kernel, kTransportMixedBlock)
 #undef CB_WAVE_M
 
 }  // namespace cbg
