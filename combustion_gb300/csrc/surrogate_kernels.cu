@@ -458,15 +458,21 @@ __device__ __forceinline__ int ordered(float f) {
 }
 
 // Network inputs of one cell (rates layout): log(T/T0), log(P / 1 atm), mole fractions X_0 .. X_{K-1}
-// with the bulk fraction from the total amount (P/R V) / T like the transport kernel's. FP32 throughout
-// (the inputs converted with integer instructions): the features end as BF16, and FP64 arithmetic here
-// would make the kernel FP64-pipe bound.
+// with the bulk fraction from the total amount N = (P/R V) / T like the transport kernel's. FP32
+// throughout (the inputs converted with integer instructions): the features end as BF16, and FP64
+// arithmetic here would make the kernel FP64-pipe bound. Features come in order, so `s` accumulates the
+// amounts read so far and the bulk (the last feature) is N - s: every input is read once.
 __device__ __forceinline__ float raw_feature(const FeatureArgs& a, size_t c, int j, float logT, float logP,
-                                             float rN, float bulk) {
+                                             float N, float rN, float& s) {
     if (j == 0) return logT;
     if (j == 1) return logP;
     const int k = j - 2;
-    return (k < a.K - 1 ? dbl_to_flt(a.in[4 + k][c]) : bulk) * rN;
+    if (k < a.K - 1) {
+        const float x = dbl_to_flt(a.in[4 + k][c]);
+        s += x;
+        return x * rN;
+    }
+    return (N - s) * rN;
 }
 
 __global__ void features_kernel(const FeatureArgs a) {
@@ -489,10 +495,8 @@ __global__ void features_kernel(const FeatureArgs a) {
         }
         const float pR = dbl_to_flt(a.uniform_pressure ? a.in[0][0] : a.in[0][c]);
         const float T = dbl_to_flt(a.in[2][c]), V = dbl_to_flt(a.in[3][c]);
-        const float N = pR * V / T;
+        const float N = pR * V / T, rN = 1.f / N;
         float s = 0.f;
-        for (int k = 0; k < a.K - 1; k++) s += dbl_to_flt(a.in[4 + k][c]);
-        const float bulk = N - s, rN = 1.f / N;
         const float logT = logf(T / (float)a.T0), logP = logf(pR * (float)a.R_over_P0);
         bool inside = true;
         for (int j0 = 0; j0 < a.n_in; j0 += 8) {
@@ -502,7 +506,7 @@ __global__ void features_kernel(const FeatureArgs a) {
                 const int j = j0 + h;
                 float f = 0.f;
                 if (j < a.n_feat) {
-                    f = raw_feature(a, c, j, logT, logP, rN, bulk);
+                    f = raw_feature(a, c, j, logT, logP, N, rN, s);
                     if (a.raw) a.raw[c * a.n_feat + j] = f;
                     if (a.lo) inside &= (f >= a.lo[j]) & (f <= a.hi[j]);
                     if (hull) {
