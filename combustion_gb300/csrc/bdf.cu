@@ -452,10 +452,20 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     std::vector<uint8_t> h0(hb), d0(db);
     BDF_CUDA(cudaMemcpy(h0.data(), s->head, hb, cudaMemcpyDeviceToHost));
     BDF_CUDA(cudaMemcpy(d0.data(), s->D, db, cudaMemcpyDeviceToHost));
-    const size_t n_save = s->n;
-    const int steps_save = s->opt.slice_steps;
-    double* const traj_save = s->traj;  // calibration slices write no outputs
-    const int peak_save = s->peak_k;
+    // the calibration runs the first n_cal reactors in 16-step slices and writes no outputs; the batch's
+    // own settings come back on every path out of this function
+    struct Restore {
+        cb_reactors* s;
+        size_t n;
+        int steps, peak;
+        double* traj;
+        ~Restore() {
+            s->n = n;
+            s->opt.slice_steps = steps;
+            s->traj = traj;
+            s->peak_k = peak;
+        }
+    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj};
     s->traj = nullptr;
     s->peak_k = -1;
     s->n = n_cal;
@@ -494,10 +504,10 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    s->n = n_save;
-    s->opt.slice_steps = steps_save;
-    s->traj = traj_save;
-    s->peak_k = peak_save;
+    s->n = restore.n;
+    s->opt.slice_steps = restore.steps;
+    s->traj = restore.traj;
+    s->peak_k = restore.peak;
     BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
