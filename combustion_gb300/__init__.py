@@ -94,6 +94,7 @@ def lib():
         L.cb_rates_transport_f64.argtypes = [vp, sz, vp, vp, vp, C.c_uint32, vp]
         L.cb_rates_transport_mixed.argtypes = [vp, sz, vp, vp, vp, C.c_uint32, vp]
         L.cb_work_model.argtypes = [vp, C.POINTER(cb_work), C.POINTER(cb_work)]
+        L.cb_count_nonfinite.argtypes = [vp, sz, C.c_int32, vp, C.POINTER(C.c_uint64), C.c_uint32, vp]
         L.cb_synchronize.argtypes = [vp, vp]
         L.cb_last_error.restype = C.c_char_p
         L.cb_version.restype = C.c_char_p
@@ -258,6 +259,15 @@ class Mechanism:
         """inputs [K+1]: sum n, T/T0, n_0..n_{K-2}; outputs [K+2]: lambda/lambda0, mu/mu0, rhoD_k/mu0."""
         fn = lib().cb_transport_mixed if mixed else lib().cb_transport_f64
         return self._call(fn, inputs, outputs, 0, stream)
+
+    def count_nonfinite(self, arrays, stream=None):
+        """Number of NaN or infinite values in the rows of `arrays` (device tensors or host arrays)."""
+        rows, n = self._rows(arrays)
+        flags = CB_HOST_MEMORY if self._is_host(arrays) else 0
+        c = C.c_uint64()
+        _check(lib().cb_count_nonfinite(self.h, n, len(rows), _ptr_array(rows), C.byref(c), flags,
+                                        None if flags else self._stream(stream)))
+        return int(c.value)
 
     def rates_transport(self, inputs, rates_out, transport_out, stream=None, mixed=False):
         """Both paths on the same cells (transport at sum n = P/R V / T, T/T0)."""

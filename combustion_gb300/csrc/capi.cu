@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -22,6 +23,7 @@ struct cb_mech {
     uint8_t* d_rates_mixed = nullptr;      // tables of the mixed-precision form
     uint8_t* d_transport_mixed = nullptr;
     int* d_status = nullptr;         // kernel status bits
+    unsigned long long* d_count = nullptr;  // cb_count_nonfinite's device counter
     // Device staging for CB_HOST_MEMORY calls: two slots, each holding one chunk of inputs and outputs;
     // streams for host->device copies, kernels and device->host copies, and per-slot events.
     double* d_stage = nullptr;
@@ -326,6 +328,7 @@ int cb_mech_create(const cb_mech_desc* desc, cb_mech** out) {
         e = cudaMemcpy(m->d_rates_mixed, m->host.rates_mixed_blob.data(), m->host.rates_mixed_blob.size(),
                        cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&m->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_count, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(m->d_status, 0, sizeof(int));
     if (e != cudaSuccess) { cb_mech_destroy(m); return cuda_fail(e, "mechanism upload"); }
     *out = m;
@@ -361,6 +364,34 @@ int cb_transport_fit(const cb_mech_desc* desc, double T0, double* cond, double* 
     return CB_OK;
 }
 
+int cb_count_nonfinite(cb_mech* m, size_t n, int32_t n_arrays, const double* const* arrays, uint64_t* count,
+                       uint32_t flags, void* stream) {
+    if (!m || !arrays || !count || n_arrays < 0) return fail(CB_ERR_INVALID, "bad argument");
+    if (flags & ~CB_HOST_MEMORY) return fail(CB_ERR_INVALID, "unknown flag");
+    for (int q = 0; q < n_arrays; q++) if (!arrays[q]) return fail(CB_ERR_INVALID, "null array");
+    if (flags & CB_HOST_MEMORY) {
+        uint64_t c = 0;
+        for (int q = 0; q < n_arrays; q++)
+            for (size_t i = 0; i < n; i++) c += !std::isfinite(arrays[q][i]);
+        *count = c;
+        return CB_OK;
+    }
+    CB_CUDA(cudaSetDevice(m->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CB_CUDA(cudaMemsetAsync(m->d_count, 0, sizeof(unsigned long long), st));
+    for (int q0 = 0; q0 < n_arrays; q0 += cbg::kCountArrays) {
+        cbg::CountArgs a;
+        a.m = std::min(cbg::kCountArrays, n_arrays - q0);
+        for (int q = 0; q < a.m; q++) a.a[q] = arrays[q0 + q];
+        CB_CUDA(cbg::launch_count_nonfinite(a, n, m->d_count, st));
+    }
+    unsigned long long c = 0;
+    CB_CUDA(cudaMemcpyAsync(&c, m->d_count, sizeof c, cudaMemcpyDeviceToHost, st));
+    CB_CUDA(cudaStreamSynchronize(st));
+    *count = c;
+    return CB_OK;
+}
+
 int cb_mech_destroy(cb_mech* m) {
     if (!m) return CB_OK;
     cudaSetDevice(m->device);
@@ -375,6 +406,7 @@ int cb_mech_destroy(cb_mech* m) {
     cudaFree(m->d_rates_mixed);
     cudaFree(m->d_transport_mixed);
     cudaFree(m->d_status);
+    cudaFree(m->d_count);
     cudaFree(m->d_stage);
     delete m;
     return CB_OK;

@@ -549,6 +549,25 @@ size_t wave_of(KS ksmem, KG kglobal, uint32_t tab_bytes) {
 }
 }  // namespace
 
+// Non-finite values by exponent bits (all ones): integer instructions only.
+__global__ void count_nonfinite_kernel(const __grid_constant__ CountArgs args, size_t n, unsigned long long* count) {
+    unsigned long long c = 0;
+    for (int q = 0; q < args.m; q++)
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+            c += (__double2hiint(args.a[q][i]) & 0x7ff00000) == 0x7ff00000;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+cudaError_t launch_count_nonfinite(const CountArgs& args, size_t n, unsigned long long* count, cudaStream_t st) {
+    if (n == 0 || args.m == 0) return cudaSuccess;
+    size_t grid = (n + 255) / 256;
+    if (grid > (size_t)sm_count() * 8) grid = (size_t)sm_count() * 8;
+    count_nonfinite_kernel<<<(unsigned)grid, 256, 0, st>>>(args, n, count);
+    return cudaGetLastError();
+}
+
 // The elementary functions of the plain path on device arrays (which: 0 exp, 1 log, 2 reciprocal), for
 // accuracy checks against CUDA's own functions.
 __global__ void math_check_kernel(const uint8_t* math, int which, const double* x, double* y, size_t n) {

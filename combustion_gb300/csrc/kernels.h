@@ -62,6 +62,14 @@ inline int kmax_for(int K, int n_eff) {
 
 int max_table_smem();
 
+// Non-finite values (NaN, infinity) in up to kCountArrays arrays of n doubles, added to *count.
+constexpr int kCountArrays = 512;
+struct CountArgs {
+    const double* a[kCountArrays];
+    int m;
+};
+cudaError_t launch_count_nonfinite(const CountArgs& args, size_t n, unsigned long long* count, cudaStream_t st);
+
 // Blocks of a persistent table kernel resident per SM, the tables in shared memory (smem: the variant
 // ksmem, whose dynamic shared memory limit is raised first) or read from global memory (kglobal, only
 // the math tables in shared memory).

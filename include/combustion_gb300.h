@@ -138,6 +138,13 @@ int cb_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, doubl
 int cb_rates_transport_f64(cb_mech* mech, size_t n, const double* const* inputs, double* const* rates_out,
                            double* const* transport_out, uint32_t flags, void* stream);
 
+/* Number of non-finite values (NaN or infinity) in n_arrays arrays of n doubles each, e.g. a call's
+ * outputs: the reference's CPU path asserts finite inputs and outputs around every evaluation
+ * (plot.rs:41-46); here the caller checks when it wants to. Device arrays (stream-ordered; *count is
+ * written when the call returns, which synchronises the stream) or, with CB_HOST_MEMORY, host arrays. */
+int cb_count_nonfinite(cb_mech* mech, size_t n, int32_t n_arrays, const double* const* arrays, uint64_t* count,
+                       uint32_t flags, void* stream);
+
 /* Mixed-precision forms of the three calls above (same inputs, outputs and flags). FP64 is kept for the
  * Gibbs polynomials and exponentials of the equilibrium constant (reaction.rs:234-304), the
  * forward-minus-reverse rate of progress (reaction.rs:305-306) and the accumulation into species rates

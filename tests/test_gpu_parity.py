@@ -221,3 +221,29 @@ def test_fused_parity(config, n):
     hro, hto = np.zeros((mech.A + 2, n)), np.zeros((mech.K + 2, n))
     mech.rates_transport(np.array(ins), hro, hto)
     assert np.array_equal(hro, ro.cpu().numpy()) and np.array_equal(hto, to.cpu().numpy())
+
+
+def test_count_nonfinite():
+    """cb_count_nonfinite (the reference's finite-output assertion, plot.rs:41-46, as a count the caller
+    reads): zero on a rates call's outputs; the planted NaN and infinities exactly, on device arrays
+    (more arrays than one launch takes) and on host arrays."""
+    torch = _torch()
+    from combustion_gb300 import synthetic
+    m = util.mechanism("k10")
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, 5000, "k10")
+    out, _, _ = _run_rates(mech, o, cells)
+    dev = torch.tensor(out, device="cuda")
+    assert mech.count_nonfinite(dev) == 0
+    dev[0, 7] = float("nan")
+    dev[3, 4999] = float("inf")
+    dev[5, 0] = float("-inf")
+    assert mech.count_nonfinite(dev) == 3
+    many = torch.zeros((1100, 33), dtype=torch.float64, device="cuda")
+    many[1099, 32] = float("nan")
+    many[0, 0] = float("nan")
+    many[600, 5] = float("inf")
+    assert mech.count_nonfinite(many) == 3
+    host = dev.cpu().numpy()
+    assert mech.count_nonfinite(host) == 3
