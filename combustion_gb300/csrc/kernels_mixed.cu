@@ -145,10 +145,8 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
     const float* cond = reinterpret_cast<const float*>(tab + H.off_cond);
     const float* visc = reinterpret_cast<const float*>(tab + H.off_visc);
     const float* W = reinterpret_cast<const float*>(tab + H.off_W);
-    const float* diff = reinterpret_cast<const float*>(tab + H.off_diff);
-    const float* A2 = reinterpret_cast<const float*>(tab + H.off_A2);
-    const float* AB = reinterpret_cast<const float*>(tab + H.off_AB);
-    const float* B2 = reinterpret_cast<const float*>(tab + H.off_B2);
+    const float4* diff = reinterpret_cast<const float4*>(tab + H.off_diff);   // two per species pair
+    const float4* wil = reinterpret_cast<const float4*>(tab + H.off_wilke);   // {a^2, 2ab, b^2, 0}
     const int K = H.K;
     float N, Tn;
     const double* const* amounts;
@@ -197,17 +195,16 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
     }
     float mu = 0.f;
     for (int k0 = 0; k0 < K; k0 += 4) {
-        const float* a2 = A2 + (size_t)k0 * K;
-        const float* ab = AB + (size_t)k0 * K;
-        const float* b2 = B2 + (size_t)k0 * K;
+        const float4* w = wil + (size_t)k0 * K;
         float s1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f}, s3[4] = {0.f, 0.f, 0.f, 0.f};
         for (int j = 0; j < K; j++) {
             const float xj = X[j], yj = Y[j], zj = Z[j];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                s1[q] = fmaf(a2[q * K + j], xj, s1[q]);
-                s2[q] = fmaf(ab[q * K + j], yj, s2[q]);
-                s3[q] = fmaf(b2[q * K + j], zj, s3[q]);
+                const float4 c = w[q * K + j];
+                s1[q] = fmaf(c.x, xj, s1[q]);
+                s2[q] = fmaf(c.y, yj, s2[q]);
+                s3[q] = fmaf(c.z, zj, s3[q]);
             }
         }
 #pragma unroll
@@ -220,23 +217,29 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
 
     float* S = Y;
     for (int k = 0; k < K; k++) S[k] = 0.f;
-    const float* P = diff;
+    // a pair's fit: float4 {P0, P1, P2, P3} then {P4, 0, 0, 0}
+    auto poly4 = [&](const float4* Q) {
+        const float4 a = Q[0];
+        const float p4 = Q[1].x;
+        return fmaf(p4, L4, fmaf(a.w, L3, fmaf(a.z, L2, fmaf(a.y, L1, a.x))));
+    };
+    const float4* P = diff;
     for (int k = 1; k < K; k++) {
         const float xk = X[k];
         float sa = 0.f, sb = 0.f;
         int j = 0;
-        for (; j + 1 < k; j += 2, P += 10) {
-            const float Ra = rcp_f32(poly(P)), Rb = rcp_f32(poly(P + 5));
+        for (; j + 1 < k; j += 2, P += 4) {
+            const float Ra = rcp_f32(poly4(P)), Rb = rcp_f32(poly4(P + 2));
             sa = fmaf(X[j], Ra, sa);
             sb = fmaf(X[j + 1], Rb, sb);
             S[j] = fmaf(xk, Ra, S[j]);
             S[j + 1] = fmaf(xk, Rb, S[j + 1]);
         }
         if (j < k) {
-            const float R = rcp_f32(poly(P));
+            const float R = rcp_f32(poly4(P));
             sa = fmaf(X[j], R, sa);
             S[j] = fmaf(xk, R, S[j]);
-            P += 5;
+            P += 2;
         }
         S[k] += sa + sb;
     }

@@ -733,8 +733,18 @@ int build_transport(HostMechanism& m, double T0, double mu0, double lambda0, std
             append(b, f.data(), f.size());
             return off;
         };
-        hm.off_cond = put(cond); hm.off_visc = put(visc); hm.off_W = put(Wc); hm.off_diff = put(diff);
-        hm.off_A2 = put(A2); hm.off_AB = put(AB); hm.off_B2 = put(B2);
+        hm.off_cond = put(cond); hm.off_visc = put(visc); hm.off_W = put(Wc);
+        std::vector<double> diff8((size_t)n_pairs * 8, 0.);  // 16-byte loads in the kernel
+        for (size_t p = 0; p < (size_t)n_pairs; p++)
+            for (int c = 0; c < 5; c++) diff8[p * 8 + c] = diff[p * 5 + c];
+        hm.off_diff = put(diff8);
+        std::vector<double> wil((size_t)K4 * K * 4, 0.);
+        for (size_t e = 0; e < (size_t)K4 * K; e++) {
+            wil[e * 4] = A2[e];
+            wil[e * 4 + 1] = AB[e];
+            wil[e * 4 + 2] = B2[e];
+        }
+        hm.off_wilke = put(wil);
         finish_blob(b, hm);
     }
 

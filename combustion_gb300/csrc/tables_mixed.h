@@ -55,7 +55,10 @@ struct RatesMixedHeader {
 
 struct TransportMixedHeader {
     int32_t K, n_pairs, total_bytes, off_math;
-    int32_t off_cond, off_visc, off_W, off_diff, off_A2, off_AB, off_B2, pad2;
+    // off_diff: per species pair (k, j < k) its 5 fit coefficients padded to 8 floats (two 16-byte
+    // loads); off_wilke: per (k, j) of the rows padded to a multiple of 4, {a^2, 2ab, b^2, 0} (one 16-byte
+    // load for the three Wilke terms)
+    int32_t off_cond, off_visc, off_W, off_diff, off_wilke, pad_w[3];
     double T0, pad3;
 };
 
