@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -180,6 +181,33 @@ size_t path_wave(const cb_mech* m, Path path) {
     return lcm <= ((size_t)1 << 20) ? lcm : std::max(w[0], w[1]);
 }
 
+// Rows [q0, q1) of one chunk between a staging slot (row q at stage + q * chunk) and the caller's host
+// arrays (row q at rows[q] + lo): one strided 2-D copy per run of equally spaced, non-overlapping host
+// rows (the rows of one 2-D array), single copies otherwise.
+cudaError_t copy_rows(double* stage, size_t chunk, const double* const* rows, int q0, int q1, size_t lo, size_t len,
+                      bool to_device, cudaStream_t st) {
+    for (int a = q0; a < q1;) {
+        int b = a + 1;  // run [a, b)
+        const ptrdiff_t step = b < q1 ? rows[b] - rows[a] : 0;
+        if (step >= (ptrdiff_t)len)
+            while (b < q1 && rows[b] - rows[b - 1] == step) b++;
+        double* dev = stage + (size_t)a * chunk;
+        double* host = const_cast<double*>(rows[a]) + lo;
+        cudaError_t e;
+        if (b - a >= 2) {
+            const size_t hp = (size_t)step * sizeof(double), dp = chunk * sizeof(double), w = len * sizeof(double);
+            e = to_device ? cudaMemcpy2DAsync(dev, dp, host, hp, w, (size_t)(b - a), cudaMemcpyHostToDevice, st)
+                          : cudaMemcpy2DAsync(host, hp, dev, dp, w, (size_t)(b - a), cudaMemcpyDeviceToHost, st);
+        } else {
+            e = to_device ? cudaMemcpyAsync(dev, host, len * sizeof(double), cudaMemcpyHostToDevice, st)
+                          : cudaMemcpyAsync(host, dev, len * sizeof(double), cudaMemcpyDeviceToHost, st);
+        }
+        if (e != cudaSuccess) return e;
+        a = b;
+    }
+    return cudaSuccess;
+}
+
 // Host arrays: chunks through two device staging slots. Copies run on their own streams and kernels on
 // one compute stream (one chunk's kernels at a time: the kernels use persistent grids), so that the
 // copies of neighbouring chunks overlap the kernels: H2D(c+1) and D2H(c-1) run while chunk c computes.
@@ -221,15 +249,11 @@ int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* 
         cudaEvent_t* ev = m->slot_event[s];
         double* base = m->d_stage + s * per_slot;
         if (c >= 2) CB_CUDA(cudaStreamWaitEvent(h2d, ev[1], 0));  // the slot's previous kernels read their inputs
-        for (int q = 0; q < ni; q++) {
-            double* dst = base + (size_t)q * chunk;
-            if (uniform && q < 2) {
-                CB_CUDA(cudaMemcpyAsync(dst, in[q], sizeof(double), cudaMemcpyHostToDevice, h2d));
-            } else {
-                CB_CUDA(cudaMemcpyAsync(dst, in[q] + lo, len * sizeof(double), cudaMemcpyHostToDevice, h2d));
-            }
-            din[q] = dst;
-        }
+        const int q_arrays = uniform ? 2 : 0;  // uniform pressure: the two constants, one value each
+        for (int q = 0; q < q_arrays; q++)
+            CB_CUDA(cudaMemcpyAsync(base + (size_t)q * chunk, in[q], sizeof(double), cudaMemcpyHostToDevice, h2d));
+        CB_CUDA(copy_rows(base, chunk, in, q_arrays, ni, lo, len, true, h2d));
+        for (int q = 0; q < ni; q++) din[q] = base + (size_t)q * chunk;
         CB_CUDA(cudaEventRecord(ev[0], h2d));
         for (int q = 0; q < no; q++) dout[q] = base + (size_t)(ni + q) * chunk;
         CB_CUDA(cudaStreamWaitEvent(comp, ev[0], 0));
@@ -238,8 +262,7 @@ int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* 
         if (rc) return rc;
         CB_CUDA(cudaEventRecord(ev[1], comp));
         CB_CUDA(cudaStreamWaitEvent(d2h, ev[1], 0));
-        for (int q = 0; q < no; q++)
-            CB_CUDA(cudaMemcpyAsync(out[q] + lo, dout[q], len * sizeof(double), cudaMemcpyDeviceToHost, d2h));
+        CB_CUDA(copy_rows(base + (size_t)ni * chunk, chunk, out, 0, no, lo, len, false, d2h));
         CB_CUDA(cudaEventRecord(ev[2], d2h));
     }
     CB_CUDA(cudaStreamSynchronize(d2h));
