@@ -611,7 +611,7 @@ def main():
     ap.add_argument("--large-steps", type=int, default=1500)
     ap.add_argument("--large-reactors", type=int, default=4096, help="K = 250 reactors in --large (0: none)")
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
-    ap.add_argument("--sur-steps", type=int, default=6000)
+    ap.add_argument("--sur-steps", type=int, default=20000)
     ap.add_argument("--sur-batch", type=int, default=65536)
     ap.add_argument("--sur-audit", type=int, default=1024)
     args = ap.parse_args()
