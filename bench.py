@@ -608,7 +608,7 @@ def main():
     ap.add_argument("--no-reactors", action="store_true")
     ap.add_argument("--reactors", type=int, default=16384)
     ap.add_argument("--large", action="store_true", help="also run the K = 250 configuration")
-    ap.add_argument("--large-steps", type=int, default=1500)
+    ap.add_argument("--large-steps", type=int, default=6000)
     ap.add_argument("--large-reactors", type=int, default=4096, help="K = 250 reactors in --large (0: none)")
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
     ap.add_argument("--sur-steps", type=int, default=20000)
