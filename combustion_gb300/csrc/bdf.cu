@@ -310,7 +310,7 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     }
     if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor batch allocation"));
     // one warp's workspace beside the math tables in shared memory, or all of them in global memory
-    s->global = (s->opt.flags & CB_BDF_GLOBAL_MEMORY) || !shape_fits(s, 1, 0);
+    s->global = (s->opt.flags & CB_BDF_GLOBAL_MEMORY) || !shape_fits(s, 1, 0) || s->N > cbg::bdf::kSmemMaxN;
     if (s->global) {
         const size_t per = (size_t)s->N * s->LD;
         e = cudaMalloc(&s->LUr, n * per * sizeof(double));

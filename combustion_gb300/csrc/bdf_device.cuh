@@ -22,6 +22,15 @@ constexpr int kDRows = kMaxOrder + 3;
 constexpr int kNewtonMaxIter = 4;
 constexpr double kMinFactor = 0.2, kMaxFactor = 10.0;
 constexpr int kPanel = 8;  // columns per panel of the blocked factorisation (global-memory matrices)
+// 1 / n (n = 0..8, entry 0 unused), gamma_q = sum_{i=1..q} 1/i summed in increasing i, and 1 / gamma_q.
+static __constant__ double kRcpInt[9] = {0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8};
+static __constant__ double kGamma[7] = {0.0, 1.0, 1.0 + 1.0 / 2, 1.0 + 1.0 / 2 + 1.0 / 3, 1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4,
+                                        1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4 + 1.0 / 5,
+                                        1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4 + 1.0 / 5 + 1.0 / 6};
+static __constant__ double kRcpGamma[7] = {0.0, 1.0 / 1.0, 1.0 / (1.0 + 1.0 / 2), 1.0 / (1.0 + 1.0 / 2 + 1.0 / 3),
+                                           1.0 / (1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4),
+                                           1.0 / (1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4 + 1.0 / 5),
+                                           1.0 / (1.0 + 1.0 / 2 + 1.0 / 3 + 1.0 / 4 + 1.0 / 5 + 1.0 / 6)};
 constexpr double kReuseSpread = 0.3;  // CB_BDF_REUSE_LU: largest |c / c_lu - 1| of a kept factorisation
 constexpr int kReuseSteps = 20;       // CB_BDF_REUSE_LU: steps a factorisation is kept at most
 
@@ -137,7 +146,7 @@ struct WarpCell {
 };
 
 struct Work {
-    double *LU, *D, *ypred, *psi, *scale, *y, *d, *f, *b, *tmp, *C, *ex, *exn, *M, *hk, *cpk, *cR, *kf, *pK, *sM, *rdiag;
+    double *LU, *D, *ypred, *psi, *rscale, *y, *d, *f, *b, *tmp, *C, *ex, *exn, *M, *hk, *cpk, *cR, *kf, *pK, *sM, *rdiag;
     int* piv;
 };
 
@@ -158,7 +167,7 @@ __device__ inline Work carve(const Params& p, uint8_t* base) {
     w.D = take((size_t)kDRows * N);
     w.ypred = take(N);
     w.psi = take(N);
-    w.scale = take(N);
+    w.rscale = take(N);
     w.y = take(N);
     w.d = take(N);
     w.f = take(N);
@@ -502,37 +511,42 @@ __device__ inline void jacobian_warp(const Params& p, const Mech& m, const Work&
     __syncwarp();
 }
 
-// In-place LU with partial pivoting of the N x N matrix in A (rows of LD); false on a zero pivot.
-__device__ inline bool lu_warp(double* A, int N, int LD, int* piv, double* rdiag, int lane) {
+// In-place LU with partial pivoting (largest |A_ik|, lowest row on ties; whole rows swapped) of the
+// N x N matrix in A (rows of LD), for matrices in shared memory; false on a zero or non-finite pivot.
+// perm receives the row order: row i of the factors is row perm[i] of the input. The pivot is found on
+// the bits of |A_ik| (non-negative doubles order as integers) by three warp reductions; the trailing
+// update loads four rows before storing them, which keeps four FMAs in flight per lane.
+__device__ inline bool lu_warp(double* A, int N, int LD, int* perm, double* rdiag, int lane) {
+    for (int i = lane; i < N; i += 32) perm[i] = i;
+    __syncwarp();
     for (int k = 0; k < N; k++) {
-        double best = -1.0;
+        unsigned long long best = 0ull;
         int bi = k;
         for (int i = k + lane; i < N; i += 32) {
-            const double v = fabs(A[(size_t)i * LD + k]);
+            const unsigned long long v = (unsigned long long)__double_as_longlong(A[(size_t)i * LD + k]) & ~(1ull << 63);
             if (v > best) {
                 best = v;
                 bi = i;
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov > best || (ov == best && oi < bi)) {
-                best = ov;
-                bi = oi;
-            }
-        }
-        best = __shfl_sync(0xffffffffu, best, 0);
-        bi = __shfl_sync(0xffffffffu, bi, 0);
-        if (!(best > 0.0) || !(best < 1e300)) return false;
-        if (lane == 0) piv[k] = bi;
-        if (bi != k)
+        const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
+        const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+        const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+        bi = (int)__reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? (unsigned)bi : 0xffffffffu);
+        const double bestd = __longlong_as_double((long long)(((unsigned long long)mhi << 32) | mlo));
+        if (!(bestd > 0.0) || !(bestd < 1e300)) return false;
+        if (bi != k) {
             for (int j = lane; j < N; j += 32) {
                 const double t = A[(size_t)k * LD + j];
                 A[(size_t)k * LD + j] = A[(size_t)bi * LD + j];
                 A[(size_t)bi * LD + j] = t;
             }
+            if (lane == 0) {
+                const int t = perm[k];
+                perm[k] = perm[bi];
+                perm[bi] = t;
+            }
+        }
         __syncwarp();
         const double rp = 1.0 / A[(size_t)k * LD + k];
         if (lane == 0) rdiag[k] = rp;
@@ -540,36 +554,82 @@ __device__ inline bool lu_warp(double* A, int N, int LD, int* piv, double* rdiag
         __syncwarp();
         for (int j = k + 1 + lane; j < N; j += 32) {
             const double akj = A[(size_t)k * LD + j];
-            for (int i = k + 1; i < N; i++) A[(size_t)i * LD + j] = fma(-A[(size_t)i * LD + k], akj, A[(size_t)i * LD + j]);
+            int i = k + 1;
+            for (; i + 3 < N; i += 4) {
+                double* r = A + (size_t)i * LD;
+                const double l0 = r[k], l1 = r[LD + k], l2 = r[2 * LD + k], l3 = r[3 * LD + k];
+                const double a0 = r[j], a1 = r[LD + j], a2 = r[2 * LD + j], a3 = r[3 * LD + j];
+                r[j] = fma(-l0, akj, a0);
+                r[LD + j] = fma(-l1, akj, a1);
+                r[2 * LD + j] = fma(-l2, akj, a2);
+                r[3 * LD + j] = fma(-l3, akj, a3);
+            }
+            for (; i < N; i++) A[(size_t)i * LD + j] = fma(-A[(size_t)i * LD + k], akj, A[(size_t)i * LD + j]);
         }
         __syncwarp();
     }
     return true;
 }
 
-__device__ inline void lu_solve_warp(const double* A, int N, int LD, const int* piv, const double* rdiag, double* b, int lane) {
-    if (lane == 0)
-        for (int k = 0; k < N; k++) {
-            const int pk = piv[k];
-            if (pk != k) {
-                const double t = b[k];
-                b[k] = b[pk];
-                b[pk] = t;
-            }
-        }
+// Rows of a lu_solve_warp right-hand side held per lane (row lane + 32 s in slot s) for N <= 32 S.
+template <int S>
+__device__ __forceinline__ double slot_value(const double (&x)[S], int k) {
+    double v = x[0];
+#pragma unroll
+    for (int s = 1; s < S; s++)
+        if (k >= 32 * s) v = x[s];
+    return v;
+}
+
+// b <- U^-1 L^-1 (b permuted by perm) with the right-hand side in registers: the eliminated row's value
+// reaches the other lanes by a shuffle, so a step waits for one FMA and one shuffle instead of a
+// shared-memory round trip and a warp barrier. Same operations, in the same order, as the textbook
+// column-oriented substitution (row k's value times column k subtracted from the rows below, then
+// above, it).
+template <int S>
+__device__ inline void lu_solve_regs(const double* A, int N, int LD, const int* perm, const double* rdiag, double* b,
+                                     int lane) {
+    double x[S];
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        const int i = lane + 32 * s;
+        x[s] = i < N ? b[perm[i]] : 0.0;
+    }
     __syncwarp();
-    for (int k = 0; k < N; k++) {
-        const double bk = b[k];
-        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-A[(size_t)i * LD + k], bk, b[i]);
-        __syncwarp();
+    for (int k = 0; k < N - 1; k++) {
+        const double xk = __shfl_sync(0xffffffffu, slot_value<S>(x, k), k & 31);
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (32 * s + 31 <= k) continue;  // warp-uniform: the slot's rows are all at or above row k
+            const int i = lane + 32 * s;
+            if (i > k && i < N) x[s] = fma(-A[(size_t)i * LD + k], xk, x[s]);
+        }
     }
     for (int k = N - 1; k >= 0; k--) {
-        const double bk = b[k] * rdiag[k];
-        __syncwarp();
-        if (lane == 0) b[k] = bk;
-        for (int i = lane; i < k; i += 32) b[i] = fma(-A[(size_t)i * LD + k], bk, b[i]);
-        __syncwarp();
+        const double xk = __shfl_sync(0xffffffffu, slot_value<S>(x, k), k & 31) * rdiag[k];
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (32 * s > k) continue;  // warp-uniform: the slot's rows are all below row k
+            const int i = lane + 32 * s;
+            if (i == k) x[s] = xk;
+            else if (i < k) x[s] = fma(-A[(size_t)i * LD + k], xk, x[s]);
+        }
     }
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        const int i = lane + 32 * s;
+        if (i < N) b[i] = x[s];
+    }
+    __syncwarp();
+}
+
+constexpr int kSmemMaxN = 160;  // largest state of the shared-memory path (lu_solve_warp's register slots)
+
+__device__ inline void lu_solve_warp(const double* A, int N, int LD, const int* perm, const double* rdiag, double* b,
+                                     int lane) {
+    if (N <= 64) lu_solve_regs<2>(A, N, LD, perm, rdiag, b, lane);
+    else if (N <= 96) lu_solve_regs<3>(A, N, LD, perm, rdiag, b, lane);
+    else lu_solve_regs<5>(A, N, LD, perm, rdiag, b, lane);
 }
 
 // lu_warp by panels of kPanel columns, for matrices in global memory: inside a panel the pivot search,
@@ -733,10 +793,11 @@ __device__ inline bool build_lu(const Params& p, double* LU, int* piv, double* r
     }
 }
 
-__device__ __forceinline__ double rms_scaled(const double* x, const double* scale, int N, int lane) {
+// Weighted RMS norm; rscale holds the reciprocal weights 1 / (atol + rtol |y_i|).
+__device__ __forceinline__ double rms_scaled(const double* x, const double* rscale, int N, int lane) {
     double s = 0.0;
     for (int i = lane; i < N; i += 32) {
-        const double v = x[i] / scale[i];
+        const double v = x[i] * rscale[i];
         s = fma(v, v, s);
     }
     return sqrt(warp_sum(s) / N);
@@ -751,8 +812,8 @@ __device__ inline void change_D(double* D, int N, int q, double factor, int lane
     }
     for (int i = 1; i <= q; i++)
         for (int j = 0; j <= q; j++) {
-            const double mr = j == 0 ? 0.0 : ((double)(i - 1) - factor * j) / i;
-            const double mu = j == 0 ? 0.0 : ((double)(i - 1) - (double)j) / i;
+            const double mr = j == 0 ? 0.0 : ((double)(i - 1) - factor * j) * kRcpInt[i];
+            const double mu = j == 0 ? 0.0 : ((double)(i - 1) - (double)j) * kRcpInt[i];
             R[i][j] = R[i - 1][j] * mr;
             U[i][j] = U[i - 1][j] * mu;
         }
@@ -775,11 +836,17 @@ __device__ inline void change_D(double* D, int N, int q, double factor, int lane
     __syncwarp();
 }
 
-__device__ __forceinline__ double gamma_k(int k) {  // sum_{i=1..k} 1/i
-    double g = 0.0;
-    for (int i = 1; i <= k; i++) g += 1.0 / i;
-    return g;
+__device__ __forceinline__ double gamma_k(int k) { return kGamma[k]; }  // sum_{i=1..k} 1/i
+
+// x^n for the small exponents of the Newton convergence test.
+__device__ __forceinline__ double ipow(double x, int n) {
+    double r = x;
+    for (int i = 1; i < n; i++) r *= x;
+    return r;
 }
+
+// x^(-1/n), x > 0 finite, for the step-size factors.
+__device__ __forceinline__ double root_factor(double x, int n) { return exp64(-log64(x) * kRcpInt[n]); }
 
 // One reactor for at most `budget` steps (warp-uniform control flow). MIXED: the first Newton iteration
 // of each step on the mixed-precision f(u); GLOBAL: workspaces and per-reactor factorisations in global
@@ -820,9 +887,9 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         __syncwarp();
         rhs_warp<false>(p, m, w, pR, rP, w.y, w.f, lane);
         hd.rhs++;
-        for (int i = lane; i < N; i += 32) w.scale[i] = p.atol + p.rtol * fabs(w.y[i]);
+        for (int i = lane; i < N; i += 32) w.rscale[i] = 1.0 / (p.atol + p.rtol * fabs(w.y[i]));
         __syncwarp();
-        const double d0 = rms_scaled(w.y, w.scale, N, lane), d1 = rms_scaled(w.f, w.scale, N, lane);
+        const double d0 = rms_scaled(w.y, w.rscale, N, lane), d1 = rms_scaled(w.f, w.rscale, N, lane);
         const double h0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * d0 / d1;
         for (int i = lane; i < N; i += 32) w.b[i] = fma(h0, w.f[i], w.y[i]);
         __syncwarp();
@@ -830,7 +897,7 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         hd.rhs++;
         for (int i = lane; i < N; i += 32) w.b[i] = w.tmp[i] - w.f[i];
         __syncwarp();
-        const double d2 = rms_scaled(w.b, w.scale, N, lane) / h0;
+        const double d2 = rms_scaled(w.b, w.rscale, N, lane) / h0;
         const double h1 = (d1 <= 1e-15 && d2 <= 1e-15) ? fmax(1e-6, h0 * 1e-3) : sqrt(0.01 / fmax(d1, d2));
         double h = fmin(100.0 * h0, h1);
         h = fmin(h, p.t_end);
@@ -890,8 +957,8 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
             for (int j = 0; j <= q; j++) yp += w.D[(size_t)j * N + i];
             for (int j = 1; j <= q; j++) ps = fma(gamma_k(j), w.D[(size_t)j * N + i], ps);
             w.ypred[i] = yp;
-            w.psi[i] = ps / gq;
-            w.scale[i] = p.atol + p.rtol * fabs(yp);
+            w.psi[i] = ps * kRcpGamma[q];
+            w.rscale[i] = 1.0 / (p.atol + p.rtol * fabs(yp));
             w.y[i] = yp;
             w.d[i] = 0.0;
         }
@@ -935,9 +1002,9 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
                     for (int i = lane; i < N; i += 32) w.b[i] *= corr;
                     __syncwarp();
                 }
-                const double dy_norm = rms_scaled(w.b, w.scale, N, lane);
+                const double dy_norm = rms_scaled(w.b, w.rscale, N, lane);
                 const double rate = dy_norm_old >= 0.0 ? dy_norm / dy_norm_old : -1.0;
-                if (rate >= 0.0 && (rate >= 1.0 || pow(rate, (double)(kNewtonMaxIter - k)) / (1.0 - rate) * dy_norm > newton_tol))
+                if (rate >= 0.0 && (rate >= 1.0 || ipow(rate, kNewtonMaxIter - k) / (1.0 - rate) * dy_norm > newton_tol))
                     break;
                 for (int i = lane; i < N; i += 32) {
                     w.y[i] += w.b[i];
@@ -974,14 +1041,14 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         }
         const double safety = 0.9 * (2 * kNewtonMaxIter + 1) / (2 * kNewtonMaxIter + n_iter);
         for (int i = lane; i < N; i += 32) {
-            w.scale[i] = p.atol + p.rtol * fabs(w.y[i]);
-            w.b[i] = w.d[i] / (q + 1);  // error = error_const(q) d
+            w.rscale[i] = 1.0 / (p.atol + p.rtol * fabs(w.y[i]));
+            w.b[i] = w.d[i] * kRcpInt[q + 1];  // error = error_const(q) d
         }
         __syncwarp();
-        const double err_norm = rms_scaled(w.b, w.scale, N, lane);
+        const double err_norm = rms_scaled(w.b, w.rscale, N, lane);
         if (err_norm > 1.0) {
             hd.err_fail++;
-            const double factor = fmax(kMinFactor, safety * pow(err_norm, -1.0 / (q + 1)));
+            const double factor = fmax(kMinFactor, safety * root_factor(err_norm, q + 1));
             change_D(w.D, N, q, factor, lane);
             hd.h = h * factor;
             hd.n_equal = 0;
@@ -1004,7 +1071,7 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         if (p.traj || p.peak_k >= 0) record_outputs(p, hd, r, w.D, t_new, h, q, lane);
         // dT/dt at the new point from the backward differences: h y' = sum_{j=1..q} D_j / j
         double g = 0.0;
-        for (int j = 1; j <= q; j++) g += w.D[(size_t)j * N] / j;
+        for (int j = 1; j <= q; j++) g += w.D[(size_t)j * N] * kRcpInt[j];
         g /= h;
         if (hd.need_next) {
             hd.tc = t_new;
@@ -1033,18 +1100,18 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         const double inf = 1e300;
         double em = inf, ep = inf;
         if (q > 1) {
-            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)q * N + i] / q;
+            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)q * N + i] * kRcpInt[q];
             __syncwarp();
-            em = rms_scaled(w.b, w.scale, N, lane);
+            em = rms_scaled(w.b, w.rscale, N, lane);
         }
         if (q < kMaxOrder) {
-            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)(q + 2) * N + i] / (q + 2);
+            for (int i = lane; i < N; i += 32) w.b[i] = w.D[(size_t)(q + 2) * N + i] * kRcpInt[q + 2];
             __syncwarp();
-            ep = rms_scaled(w.b, w.scale, N, lane);
+            ep = rms_scaled(w.b, w.rscale, N, lane);
         }
-        const double fm = em >= inf ? 0.0 : (em > 0.0 ? pow(em, -1.0 / q) : inf);
-        const double fz = err_norm > 0.0 ? pow(err_norm, -1.0 / (q + 1)) : inf;
-        const double fp = ep >= inf ? 0.0 : (ep > 0.0 ? pow(ep, -1.0 / (q + 2)) : inf);
+        const double fm = em >= inf ? 0.0 : (em > 0.0 ? root_factor(em, q) : inf);
+        const double fz = err_norm > 0.0 ? root_factor(err_norm, q + 1) : inf;
+        const double fp = ep >= inf ? 0.0 : (ep > 0.0 ? root_factor(ep, q + 2) : inf);
         int dq = 0;
         double best = fz;
         if (fm > best) {
