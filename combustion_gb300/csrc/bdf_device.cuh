@@ -201,12 +201,77 @@ struct RhsOut {
     double T, V, md, Ctot, S, E, Cp, dtE;
 };
 
+// One third-body sum sum_k E_k C_k in four interleaved partial sums (independent FMA chains), added
+// pairwise at the end.
+__device__ __forceinline__ double eff_dot(const double* E, const double* C, int K) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int k = 0;
+    for (; k + 3 < K; k += 4) {
+        s0 = fma(E[k], C[k], s0);
+        s1 = fma(E[k + 1], C[k + 1], s1);
+        s2 = fma(E[k + 2], C[k + 2], s2);
+        s3 = fma(E[k + 3], C[k + 3], s3);
+    }
+    for (; k < K; k++) s0 = fma(E[k], C[k], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+// The same in FP32 over the FP64 concentrations (the mixed program's third-body sums).
+__device__ __forceinline__ float eff_dot_f32(const float* E, const double* C, int K) {
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int k = 0;
+    for (; k + 3 < K; k += 4) {
+        s0 = fmaf(E[k], dbl_to_flt(C[k]), s0);
+        s1 = fmaf(E[k + 1], dbl_to_flt(C[k + 1]), s1);
+        s2 = fmaf(E[k + 2], dbl_to_flt(C[k + 2]), s2);
+        s3 = fmaf(E[k + 3], dbl_to_flt(C[k + 3]), s3);
+    }
+    for (; k < K; k++) s0 = fmaf(E[k], dbl_to_flt(C[k]), s0);
+    return (s0 + s1) + (s2 + s3);
+}
+
+// Net production rate of species k, sum over its reactions of nu cR (reaction.rs:312-327), in two
+// interleaved partial sums.
+__device__ __forceinline__ double species_rate(const Mech& m, const double* cR, int k) {
+    double w0 = 0.0, w1 = 0.0;
+    int q = m.csr_start[k];
+    const int qe = m.csr_start[k + 1];
+    for (; q + 1 < qe; q += 2) {
+        const int e0 = m.csr[q], e1 = m.csr[q + 1];
+        w0 = fma(small_int_to_double((int)(int8_t)(e0 & 0xff)), cR[e0 >> 8], w0);
+        w1 = fma(small_int_to_double((int)(int8_t)(e1 & 0xff)), cR[e1 >> 8], w1);
+    }
+    if (q < qe) {
+        const int e = m.csr[q];
+        w0 = fma(small_int_to_double((int)(int8_t)(e & 0xff)), cR[e >> 8], w0);
+    }
+    return w0 + w1;
+}
+
+// Rates of progress of the reactions of one model (the tables group reactions by model), lanes strided
+// over the group, so that a warp never runs two models' programs under partial masks.
+template <int MODEL, bool PARTS>
+__device__ __forceinline__ void rates_group_warp(const Mech& m, const Work& w, const WarpCell& c, int lane) {
+    const RatesHeader& H = *m.tb.H;
+    const int end = H.group_end[MODEL];
+    for (int r = (MODEL ? H.group_end[MODEL - 1] : 0) + lane; r < end; r += 32) {
+        const Reaction& x = m.tb.reactions[r];
+        ReactionParts pp;
+        w.cR[r] = reaction_eval<MODEL, PARTS>(m.tb, x, c, &pp);
+        if (PARTS) {
+            w.kf[r] = pp.kf;
+            w.pK[r] = pp.pK;
+            w.sM[r] = pp.dkf_dM * pp.Rnet;
+        }
+    }
+}
+
 // du/dt of the reactor: the outputs of reaction.rs:356-391 at state y = [T, V, n_0 .. n_{A-1}].
 template <bool PARTS>
 __device__ inline RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
                            double* f, int lane) {
     const RatesHeader& H = *m.tb.H;
-    const int K = p.K, A = p.A, R = p.R;
+    const int K = p.K, A = p.A;
     RhsOut o;
     const double T = y[0], V = y[1];
     WarpCell c;
@@ -248,44 +313,22 @@ __device__ inline RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w,
         }
     }
     __syncwarp();
-    for (int e = lane; e < H.n_eff; e += 32) {
-        const double* E = m.tb.eff + (size_t)e * K;
-        double sum = 0.0;
-        for (int k = 0; k < K; k++) sum = fma(E[k], w.C[k], sum);
-        w.M[e] = Ctot + sum;
-    }
+    for (int e = lane; e < H.n_eff; e += 32) w.M[e] = Ctot + eff_dot(m.tb.eff + (size_t)e * K, w.C, K);
     __syncwarp();
     c.C = w.C;
     c.ex = w.ex;
     c.exn = w.exn;
     c.M = w.M;
-    for (int r = lane; r < R; r += 32) {
-        const Reaction& x = m.tb.reactions[r];
-        ReactionParts pp;
-        double cR;
-        switch (x.model) {
-        case 0: cR = reaction_eval<0, PARTS>(m.tb, x, c, &pp); break;
-        case 1: cR = reaction_eval<1, PARTS>(m.tb, x, c, &pp); break;
-        case 2: cR = reaction_eval<2, PARTS>(m.tb, x, c, &pp); break;
-        case 3: cR = reaction_eval<3, PARTS>(m.tb, x, c, &pp); break;
-        case 4: cR = reaction_eval<4, PARTS>(m.tb, x, c, &pp); break;
-        default: cR = reaction_eval<5, PARTS>(m.tb, x, c, &pp); break;
-        }
-        w.cR[r] = cR;
-        if (PARTS) {
-            w.kf[r] = pp.kf;
-            w.pK[r] = pp.pK;
-            w.sM[r] = pp.dkf_dM * pp.Rnet;
-        }
-    }
+    rates_group_warp<0, PARTS>(m, w, c, lane);
+    rates_group_warp<1, PARTS>(m, w, c, lane);
+    rates_group_warp<2, PARTS>(m, w, c, lane);
+    rates_group_warp<3, PARTS>(m, w, c, lane);
+    rates_group_warp<4, PARTS>(m, w, c, lane);
+    rates_group_warp<5, PARTS>(m, w, c, lane);
     __syncwarp();
     double E = 0.0, dtE = 0.0, Cp = 0.0;
     for (int k = lane; k < A; k += 32) {
-        double wk = 0.0;
-        for (int q = m.csr_start[k]; q < m.csr_start[k + 1]; q++) {
-            const int e = m.csr[q];
-            wk = fma(small_int_to_double((int)(int8_t)(e & 0xff)), w.cR[e >> 8], wk);
-        }
+        const double wk = species_rate(m, w.cR, k);
         f[2 + k] = wk;
         E = fma(wk, w.hk[k], E);
         dtE = fma(m.tb.species[k].dtE, wk, dtE);
@@ -321,6 +364,14 @@ struct WarpCellM {
     float Ctotf, Tf, lnTf, rcpTf;
 };
 
+// rates_group_warp for the mixed-precision program.
+template <int MODEL>
+__device__ __forceinline__ void rates_group_warp_m(const RatesMixedTables& tm, const Work& w, const WarpCellM& c, int lane) {
+    const int end = tm.H->group_end[MODEL];
+    for (int r = (MODEL ? tm.H->group_end[MODEL - 1] : 0) + lane; r < end; r += 32)
+        w.cR[r] = reaction_rate_m<MODEL>(tm, tm.reactions[r], c);
+}
+
 // du/dt by the mixed-precision rates program (the arithmetic of kernels_mixed.cu's rates_mixed_cell,
 // warp-cooperative as rhs_warp): FP64 concentrations, Gibbs polynomials and exponentials, rates of
 // progress, accumulation and energy sums; FP32 Arrhenius terms, third-body sums, falloff blending and
@@ -328,7 +379,7 @@ struct WarpCellM {
 __device__ inline void rhs_warp_mixed(const Params& p, const Mech& m, const RatesMixedTables& tm, const Work& w, double pR,
                                double rP, const double* y, double* f, int lane) {
     const RatesMixedHeader& H = *tm.H;
-    const int K = p.K, A = p.A, R = p.R;
+    const int K = p.K, A = p.A;
     const double T = y[0], V = y[1];
     const double rcpT = rcp64(T), lnT = log64(T);
     const double T2 = T * T, T3 = T * T2, T4 = T2 * T2;
@@ -369,38 +420,22 @@ __device__ inline void rhs_warp_mixed(const Params& p, const Mech& m, const Rate
     }
     __syncwarp();
     float* Mf = reinterpret_cast<float*>(w.M);
-    for (int e = lane; e < H.n_eff; e += 32) {
-        const float* E = tm.eff + (size_t)e * K;
-        float sum = 0.f;
-        for (int k = 0; k < K; k++) sum = fmaf(E[k], dbl_to_flt(w.C[k]), sum);
-        Mf[e] = c.Ctotf + sum;
-    }
+    for (int e = lane; e < H.n_eff; e += 32) Mf[e] = c.Ctotf + eff_dot_f32(tm.eff + (size_t)e * K, w.C, K);
     __syncwarp();
     c.C = w.C;
     c.ex = w.ex;
     c.exn = w.exn;
     c.Mf = Mf;
-    for (int r = lane; r < R; r += 32) {
-        const ReactionF& x = tm.reactions[r];
-        double cR;
-        switch (x.model) {
-        case 0: cR = reaction_rate_m<0>(tm, x, c); break;
-        case 1: cR = reaction_rate_m<1>(tm, x, c); break;
-        case 2: cR = reaction_rate_m<2>(tm, x, c); break;
-        case 3: cR = reaction_rate_m<3>(tm, x, c); break;
-        case 4: cR = reaction_rate_m<4>(tm, x, c); break;
-        default: cR = reaction_rate_m<5>(tm, x, c); break;
-        }
-        w.cR[r] = cR;
-    }
+    rates_group_warp_m<0>(tm, w, c, lane);
+    rates_group_warp_m<1>(tm, w, c, lane);
+    rates_group_warp_m<2>(tm, w, c, lane);
+    rates_group_warp_m<3>(tm, w, c, lane);
+    rates_group_warp_m<4>(tm, w, c, lane);
+    rates_group_warp_m<5>(tm, w, c, lane);
     __syncwarp();
     double E = 0.0, dtE = 0.0, Cp = 0.0;
     for (int k = lane; k < A; k += 32) {
-        double wk = 0.0;
-        for (int q = m.csr_start[k]; q < m.csr_start[k + 1]; q++) {
-            const int e = m.csr[q];
-            wk = fma(small_int_to_double((int)(int8_t)(e & 0xff)), w.cR[e >> 8], wk);
-        }
+        const double wk = species_rate(m, w.cR, k);
         f[2 + k] = wk;
         E = fma(wk, w.hk[k], E);
         dtE = fma(tm.species[k].dtE, wk, dtE);
