@@ -245,7 +245,8 @@ def run_reactors(args, rank):
     res = R.results()
     n_ref = min(256, n)
     ref = RX.Reactors(mech, n_ref, rtol=1e-10, atol=1e-16, t_end=1e-3, warps_per_block=tune["warps_per_block"],
-                      tables_in_shared=tune["tables_in_shared"])
+                      tables_in_shared=tune["tables_in_shared"],
+                      flags=RX.GLOBAL_MEMORY if tune["global_memory"] else 0)
     ref.set_state(*[a[..., :n_ref] for a in state])
     ref.integrate()
     rr = ref.results()
@@ -267,6 +268,7 @@ def run_reactors(args, rank):
         "rhs_evals_per_s": st["rhs_evals"] / secs, "factorizations_per_s": st["factorizations"] / secs,
         "jacobians": st["jacobians"], "finished": st["finished"], "failed": st["failed"],
         "launch": {"warps_per_block": st["warps_per_block"], "tables_in_shared": st["tables_in_shared"],
+                   "workspaces": "global memory" if st["global_memory"] else "shared memory",
                    "graph_replays": st["graph_replays"], "slices": st["slices"], "autotune": tune["candidates"]},
         "ignition_delay_vs_rtol_1e-10": {"reactors": int(ok.sum()), "max_rel": float(rel.max()) if rel.size else None,
                                           "median_rel": float(np.median(rel)) if rel.size else None},

@@ -52,7 +52,7 @@ __global__ void eval_kernel(const Params p, int count) {
     }
     const Mech m(tab, p);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Work w = carve(p, workspace_of(p, warp));
+    const Work w = carve(p, workspace_of(p, warp), (size_t)blockIdx.x * (blockDim.x >> 5) + warp);
     const int N = p.N;
     for (int s = blockIdx.x * (blockDim.x >> 5) + warp; s < count; s += gridDim.x * (blockDim.x >> 5)) {
         for (int i = lane; i < N; i += 32) w.y[i] = p.eval_y[(size_t)s * N + i];
@@ -73,10 +73,11 @@ struct cb_reactors {
     cb_mech* mech = nullptr;
     int device = 0;
     int K = 0, A = 0, R = 0, N = 0, LD = 0, n_eff = 0;
-    size_t n = 0;
+    size_t n = 0;         // reactors the launches cover (the autotuner lowers it while it calibrates)
+    size_t capacity = 0;  // reactors of the batch: every per-reactor buffer holds this many
     cb_bdf_options opt{};
     std::vector<uint8_t> blob;
-    int off_csr_start = 0, off_csr = 0;
+    int off_csr_start = 0, off_csr = 0, off_eff_t = 0;
     uint8_t* d_tab = nullptr;
     double* pR = nullptr;
     Head* head = nullptr;
@@ -90,10 +91,15 @@ struct cb_reactors {
     // Workspaces in global memory when one warp's does not fit in shared memory (large mechanisms):
     // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, pivots and 1 / U_kk.
     bool global = false;
+    bool smem_ok = false;  // one workspace fits in shared memory and CB_BDF_GLOBAL_MEMORY is not set
     uint8_t* ws = nullptr;
     size_t ws_slots = 0;
     double *LUr = nullptr, *LUt = nullptr, *rdiag_r = nullptr;
     int* piv_r = nullptr;
+    // Shared-memory workspaces: the Jacobian's per-reaction terms (kf, pK, sM) of every warp slot in
+    // global memory instead, [jac_slots][3 R] (they are used by the Jacobian only).
+    double* jac_ws = nullptr;
+    size_t jac_slots = 0;
     // cb_reactors_set_outputs: trajectory [n][n_points][N] and the peak species' state [n][N]
     double* traj = nullptr;
     int n_points = 0, peak_k = -1;
@@ -109,7 +115,7 @@ namespace {
     } while (0)
 
 uint32_t ws_bytes(const cb_reactors* s) {
-    const size_t d = workspace_doubles(s->K, s->A, s->R, s->N, s->LD, s->n_eff);
+    const size_t d = workspace_doubles(s->K, s->A, s->R, s->N, s->LD, s->n_eff, s->global);
     return (uint32_t)(((d * sizeof(double) + (size_t)s->N * sizeof(int)) + 127) & ~(size_t)127);
 }
 
@@ -140,6 +146,7 @@ Params params(cb_reactors* s, int tables) {
     p.smem_tables = tables;
     p.off_csr_start = s->off_csr_start;
     p.off_csr = s->off_csr;
+    p.off_eff_t = s->off_eff_t;
     p.K = s->K;
     p.A = s->A;
     p.R = s->R;
@@ -169,6 +176,7 @@ Params params(cb_reactors* s, int tables) {
     p.mixed = (s->opt.flags & CB_BDF_MIXED_RHS) ? 1 : 0;
     p.reuse_lu = (s->opt.flags & CB_BDF_REUSE_LU) ? 1 : 0;
     p.lu32 = (s->global && (s->opt.flags & CB_BDF_LU32)) ? 1 : 0;
+    p.jac_ws = s->global ? nullptr : s->jac_ws;
     if (s->global) {
         p.ws_global = s->ws;
         p.LUr = s->LUr;
@@ -194,6 +202,21 @@ cudaError_t ensure_slots(cb_reactors* s, size_t slots) {
     return e;
 }
 
+// Per-reactor factorisations and the evaluation hook's workspaces of the global-memory placement
+// (s->global set; outside any stream capture).
+cudaError_t ensure_global(cb_reactors* s) {
+    cudaError_t e = cudaSuccess;
+    if (!s->LUr) {
+        const size_t per = (size_t)s->N * s->LD, n = s->capacity;
+        e = cudaMalloc(&s->LUr, n * per * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->LUt, n * per * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->rdiag_r, n * (size_t)s->N * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&s->piv_r, n * (size_t)s->N * sizeof(int));
+        if (e != cudaSuccess) return e;
+    }
+    return ensure_slots(s, (size_t)sm_count());
+}
+
 // The slice kernel of the batch's variant: FP64 or mixed-precision first Newton iterations, workspaces
 // in shared or global memory.
 SliceFn slice_fn(const cb_reactors* s) {
@@ -211,6 +234,7 @@ cudaError_t prepare_slice(cb_reactors* s, int warps, int tables, int* grid) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * warps, smem);
     if (e != cudaSuccess) return e;
     *grid = sm_count() * (per_sm < 1 ? 1 : per_sm);
+    if (!s->global && (size_t)*grid * warps > s->jac_slots) return cudaErrorInvalidConfiguration;
     return ensure_slots(s, (size_t)*grid * warps);
 }
 
@@ -256,6 +280,7 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     s->N = v.A + 2;
     s->LD = s->N | 1;
     s->n = n;
+    s->capacity = n;
     s->opt = *opt;
     if (s->opt.slice_steps <= 0) s->opt.slice_steps = 256;
     s->warps = opt->warps_per_block;
@@ -289,6 +314,15 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
     s->blob.resize(s->blob.size() + std::max<size_t>(flat.size(), 1) * 4);
     if (!flat.empty()) std::memcpy(s->blob.data() + s->off_csr, flat.data(), flat.size() * 4);
     while (s->blob.size() % 16) s->blob.push_back(0);
+    // the third-body efficiencies transposed, [K][n_eff], so that the lanes of a warp (one row each)
+    // read consecutive doubles
+    s->off_eff_t = (int)s->blob.size();
+    s->blob.resize(s->blob.size() + std::max<size_t>((size_t)s->K * s->n_eff, 1) * sizeof(double));
+    for (int e = 0; e < s->n_eff; e++)
+        for (int k = 0; k < s->K; k++)
+            std::memcpy(s->blob.data() + s->off_eff_t + ((size_t)k * s->n_eff + e) * sizeof(double),
+                        rb.data() + H.off_eff + ((size_t)e * s->K + k) * sizeof(double), sizeof(double));
+    while (s->blob.size() % 16) s->blob.push_back(0);
     auto fail_free = [&](int rc) {
         cb_reactors_destroy(s);
         return rc;
@@ -309,16 +343,22 @@ int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* opt, cb_re
         if (e == cudaSuccess) e = cudaMemcpy(s->d_tab_m, mb.data(), mb.size(), cudaMemcpyHostToDevice);
     }
     if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor batch allocation"));
-    // one warp's workspace beside the math tables in shared memory, or all of them in global memory
-    s->global = (s->opt.flags & CB_BDF_GLOBAL_MEMORY) || !shape_fits(s, 1, 0) || s->N > cbg::bdf::kSmemMaxN;
+    // one warp's workspace beside the math tables in shared memory, or all of them in global memory (the
+    // autotuner tries both placements when the first is possible)
+    s->smem_ok = !(s->opt.flags & CB_BDF_GLOBAL_MEMORY) && shape_fits(s, 1, 0) && s->N <= cbg::bdf::kSmemMaxN;
+    s->global = !s->smem_ok;
     if (s->global) {
-        const size_t per = (size_t)s->N * s->LD;
-        e = cudaMalloc(&s->LUr, n * per * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&s->LUt, n * per * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&s->rdiag_r, n * (size_t)s->N * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&s->piv_r, n * (size_t)s->N * sizeof(int));
-        if (e == cudaSuccess) e = ensure_slots(s, (size_t)sm_count());  // the evaluation hook's warps
+        e = ensure_global(s);
         if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor workspaces in global memory"));
+    } else {
+        // as many warp slots as shared memory lets the SMs hold (every launch shape's grid fits)
+        int dev = 0, smem_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        const size_t per_sm = std::max<size_t>(1, (size_t)smem_sm / ws_bytes(s));
+        s->jac_slots = (size_t)sm_count() * per_sm;
+        e = cudaMalloc(&s->jac_ws, s->jac_slots * 3 * (size_t)s->R * sizeof(double));
+        if (e != cudaSuccess) return fail_free(cbi::cuda_fail(e, "reactor Jacobian scratch"));
     }
     *out = s;
     return CB_OK;
@@ -343,6 +383,7 @@ int cb_reactors_destroy(cb_reactors* s) {
     cudaFree(s->LUt);
     cudaFree(s->rdiag_r);
     cudaFree(s->piv_r);
+    cudaFree(s->jac_ws);
     cudaFree(s->traj);
     cudaFree(s->peak_state);
     delete s;
@@ -438,15 +479,21 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     if (!s) return cbi::fail(CB_ERR_INVALID, "null argument");
     if (!s->have_state) return cbi::fail(CB_ERR_NOT_READY, "cb_reactors_set_state has not run");
     BDF_CUDA(cudaSetDevice(s->device));
-    // candidates: reactors in flight per block, tables in shared memory or read through L1
-    struct Cand { int warps, tables; };
+    // candidates: workspaces in shared or global memory, reactors in flight per block, tables in shared
+    // memory or read through L1
+    struct Cand { int warps, tables, global; };
     std::vector<Cand> cands;
-    for (int tables = 1; tables >= 0; tables--)
-        for (int w = 1; w <= 8; w++)
-            if (shape_fits(s, w, tables) && (!s->global || (w & (w - 1)) == 0)) cands.push_back({w, tables});
+    const bool placement = s->global;
+    for (int g = s->smem_ok ? 0 : 1; g <= 1; g++) {
+        s->global = g != 0;
+        for (int tables = 1; tables >= 0; tables--)
+            for (int w = 1; w <= 8; w++)
+                if (shape_fits(s, w, tables) && (!g || (w & (w - 1)) == 0)) cands.push_back({w, tables, g});
+    }
+    s->global = placement;
     if (cands.empty()) return cbi::fail(CB_ERR_UNSUPPORTED, "no launch shape fits");
     // calibrate on copies of the state: a few slices of the first reactors, then restore the state
-    const size_t n_def = s->global ? 512 : 4096;
+    const size_t n_def = s->smem_ok ? 4096 : 512;
     const size_t n_cal = std::min<size_t>(s->n, calib_reactors > 0 ? (size_t)calib_reactors : n_def);
     const size_t hb = s->n * sizeof(Head), db = s->n * kDRows * (size_t)s->N * sizeof(double);
     std::vector<uint8_t> h0(hb), d0(db);
@@ -459,13 +506,15 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         size_t n;
         int steps, peak;
         double* traj;
+        bool global;
         ~Restore() {
             s->n = n;
             s->opt.slice_steps = steps;
             s->traj = traj;
             s->peak_k = peak;
+            s->global = global;
         }
-    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj};
+    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj, s->global};
     s->traj = nullptr;
     s->peak_k = -1;
     s->n = n_cal;
@@ -480,6 +529,8 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         cudaMemcpy(s->head, h0.data(), n_cal * sizeof(Head), cudaMemcpyHostToDevice);
         cudaMemcpy(s->D, d0.data(), n_cal * kDRows * (size_t)s->N * sizeof(double), cudaMemcpyHostToDevice);
         cudaMemset(s->counters, 0, 4 * sizeof(int));
+        s->global = c.global != 0;
+        if (s->global && ensure_global(s) != cudaSuccess) continue;
         int grid = 0;
         if (prepare_slice(s, c.warps, c.tables, &grid) != cudaSuccess) continue;
         cudaEventRecord(a, s->stream);
@@ -491,9 +542,10 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         if (cudaEventSynchronize(b) != cudaSuccess) break;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, a, b);
-        if (out && tried < 16) {
+        if (out && tried < 32) {
             out->candidates[tried].warps_per_block = c.warps;
             out->candidates[tried].tables_in_shared = c.tables;
+            out->candidates[tried].global_memory = c.global;
             out->candidates[tried].ms = ms;
         }
         tried++;
@@ -508,6 +560,8 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     s->opt.slice_steps = restore.steps;
     s->traj = restore.traj;
     s->peak_k = restore.peak;
+    restore.global = pick.global != 0;
+    s->global = restore.global;
     BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
@@ -517,7 +571,8 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     if (out) {
         out->warps_per_block = pick.warps;
         out->tables_in_shared = pick.tables;
-        out->n_candidates = std::min(tried, 16);
+        out->global_memory = pick.global;
+        out->n_candidates = std::min(tried, 32);
         out->calib_reactors = (int32_t)n_cal;
     }
     int st = 0;
@@ -598,6 +653,7 @@ int cb_reactors_integrate(cb_reactors* s, cb_reactor_stats* stats) {
         stats->ms = ms;
         stats->warps_per_block = s->warps;
         stats->tables_in_shared = s->smem_tables;
+        stats->global_memory = s->global ? 1 : 0;
         stats->graph_replays = replays;
         stats->slices = replays * G;
     }

@@ -52,6 +52,7 @@ struct Params {
     uint32_t tab_bytes;
     int smem_tables;
     int off_csr_start, off_csr;  // per-species reaction lists inside the blob
+    int off_eff_t;               // the third-body efficiencies transposed, [K][n_eff], inside the blob
     int K, A, R, N, LD, n_eff;
     uint32_t ws_bytes;           // per-warp workspace
     int n;
@@ -83,6 +84,9 @@ struct Params {
     double* traj;
     int n_points, peak_k;
     double* peak_state;
+    // Shared-memory workspaces: kf, pK, sM of the Jacobian per warp slot, [slots][3 R] (null: in the
+    // workspace).
+    double* jac_ws;
 };
 
 
@@ -150,11 +154,14 @@ struct Work {
     int* piv;
 };
 
-__host__ __device__ inline size_t workspace_doubles(int K, int A, int R, int N, int LD, int n_eff) {
-    return (size_t)N * LD + (size_t)kDRows * N + 8 * (size_t)N + K + 2 * (size_t)A + n_eff + A + K + 4 * (size_t)R + N;
+// Doubles of one warp's workspace; jac_parts: with the Jacobian's kf, pK, sM (global-memory workspaces).
+__host__ __device__ inline size_t workspace_doubles(int K, int A, int R, int N, int LD, int n_eff, bool jac_parts) {
+    return (size_t)N * LD + (size_t)kDRows * N + 8 * (size_t)N + K + 2 * (size_t)A + n_eff + A + K +
+           (jac_parts ? 4 : 1) * (size_t)R + N;
 }
 
-__device__ inline Work carve(const Params& p, uint8_t* base) {
+// The workspace of warp slot `slot` at `base`.
+__device__ inline Work carve(const Params& p, uint8_t* base, size_t slot) {
     Work w;
     double* q = reinterpret_cast<double*>(base);
     auto take = [&](size_t n) {
@@ -180,9 +187,16 @@ __device__ inline Work carve(const Params& p, uint8_t* base) {
     w.hk = take(p.A);
     w.cpk = take(p.K);
     w.cR = take(p.R);
-    w.kf = take(p.R);
-    w.pK = take(p.R);
-    w.sM = take(p.R);
+    if (p.jac_ws) {
+        double* j = p.jac_ws + slot * 3 * (size_t)p.R;
+        w.kf = j;
+        w.pK = j + p.R;
+        w.sM = j + 2 * (size_t)p.R;
+    } else {
+        w.kf = take(p.R);
+        w.pK = take(p.R);
+        w.sM = take(p.R);
+    }
     w.rdiag = take(N);
     w.piv = reinterpret_cast<int*>(q);
     return w;
@@ -192,27 +206,29 @@ struct Mech {
     RatesTables tb;
     const int* csr_start;
     const int* csr;
+    const double* eff_t;  // [K][n_eff]
     __device__ Mech(const uint8_t* tab, const Params& p)
         : tb(tab), csr_start(reinterpret_cast<const int*>(tab + p.off_csr_start)),
-          csr(reinterpret_cast<const int*>(tab + p.off_csr)) {}
+          csr(reinterpret_cast<const int*>(tab + p.off_csr)),
+          eff_t(reinterpret_cast<const double*>(tab + p.off_eff_t)) {}
 };
 
 struct RhsOut {
     double T, V, md, Ctot, S, E, Cp, dtE;
 };
 
-// One third-body sum sum_k E_k C_k in four interleaved partial sums (independent FMA chains), added
-// pairwise at the end.
-__device__ __forceinline__ double eff_dot(const double* E, const double* C, int K) {
+// Third-body sum e, sum_k E_ek C_k, from the transposed table Et [K][ld] (lanes on consecutive rows e
+// read consecutive doubles), in four interleaved partial sums added pairwise at the end.
+__device__ __forceinline__ double eff_dot(const double* Et, int ld, int e, const double* C, int K) {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     int k = 0;
     for (; k + 3 < K; k += 4) {
-        s0 = fma(E[k], C[k], s0);
-        s1 = fma(E[k + 1], C[k + 1], s1);
-        s2 = fma(E[k + 2], C[k + 2], s2);
-        s3 = fma(E[k + 3], C[k + 3], s3);
+        s0 = fma(Et[(size_t)k * ld + e], C[k], s0);
+        s1 = fma(Et[(size_t)(k + 1) * ld + e], C[k + 1], s1);
+        s2 = fma(Et[(size_t)(k + 2) * ld + e], C[k + 2], s2);
+        s3 = fma(Et[(size_t)(k + 3) * ld + e], C[k + 3], s3);
     }
-    for (; k < K; k++) s0 = fma(E[k], C[k], s0);
+    for (; k < K; k++) s0 = fma(Et[(size_t)k * ld + e], C[k], s0);
     return (s0 + s1) + (s2 + s3);
 }
 
@@ -313,7 +329,7 @@ __device__ inline RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w,
         }
     }
     __syncwarp();
-    for (int e = lane; e < H.n_eff; e += 32) w.M[e] = Ctot + eff_dot(m.tb.eff + (size_t)e * K, w.C, K);
+    for (int e = lane; e < H.n_eff; e += 32) w.M[e] = Ctot + eff_dot(m.eff_t, H.n_eff, e, w.C, K);
     __syncwarp();
     c.C = w.C;
     c.ex = w.ex;
@@ -671,10 +687,12 @@ __device__ inline void lu_solve_warp(const double* A, int N, int LD, const int* 
 // row swap (whole rows), scaling and update of the panel's own columns go column by column; then the
 // panel's U rows right of it by forward substitution, and one rank-kPanel update of the trailing matrix,
 // which so is read and written once per panel instead of once per column. Every element receives the
-// same FMAs in the same order as in lu_warp. T = float: the FP32 factorisation of CB_BDF_LU32 (1 / U_kk
-// still stored as a double).
+// same FMAs in the same order as in lu_warp, and perm the same row order. T = float: the FP32
+// factorisation of CB_BDF_LU32 (1 / U_kk still stored as a double).
 template <class T>
-__device__ inline bool lu_warp_blocked(T* A, int N, int LD, int* piv, double* rdiag, int lane) {
+__device__ inline bool lu_warp_blocked(T* A, int N, int LD, int* perm, double* rdiag, int lane) {
+    for (int i = lane; i < N; i += 32) perm[i] = i;
+    __syncwarp();
     for (int kb = 0; kb < N; kb += kPanel) {
         const int ke = min(kb + kPanel, N);
         for (int k = kb; k < ke; k++) {
@@ -699,13 +717,18 @@ __device__ inline bool lu_warp_blocked(T* A, int N, int LD, int* piv, double* rd
             best = __shfl_sync(0xffffffffu, best, 0);
             bi = __shfl_sync(0xffffffffu, bi, 0);
             if (!(best > (T)0) || !(best < (sizeof(T) == 8 ? (T)1e300 : (T)1e38))) return false;
-            if (lane == 0) piv[k] = bi;
-            if (bi != k)
+            if (bi != k) {
                 for (int j = lane; j < N; j += 32) {
                     const T t = A[(size_t)k * LD + j];
                     A[(size_t)k * LD + j] = A[(size_t)bi * LD + j];
                     A[(size_t)bi * LD + j] = t;
                 }
+                if (lane == 0) {
+                    const int t = perm[k];
+                    perm[k] = perm[bi];
+                    perm[bi] = t;
+                }
+            }
             __syncwarp();
             const T rp = (T)1 / A[(size_t)k * LD + k];
             if (lane == 0) rdiag[k] = (double)rp;
@@ -762,26 +785,65 @@ __device__ inline void transpose_warp(const T* A, T* At, int N, int LD, int lane
     __syncwarp();
 }
 
-// lu_solve_warp on the transposed factors: column k of L and U is row k of At, so every lane's reads of
+// A factor as a double: FP32 factors widened with integer instructions (off the FP64 pipe).
+__device__ __forceinline__ double as_f64(double v) { return v; }
+__device__ __forceinline__ double as_f64(float v) { return flt_to_dbl(v); }
+
+// lu_solve_regs on the transposed factors: column k of L and U is row k of At, so every lane's reads of
 // one elimination step fall in one contiguous row (global-memory matrices). Same operations and order;
 // with FP32 factors (T = float) the right-hand side and its updates stay FP64.
-template <class T>
-__device__ inline void lu_solve_t_warp(const T* At, int N, int LD, const int* piv, const double* rdiag, double* b,
-                                int lane) {
-    if (lane == 0)
-        for (int k = 0; k < N; k++) {
-            const int pk = piv[k];
-            if (pk != k) {
-                const double t = b[k];
-                b[k] = b[pk];
-                b[pk] = t;
-            }
+template <int S, class T>
+__device__ inline void lu_solve_t_regs(const T* At, int N, int LD, const int* perm, const double* rdiag, double* b,
+                                       int lane) {
+    double x[S];
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        const int i = lane + 32 * s;
+        x[s] = i < N ? b[perm[i]] : 0.0;
+    }
+    __syncwarp();
+    for (int k = 0; k < N - 1; k++) {
+        const double xk = __shfl_sync(0xffffffffu, slot_value<S>(x, k), k & 31);
+        const T* col = At + (size_t)k * LD;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (32 * s + 31 <= k) continue;
+            const int i = lane + 32 * s;
+            if (i > k && i < N) x[s] = fma(-as_f64(col[i]), xk, x[s]);
         }
+    }
+    for (int k = N - 1; k >= 0; k--) {
+        const double xk = __shfl_sync(0xffffffffu, slot_value<S>(x, k), k & 31) * rdiag[k];
+        const T* col = At + (size_t)k * LD;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (32 * s > k) continue;
+            const int i = lane + 32 * s;
+            if (i == k) x[s] = xk;
+            else if (i < k) x[s] = fma(-as_f64(col[i]), xk, x[s]);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+        const int i = lane + 32 * s;
+        if (i < N) b[i] = x[s];
+    }
+    __syncwarp();
+}
+
+// The same for any N with the right-hand side in memory (large mechanisms): b permuted through tmp, then
+// one warp barrier per elimination step.
+template <class T>
+__device__ inline void lu_solve_t_mem(const T* At, int N, int LD, const int* perm, const double* rdiag, double* b,
+                                      double* tmp, int lane) {
+    for (int i = lane; i < N; i += 32) tmp[i] = b[perm[i]];
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) b[i] = tmp[i];
     __syncwarp();
     for (int k = 0; k < N; k++) {
         const double bk = b[k];
         const T* col = At + (size_t)k * LD;
-        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-(double)col[i], bk, b[i]);
+        for (int i = k + 1 + lane; i < N; i += 32) b[i] = fma(-as_f64(col[i]), bk, b[i]);
         __syncwarp();
     }
     for (int k = N - 1; k >= 0; k--) {
@@ -789,9 +851,17 @@ __device__ inline void lu_solve_t_warp(const T* At, int N, int LD, const int* pi
         __syncwarp();
         if (lane == 0) b[k] = bk;
         const T* col = At + (size_t)k * LD;
-        for (int i = lane; i < k; i += 32) b[i] = fma(-(double)col[i], bk, b[i]);
+        for (int i = lane; i < k; i += 32) b[i] = fma(-as_f64(col[i]), bk, b[i]);
         __syncwarp();
     }
+}
+
+template <class T>
+__device__ inline void lu_solve_t_warp(const T* At, int N, int LD, const int* perm, const double* rdiag, double* b,
+                                       double* tmp, int lane) {
+    if (N <= 64) lu_solve_t_regs<2>(At, N, LD, perm, rdiag, b, lane);
+    else if (N <= 96) lu_solve_t_regs<3>(At, N, LD, perm, rdiag, b, lane);
+    else lu_solve_t_mem(At, N, LD, perm, rdiag, b, tmp, lane);
 }
 
 // I - c J (J in LU already when `fresh`, else from global) factorised in LU (pivots, 1 / U_kk); with
@@ -1026,9 +1096,9 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
                 if constexpr (GLOBAL) {
                     if (p.lu32) {
                         const float* F = reinterpret_cast<const float*>(LUt);
-                        lu_solve_t_warp(F + (size_t)N * p.LD, N, p.LD, piv, rdiag, w.b, lane);
+                        lu_solve_t_warp(F + (size_t)N * p.LD, N, p.LD, piv, rdiag, w.b, w.tmp, lane);
                     } else {
-                        lu_solve_t_warp(LUt, N, p.LD, piv, rdiag, w.b, lane);
+                        lu_solve_t_warp(LUt, N, p.LD, piv, rdiag, w.b, w.tmp, lane);
                     }
                 } else {
                     lu_solve_warp(LU, N, p.LD, piv, rdiag, w.b, lane);
@@ -1166,7 +1236,7 @@ __device__ inline void integrate(const Params& p, const Mech& m, const Work& w, 
         lu_refresh = true;
     }
     for (int i = lane; i < kDRows * N; i += 32) Dg[i] = w.D[i];
-    hd.lu_have = lu_have ? 1 : 0;
+    hd.lu_have = (GLOBAL && lu_have) ? 1 : 0;  // only a reactor's own (global) factorisation outlives the launch
     hd.lu_refresh = lu_refresh ? 1 : 0;
     hd.c_lu = c_lu;
     if (lane == 0) {
@@ -1195,7 +1265,7 @@ __device__ __forceinline__ void slice_body(const Params& p) {
     }
     const Mech m(tab, p);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Work w = carve(p, workspace_of(p, warp));
+    const Work w = carve(p, workspace_of(p, warp), (size_t)blockIdx.x * (blockDim.x >> 5) + warp);
     for (;;) {
         int r = 0;
         if (lane == 0) r = atomicAdd(p.queue, 1);

@@ -84,14 +84,18 @@ def test_autotune_graph_replays_and_tolerance_convergence():
     tune = R.autotune(512)
     print(tune)
     assert tune["candidates"] and tune["warps_per_block"] >= 1
+    # one workspace fits in shared memory: both placements are timed
+    assert {c["global_memory"] for c in tune["candidates"]} == {0, 1}
     st = R.integrate()
+    assert st["global_memory"] == tune["global_memory"]
     print(st)
     assert st["finished"] == n and st["graph_replays"] >= 2  # 64-step slices: several replays
     res = R.results()
     import combustion_gb300 as cb
     from combustion_gb300 import reactors as RX
     tight = RX.Reactors(mech, n, rtol=1e-10, atol=1e-16, t_end=1e-3, warps_per_block=tune["warps_per_block"],
-                        tables_in_shared=tune["tables_in_shared"])
+                        tables_in_shared=tune["tables_in_shared"],
+                        flags=RX.GLOBAL_MEMORY if tune["global_memory"] else 0)
     tight.set_state(*state)
     st2 = tight.integrate()
     ref = tight.results()
