@@ -240,7 +240,7 @@ def run_reactors(args, rank):
     state = RX.initial_states(m.K, n, seed=4)
     R = RX.Reactors(mech, n, rtol=1e-6, atol=1e-12, t_end=1e-3)
     R.set_state(*state)
-    tune = R.autotune(2048)
+    tune = R.autotune(0)
     st = R.integrate()
     res = R.results()
     n_ref = min(256, n)
@@ -269,6 +269,7 @@ def run_reactors(args, rank):
         "jacobians": st["jacobians"], "finished": st["finished"], "failed": st["failed"],
         "launch": {"warps_per_block": st["warps_per_block"], "tables_in_shared": st["tables_in_shared"],
                    "workspaces": "global memory" if st["global_memory"] else "shared memory",
+                   "register_cap": st["register_cap"],
                    "graph_replays": st["graph_replays"], "slices": st["slices"], "autotune": tune["candidates"]},
         "ignition_delay_vs_rtol_1e-10": {"reactors": int(ok.sum()), "max_rel": float(rel.max()) if rel.size else None,
                                           "median_rel": float(np.median(rel)) if rel.size else None},

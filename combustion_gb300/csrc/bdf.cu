@@ -92,6 +92,7 @@ struct cb_reactors {
     // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, pivots and 1 / U_kk.
     bool global = false;
     bool smem_ok = false;  // one workspace fits in shared memory and CB_BDF_GLOBAL_MEMORY is not set
+    bool wide = false;     // global memory: the 128-register kernel (two blocks per SM) instead of 64
     uint8_t* ws = nullptr;
     size_t ws_slots = 0;
     double *LUr = nullptr, *LUt = nullptr, *rdiag_r = nullptr;
@@ -221,7 +222,8 @@ cudaError_t ensure_global(cb_reactors* s) {
 // in shared or global memory.
 SliceFn slice_fn(const cb_reactors* s) {
     const bool mixed = (s->opt.flags & CB_BDF_MIXED_RHS) != 0;
-    return s->global ? slice_kernel_global_fn(mixed) : slice_kernel_fn(mixed);
+    if (!s->global) return slice_kernel_fn(mixed);
+    return s->wide ? slice_kernel_global_wide_fn(mixed) : slice_kernel_global_fn(mixed);
 }
 
 // Shared-memory limit and grid of a launch shape (outside any stream capture).
@@ -481,19 +483,22 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     BDF_CUDA(cudaSetDevice(s->device));
     // candidates: workspaces in shared or global memory, reactors in flight per block, tables in shared
     // memory or read through L1
-    struct Cand { int warps, tables, global; };
+    struct Cand { int warps, tables, global, wide; };
     std::vector<Cand> cands;
-    const bool placement = s->global;
+    const bool placement = s->global, wide = s->wide;
     for (int g = s->smem_ok ? 0 : 1; g <= 1; g++) {
         s->global = g != 0;
         for (int tables = 1; tables >= 0; tables--)
             for (int w = 1; w <= 8; w++)
-                if (shape_fits(s, w, tables) && (!g || (w & (w - 1)) == 0)) cands.push_back({w, tables, g});
+                if (shape_fits(s, w, tables) && (!g || (w & (w - 1)) == 0)) {
+                    cands.push_back({w, tables, g, 0});
+                    if (g && w >= 4) cands.push_back({w, tables, g, 1});  // 128 registers: full blocks only
+                }
     }
     s->global = placement;
     if (cands.empty()) return cbi::fail(CB_ERR_UNSUPPORTED, "no launch shape fits");
     // calibrate on copies of the state: a few slices of the first reactors, then restore the state
-    const size_t n_def = s->smem_ok ? 4096 : 512;
+    const size_t n_def = s->smem_ok ? 8192 : 512;
     const size_t n_cal = std::min<size_t>(s->n, calib_reactors > 0 ? (size_t)calib_reactors : n_def);
     const size_t hb = s->n * sizeof(Head), db = s->n * kDRows * (size_t)s->N * sizeof(double);
     std::vector<uint8_t> h0(hb), d0(db);
@@ -506,15 +511,16 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         size_t n;
         int steps, peak;
         double* traj;
-        bool global;
+        bool global, wide;
         ~Restore() {
             s->n = n;
             s->opt.slice_steps = steps;
             s->traj = traj;
             s->peak_k = peak;
             s->global = global;
+            s->wide = wide;
         }
-    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj, s->global};
+    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj, placement, wide};
     s->traj = nullptr;
     s->peak_k = -1;
     s->n = n_cal;
@@ -530,6 +536,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         cudaMemcpy(s->D, d0.data(), n_cal * kDRows * (size_t)s->N * sizeof(double), cudaMemcpyHostToDevice);
         cudaMemset(s->counters, 0, 4 * sizeof(int));
         s->global = c.global != 0;
+        s->wide = c.wide != 0;
         if (s->global && ensure_global(s) != cudaSuccess) continue;
         int grid = 0;
         if (prepare_slice(s, c.warps, c.tables, &grid) != cudaSuccess) continue;
@@ -546,6 +553,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
             out->candidates[tried].warps_per_block = c.warps;
             out->candidates[tried].tables_in_shared = c.tables;
             out->candidates[tried].global_memory = c.global;
+            out->candidates[tried].register_cap = c.global ? (c.wide ? 128 : 64) : 0;
             out->candidates[tried].ms = ms;
         }
         tried++;
@@ -561,7 +569,9 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     s->traj = restore.traj;
     s->peak_k = restore.peak;
     restore.global = pick.global != 0;
+    restore.wide = pick.wide != 0;
     s->global = restore.global;
+    s->wide = restore.wide;
     BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
@@ -572,6 +582,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         out->warps_per_block = pick.warps;
         out->tables_in_shared = pick.tables;
         out->global_memory = pick.global;
+        out->register_cap = pick.global ? (pick.wide ? 128 : 64) : 0;
         out->n_candidates = std::min(tried, 32);
         out->calib_reactors = (int32_t)n_cal;
     }
@@ -654,6 +665,7 @@ int cb_reactors_integrate(cb_reactors* s, cb_reactor_stats* stats) {
         stats->warps_per_block = s->warps;
         stats->tables_in_shared = s->smem_tables;
         stats->global_memory = s->global ? 1 : 0;
+        stats->register_cap = s->global ? (s->wide ? 128 : 64) : 0;
         stats->graph_replays = replays;
         stats->slices = replays * G;
     }

@@ -1288,9 +1288,16 @@ __global__ void __launch_bounds__(256, 4) slice_kernel_global(const Params p) {
     slice_body<MIXED, true>(p);
 }
 
+// The same with two blocks per SM (128 registers a thread, fewer spills, half the warps).
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 2) slice_kernel_global_wide(const Params p) {
+    slice_body<MIXED, true>(p);
+}
+
 using SliceFn = void (*)(Params);
-SliceFn slice_kernel_fn(bool mixed);         // bdf_slice.cu: workspaces in shared memory
-SliceFn slice_kernel_global_fn(bool mixed);  // bdf_slice_global.cu: workspaces in global memory
+SliceFn slice_kernel_fn(bool mixed);              // bdf_slice.cu: workspaces in shared memory
+SliceFn slice_kernel_global_fn(bool mixed);       // bdf_slice_global.cu: workspaces in global memory
+SliceFn slice_kernel_global_wide_fn(bool mixed);  // bdf_slice_global_wide.cu: the same, 128 registers
 
 }  // namespace bdf
 }  // namespace cbg

@@ -31,27 +31,28 @@ class cb_reactor_stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("steps", "rhs_evals", "jacobians", "factorizations", "newton_failures",
                                            "error_failures", "finished", "failed")] + [
         ("ms", C.c_double), ("warps_per_block", C.c_int32), ("tables_in_shared", C.c_int32),
-        ("graph_replays", C.c_int32), ("slices", C.c_int32), ("global_memory", C.c_int32), ("pad0", C.c_int32)]
+        ("graph_replays", C.c_int32), ("slices", C.c_int32), ("global_memory", C.c_int32), ("register_cap", C.c_int32)]
 
     def as_dict(self):
-        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad0"}
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 class _cand(C.Structure):
     _fields_ = [("warps_per_block", C.c_int32), ("tables_in_shared", C.c_int32), ("global_memory", C.c_int32),
-                ("pad", C.c_int32), ("ms", C.c_double)]
+                ("register_cap", C.c_int32), ("ms", C.c_double)]
 
 
 class cb_reactor_tuning(C.Structure):
     _fields_ = [("warps_per_block", C.c_int32), ("tables_in_shared", C.c_int32), ("n_candidates", C.c_int32),
-                ("calib_reactors", C.c_int32), ("global_memory", C.c_int32), ("pad0", C.c_int32),
+                ("calib_reactors", C.c_int32), ("global_memory", C.c_int32), ("register_cap", C.c_int32),
                 ("candidates", _cand * 32)]
 
     def as_dict(self):
         return {"warps_per_block": self.warps_per_block, "tables_in_shared": self.tables_in_shared,
-                "global_memory": self.global_memory, "calib_reactors": self.calib_reactors,
+                "global_memory": self.global_memory, "register_cap": self.register_cap,
+                "calib_reactors": self.calib_reactors,
                 "candidates": [{"warps_per_block": c.warps_per_block, "tables_in_shared": c.tables_in_shared,
-                                "global_memory": c.global_memory, "ms": c.ms}
+                                "global_memory": c.global_memory, "register_cap": c.register_cap, "ms": c.ms}
                                for c in self.candidates[:self.n_candidates]]}
 
 

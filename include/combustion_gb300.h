@@ -304,12 +304,13 @@ typedef struct cb_reactor_stats {
     uint64_t finished, failed;
     double ms;                  /* device time of the integration */
     int32_t warps_per_block, tables_in_shared, graph_replays, slices;
-    int32_t global_memory, pad0; /* workspaces in global (1) or shared (0) memory */
+    int32_t global_memory;       /* workspaces in global (1) or shared (0) memory */
+    int32_t register_cap;        /* global memory: the kernel's registers a thread, 64 or 128 */
 } cb_reactor_stats;
 typedef struct cb_reactor_tuning {
     int32_t warps_per_block, tables_in_shared, n_candidates, calib_reactors;
-    int32_t global_memory, pad0;
-    struct { int32_t warps_per_block, tables_in_shared, global_memory, pad; double ms; } candidates[32];
+    int32_t global_memory, register_cap;
+    struct { int32_t warps_per_block, tables_in_shared, global_memory, register_cap; double ms; } candidates[32];
 } cb_reactor_tuning;
 int cb_reactors_create(cb_mech* mech, size_t n, const cb_bdf_options* options, cb_reactors** out);
 int cb_reactors_destroy(cb_reactors* batch);
@@ -317,9 +318,9 @@ int cb_reactors_destroy(cb_reactors* batch);
 int cb_reactors_set_state(cb_reactors* batch, const double* pressure_R, const double* T, const double* V,
                           const double* amounts);
 /* Times the launch shapes that fit (reactors per block, table placement, workspaces in shared or global
- * memory; global only with CB_BDF_GLOBAL_MEMORY or when one workspace does not fit in shared memory) on
- * copies of the first calib_reactors reactors (0: 4096, or 512 with global memory only) and keeps the
- * fastest; the state is left as it was. */
+ * memory, and for global memory the kernel's register cap; global only with CB_BDF_GLOBAL_MEMORY or when
+ * one workspace does not fit in shared memory) on copies of the first calib_reactors reactors (0: 8192,
+ * or 512 with global memory only) and keeps the fastest; the state is left as it was. */
 int cb_reactors_autotune(cb_reactors* batch, int32_t calib_reactors, cb_reactor_tuning* result);
 /* Integrates every reactor to t_end (autotuning first when the shape is not set). */
 int cb_reactors_integrate(cb_reactors* batch, cb_reactor_stats* stats);
