@@ -36,6 +36,47 @@ def test_library_exports_every_declared_symbol():
     assert "sm_103a" in cb.version()
 
 
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    """Every ctypes Structure the Python side passes through the C ABI has the size and field offsets
+    that a C compiler gives the header's struct of the same name."""
+    import ctypes
+    import shutil
+    import subprocess
+    import combustion_gb300 as cb
+    from combustion_gb300 import reactors, surrogate
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = [cls for mod in (cb, reactors, surrogate) for cls in vars(mod).values()
+               if isinstance(cls, type) and issubclass(cls, ctypes.Structure) and cls.__name__.startswith("cb_")]
+    assert {"cb_bdf_options", "cb_reactor_stats", "cb_reactor_tuning"} <= {c.__name__ for c in mirrors}
+    lines, expect = [], {}
+    for cls in mirrors:
+        t = cls.__name__
+        lines.append(f'printf("{t} %zu\\n", sizeof({t}));')
+        expect[t] = ctypes.sizeof(cls)
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{t}.{f} %zu\\n", offsetof({t}, {f}));')
+            expect[f"{t}.{f}"] = getattr(cls, f).offset
+    # the autotuner's candidate records, an anonymous struct inside cb_reactor_tuning
+    cand = reactors.cb_reactor_tuning._fields_[-1][1]._type_
+    lines.append('printf("cand %zu\\n", sizeof(((cb_reactor_tuning*)0)->candidates[0]));')
+    expect["cand"] = ctypes.sizeof(cand)
+    for f, _ in cand._fields_:
+        lines.append(f'printf("cand.{f} %zu\\n", offsetof(cb_reactor_tuning, candidates[0].{f}) - '
+                     f'offsetof(cb_reactor_tuning, candidates));')
+        expect[f"cand.{f}"] = getattr(cand, f).offset
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "combustion_gb300.h"\nint main(void) {\n'
+                   + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    bad = {k: (int(got[k]), v) for k, v in expect.items() if int(got[k]) != v}
+    assert not bad, bad
+
+
 def test_validate_counts_and_sizes():
     cb = _cb()
     for config, (K, R) in {"k10": (10, 25), "k53": (53, 325)}.items():
