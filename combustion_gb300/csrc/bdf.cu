@@ -5,9 +5,9 @@
 // rates function's outputs, reaction.rs:356-391) and the cvode crate's BDF (cvode/lib.rs:17-47: CV_BDF,
 // dense linear solver, difference-quotient Jacobian). Here many reactors advance together: each warp
 // owns one reactor at a time, taken from a work queue, and keeps its iteration matrix (LU with partial
-// pivoting), difference array and rates scratch in shared memory (in global memory when they do not fit,
-// for large mechanisms: then each reactor keeps its own factorisation, made by panels, with a
-// transposed copy for coalesced triangular solves); the rates program runs
+// pivoting), difference array and rates scratch in shared memory, or in global memory (large mechanisms,
+// or where the autotuner finds it faster: then each reactor keeps its own factorisation, made by panels,
+// with a transposed copy for coalesced triangular solves); the rates program runs
 // warp-cooperatively (lanes split species, third-body rows and reactions; per-species sums in the
 // reactions' order). Launches are slices of at most `slice_steps` steps per reactor so that reactors of
 // uneven stiffness rebalance between launches; a CUDA graph replays the slice sequence.

@@ -265,8 +265,10 @@ int cb_yaml_free(cb_yaml_mech* mech);
  * Replaces the reactor loop of plot.rs:32-118 with the cvode crate's role (cvode/lib.rs:17-47: BDF,
  * dense Newton): state u = [T, V, n_0 .. n_{A-1}] at fixed P/R, du/dt = the outputs of cb_rates_f64 for
  * that state (reaction.rs:356-391). Needs every non-bulk species active (A = K - 1). Up to 65 species a
- * reactor's workspace sits in shared memory; above, in global memory (24 (K + 1)^2 bytes per reactor
- * for its Jacobian and factorisation, plus about 0.6 MB per reactor in flight at 250 species).
+ * reactor's workspace fits in shared memory, and the autotuner chooses between that placement and global
+ * memory (at 53 species it picks global: more warps per SM); above, always global memory (24 (K + 1)^2
+ * bytes per reactor for its Jacobian and factorisation, plus about 0.6 MB per reactor in flight at 250
+ * species).
  * Every reactor is integrated from t = 0 to t_end with its own step size and order (1-5) against
  * atol + rtol |u_i| for every component; its ignition delay is the time of the largest dT/dt (the
  * vertex of a parabola through the samples around it). The host side is synchronous. */
@@ -290,9 +292,9 @@ typedef struct cb_bdf_options {
  * for at most 20 steps (the Newton correction is then scaled by 2 / (1 + c / c_lu), as in CVODE); the
  * factorisation also carries over between launches when it lives in global memory. */
 #define CB_BDF_REUSE_LU 2u
-/* Workspaces and factorisations in global memory even when one reactor's fit in shared memory (they go
- * there by themselves for large mechanisms; without CB_BDF_REUSE_LU the integration takes the same
- * steps either way). */
+/* Workspaces and factorisations in global memory only, even when one reactor's fit in shared memory
+ * (without this flag the autotuner times both placements; large mechanisms always use global memory;
+ * without CB_BDF_REUSE_LU the integration takes the same steps either way). */
 #define CB_BDF_GLOBAL_MEMORY 4u
 /* With workspaces in global memory: factorise I - c J in FP32 (the FP32 pipe is many times the FP64 one
  * on this GPU). The Newton residuals, corrections and triangular-solve accumulations stay FP64, so a
