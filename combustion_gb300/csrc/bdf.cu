@@ -537,7 +537,10 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         cudaMemset(s->counters, 0, 4 * sizeof(int));
         s->global = c.global != 0;
         s->wide = c.wide != 0;
-        if (s->global && ensure_global(s) != cudaSuccess) continue;
+        if (s->global && ensure_global(s) != cudaSuccess) {
+            cudaGetLastError();  // out of memory for the global placement: its candidates are skipped
+            continue;
+        }
         int grid = 0;
         if (prepare_slice(s, c.warps, c.tables, &grid) != cudaSuccess) continue;
         cudaEventRecord(a, s->stream);
