@@ -88,8 +88,8 @@ struct cb_reactors {
     bool have_state = false;
     cudaStream_t stream = nullptr;
     uint8_t* d_tab_m = nullptr;  // mixed-precision rates tables (CB_BDF_MIXED_RHS)
-    // Workspaces in global memory when one warp's does not fit in shared memory (large mechanisms):
-    // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, pivots and 1 / U_kk.
+    // Workspaces in global memory (large mechanisms, CB_BDF_GLOBAL_MEMORY or the autotuner's choice):
+    // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, row order and 1 / U_kk.
     bool global = false;
     bool smem_ok = false;  // one workspace fits in shared memory and CB_BDF_GLOBAL_MEMORY is not set
     bool wide = false;     // global memory: the 128-register kernel (two blocks per SM) instead of 64
@@ -207,13 +207,21 @@ cudaError_t ensure_slots(cb_reactors* s, size_t slots) {
 // (s->global set; outside any stream capture).
 cudaError_t ensure_global(cb_reactors* s) {
     cudaError_t e = cudaSuccess;
-    if (!s->LUr) {
+    if (!s->LUr) {  // all four or none: a partial allocation is released
         const size_t per = (size_t)s->N * s->LD, n = s->capacity;
         e = cudaMalloc(&s->LUr, n * per * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&s->LUt, n * per * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&s->rdiag_r, n * (size_t)s->N * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&s->piv_r, n * (size_t)s->N * sizeof(int));
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess) {
+            cudaFree(s->LUr);
+            cudaFree(s->LUt);
+            cudaFree(s->rdiag_r);
+            cudaFree(s->piv_r);
+            s->LUr = s->LUt = s->rdiag_r = nullptr;
+            s->piv_r = nullptr;
+            return e;
+        }
     }
     return ensure_slots(s, (size_t)sm_count());
 }
