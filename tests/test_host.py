@@ -77,6 +77,26 @@ def test_ctypes_mirrors_match_the_header_layout(tmp_path):
     assert not bad, bad
 
 
+def test_python_flag_constants_match_the_header():
+    """The flag values the Python side passes (CB_* in the package, CB_BDF_* as reactors.<NAME>) are the
+    header's #defines."""
+    import combustion_gb300 as cb
+    from combustion_gb300 import reactors, surrogate
+    text = open(os.path.join(ROOT, "include", "combustion_gb300.h")).read()
+    defines = {k: int(v) for k, v in re.findall(r"^#define (CB_\w+) (\d+)u", text, re.M)}
+    checked = 0
+    for mod in (cb, surrogate):
+        for name, value in vars(mod).items():
+            if name.startswith("CB_") and isinstance(value, int):
+                assert defines[name] == value, name
+                checked += 1
+    for name, value in defines.items():
+        if name.startswith("CB_BDF_"):
+            assert getattr(reactors, name[len("CB_BDF_"):]) == value, name
+            checked += 1
+    assert checked >= 8
+
+
 def test_validate_counts_and_sizes():
     cb = _cb()
     for config, (K, R) in {"k10": (10, 25), "k53": (53, 325)}.items():
