@@ -256,10 +256,12 @@ cudaError_t launch_slice(cb_reactors* s, int warps, int tables, int grid, cudaSt
 bool shape_fits(cb_reactors* s, int warps, int tables) { return (int)smem_bytes(s, warps, tables) <= max_smem(); }
 
 // Scratch of cb_reactors_eval_noalloc, in the module's static device memory instead of cudaMalloc:
-// states, pressures, du/dt and Jacobians of one call, at most kEvalScratchDoubles doubles (4 MiB; 167
-// states at 53 species). Its address is resolved once per device (cudaGetSymbolAddress) by the first
-// call on that device. Every element a call reads back is written by that call's kernel, so nothing in
-// it has to start at zero; two calls in flight at once on one device share it and race.
+// states, pressures, du/dt and Jacobians of one call, at most kEvalScratchDoubles doubles (4 MiB; 173
+// states at 53 species, N = 54). Its address is resolved once per device (cudaGetSymbolAddress) by the
+// first call on that device and cached for the life of the process: a cudaDeviceReset (or anything else
+// that destroys the device's primary context) invalidates it. Every element a call reads back is written
+// by that call's kernel, so nothing in it has to start at zero; two calls in flight at once on one device
+// share it and race.
 constexpr size_t kEvalScratchDoubles = (size_t)1 << 19;
 constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_eval_scratch[kEvalScratchDoubles];
@@ -737,6 +739,9 @@ int cb_reactors_eval(cb_reactors* s, int32_t m, const double* pressure_R, const 
     if (e == cudaSuccess) e = cudaMemcpy(dy, states, (size_t)m * N * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(dp, pressure_R, (size_t)m * sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cleanup(cbi::cuda_fail(e, "evaluation buffers"));
+    // The staging-timeout status word is this call's own: a bit left by an earlier launch is cleared.
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->counters + 2, 0, sizeof(int), s->stream);
+    if (e != cudaSuccess) return cleanup(cbi::cuda_fail(e, "evaluation status"));
     Params p = params(s, shape_fits(s, 1, 1) ? 1 : 0);
     p.pR = dp;
     p.eval_y = dy;
@@ -792,6 +797,7 @@ int cb_reactors_eval_noalloc(cb_reactors* s, int32_t m, const double* pressure_R
     cudaStream_t st = s->stream;
     BDF_CUDA(cudaMemcpyAsync(dy, states, (size_t)m * N * sizeof(double), cudaMemcpyHostToDevice, st));
     BDF_CUDA(cudaMemcpyAsync(dp, pressure_R, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, st));
+    BDF_CUDA(cudaMemsetAsync(s->counters + 2, 0, sizeof(int), st));  // this call's own staging status
     Params p = params(s, shape_fits(s, 1, 1) ? 1 : 0);
     p.pR = dp;
     p.eval_y = dy;

@@ -348,10 +348,11 @@ int cb_reactors_eval(cb_reactors* batch, int32_t m, const double* pressure_R, co
 /* cb_reactors_eval without any device allocation; no reference counterpart. For callers that evaluate
  * du/dt and Jacobians inside a time-critical host loop and must not allocate per call (cudaFree
  * synchronises the whole device; under a caching allocator cudaMalloc can fail). Device staging is a
- * fixed 4 MiB static buffer of the library: m is limited to 2^19 / (N^2 + 2N + 1) states (167 at 53
- * species; larger m fails with CB_ERR_INVALID). The first call on a device resolves that buffer's
- * address (cudaGetSymbolAddress): make it before any stream capture. Calls in flight at the same time
- * on one device share the buffer and race. */
+ * fixed 4 MiB static buffer of the library: m is limited to 2^19 / (N^2 + 2N + 1) states (173 at 53
+ * species, N = 54; larger m fails with CB_ERR_INVALID). The first call on a device resolves that
+ * buffer's address (cudaGetSymbolAddress) and keeps it for the life of the process: make that call
+ * before any stream capture, and not across a cudaDeviceReset (which invalidates the kept address).
+ * Calls in flight at the same time on one device share the buffer and race. */
 int cb_reactors_eval_noalloc(cb_reactors* batch, int32_t m, const double* pressure_R, const double* states,
                              double* f, double* J);
 

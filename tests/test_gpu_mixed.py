@@ -1,7 +1,9 @@
 """The mixed-precision form against the FP64 oracle, through the C ABI.
 
 Stated error bar: 1e-4 per output, relative to the output's condition scale (the metric of the plain
-form's 1e-12 bar). Max and RMS errors per output group are printed.
+form's 1e-12 bar). Max and RMS errors per output group are printed: condition-scaled, pure relative,
+and for species rates the reference's floored metric |x - r| / max(r, 1e3) (cantera.rs:147). Transport
+outputs barely cancel, so their pure relative error is asserted at the same 1e-4 bar.
 """
 import os
 
@@ -34,14 +36,21 @@ def _dev(rows):
 
 
 def _report(name, x, ref, scale):
+    """Condition-scaled error, pure relative error (max and RMS, unclipped) and, for species rates, the
+    reference's floored metric; returns the condition-scaled errors."""
     ce = util.cond_err(x, ref, scale)
     re = util.rel_err(x, ref)
-    print(f"{name}: cond err max {ce.max():.2e} rms {np.sqrt((ce ** 2).mean()):.2e}; "
-          f"rel err median {np.median(re):.2e} rms(99%) {np.sqrt((np.minimum(re, np.quantile(re, 0.99)) ** 2).mean()):.2e}")
+    line = (f"{name}: cond err max {ce.max():.2e} rms {np.sqrt((ce ** 2).mean()):.2e}; "
+            f"rel err max {re.max():.2e} rms {np.sqrt((re ** 2).mean()):.2e}")
+    if "species" in name:
+        fe, fa = util.floored_err(x, ref), util.floored_abs_err(x, ref)
+        line += (f"; floored max {fe.max():.2e} rms {np.sqrt((fe ** 2).mean()):.2e}"
+                 f" (on |r|: max {fa.max():.2e} rms {np.sqrt((fa ** 2).mean()):.2e})")
+    print(line)
     return ce
 
 
-@pytest.mark.parametrize("config,n", [("k10", 65536), ("k53", 16384)])
+@pytest.mark.parametrize("config,n", [("k10", 65536), ("k53", 16384), ("k250", 2048)])
 def test_mixed_rates_and_transport(config, n):
     import torch
     from combustion_gb300 import synthetic
@@ -64,6 +73,7 @@ def test_mixed_rates_and_transport(config, n):
     assert _report(f"mixed transport {config} lambda", tt[:1], tref[:1], tsc[:1]).max() <= MIXED_TOL
     assert _report(f"mixed transport {config} mu", tt[1:2], tref[1:2], tsc[1:2]).max() <= MIXED_TOL
     assert _report(f"mixed transport {config} rhoD", tt[2:], tref[2:], tsc[2:]).max() <= MIXED_TOL
+    assert util.rel_err(tt, tref).max() <= MIXED_TOL
 
 
 @pytest.mark.parametrize("name", ["branches", "sri"])
