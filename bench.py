@@ -111,11 +111,10 @@ def run_reference(args):
         return
     import oracle
     from combustion_gb300 import synthetic
-    import combustion_gb300 as cb
     m = synthetic.generate_mechanism(CONFIG)
     scales = synthetic.transport_scales(m)
     o = oracle.Oracle(m)
-    o.set_transport(*scales, *cb.transport_fit(m, scales[0]))
+    o.set_transport(*scales, *o.fit(scales[0]))  # the oracle's own fit: nothing of the library is loaded
     threads = os.cpu_count() or 1
     n = args.ref_cells
     rates = []
@@ -134,7 +133,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "cells_per_step": n, "form": "plain_f64",
-                   "implementation": "oracle/oracle.c: C restatement of the reference interpreter (Rust not buildable here)"},
+                   "implementation": "oracle/oracle.c: C restatement of the reference interpreter (Rust not buildable here)",
+                   "rate": "per-cell rate: each step evaluates a bounded sample of %d cells of the same seeded "
+                           "2^22-cell workload (the GPU arm's step is all 2^22 cells)" % n},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -147,6 +148,30 @@ def measured_bf16_peak():
         if v:
             return float(v), "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst), of measured"
     return 1900.0, "fallback 1.9 PFLOP/s bf16, of fallback"
+
+
+RATES_GROUPS = (("dTdt", slice(0, 1)), ("dVdt", slice(1, 2)), ("species", slice(2, None)))
+TRANSPORT_GROUPS = (("conductivity", slice(0, 1)), ("viscosity", slice(1, 2)), ("diffusion", slice(2, None)))
+
+
+def error_block(x, ref, scale, groups):
+    """Per output group, max and RMS of: the condition-scaled error |x - r| / scale (scale: the sum of
+    magnitudes of the terms the output accumulates, from the oracle), the pure relative error
+    |x - r| / |r|, and for species rates the reference's floored metric |x - r| / max(r, 1e3)
+    (cantera.rs:147, r signed as written there) and the same floor on |r|."""
+    def mr(e):
+        e = e.ravel()
+        return {"max": float(e.max()), "rms": float(np.sqrt(np.mean(e * e)))}
+    d = np.abs(x - ref)
+    out = {}
+    for name, rows in groups:
+        g = {"cond": mr(d[rows] / np.maximum(scale[rows], 1e-300)),
+             "rel": mr(d[rows] / np.maximum(np.abs(ref[rows]), 1e-300))}
+        if name == "species":
+            g["floored"] = mr(d[rows] / np.maximum(ref[rows], 1e3))
+            g["floored_abs"] = mr(d[rows] / np.maximum(np.abs(ref[rows]), 1e3))
+        out[name] = g
+    return out
 
 
 def rel_err_groups(x, ref):
@@ -280,12 +305,12 @@ def run_reactors(args, rank):
     }
 
 
-def run_large(args):
-    """The large-mechanism configuration (K = 250, R = 1,500; opt-in with --large): plain FP64 and mixed
-    rates+transport on 2^20 device-generated cells, the width-512 surrogate (252 -> 512 x 4 -> 252) trained
-    on 2^23 plain-kernel cells and run gated on the same cells, and args.large_reactors constant-pressure
-    reactors of the 250-species reactor variant to 1 ms (workspaces in global memory), in the mixed form
-    (mixed-precision first Newton iterations, FP32 factorisation, kept factorisations) and in plain FP64."""
+def run_large(args, with_learned):
+    """The large-mechanism configuration (K = 250, R = 1,500) on 2^20 device-generated cells: plain FP64
+    and mixed rates+transport, each timed and checked against the FP64 oracle on 256 sampled cells
+    (always run: about 10 s). With ``with_learned`` (--large) also the width-512 surrogate
+    (252 -> 512 x 4 -> 252) trained on 2^23 plain-kernel cells and run gated on the same cells, and
+    args.large_reactors constant-pressure reactors of the 250-species reactor variant to 1 ms."""
     import torch
     import combustion_gb300 as cb
     import oracle
@@ -315,7 +340,7 @@ def run_large(args):
         return a.elapsed_time(b) / reps
 
     plain_ms = timed(lambda: mech.rates_transport(cells, r_out, t_out), 2)
-    mixed_ms = timed(lambda: mech.rates_transport(cells, m_r, m_t, mixed=True), 2)
+    mixed_ms = timed(lambda: mech.rates_transport(cells, m_r, m_t, mixed=True), 3)
     o = oracle.Oracle(m)
     o.set_transport(*scales, *mech.transport_coefficients())
     idx = torch.arange(0, n, n // 256, device="cuda")
@@ -325,9 +350,29 @@ def run_large(args):
     tin = [(ins[0] * ins[3]) / ins[2], ins[2] / scales[0]] + ins[4:]
     tref, tsc = o.transport(tin, nthreads=os.cpu_count() or 1, scale=True)
 
-    def cerr(x, ref, sc):
-        return float((np.abs(x.index_select(1, idx).cpu().numpy() - ref) / np.maximum(sc, 1e-300)).max())
+    def sample(x):
+        return x.index_select(1, idx).cpu().numpy()
 
+    def cerr(x, ref, sc):
+        return float((np.abs(sample(x) - ref) / np.maximum(sc, 1e-300)).max())
+
+    out = {
+        "workload": "K=250 / R=1500 (1200 reversible, 180 three-body, 120 Troe), 2^20 cells, T~U[300,3000] K, "
+                    "P log-uniform [0.1,40] atm, X~Dirichlet(0.3) (device generator)",
+        "plain_f64": {"cells_per_s": n / (plain_ms * 1e-3), "ms": plain_ms,
+                      "max_err": max(cerr(r_out, rref, rsc), cerr(t_out, tref, tsc)),
+                      "error": {"rates": error_block(sample(r_out), rref, rsc, RATES_GROUPS),
+                                "transport": error_block(sample(t_out), tref, tsc, TRANSPORT_GROUPS)},
+                      "api": "cb_rates_transport_f64 (tables read through L1: KMAX 256)"},
+        "mixed": {"cells_per_s": n / (mixed_ms * 1e-3), "ms": mixed_ms,
+                  "rates_max_err": cerr(m_r, rref, rsc), "transport_max_err": cerr(m_t, tref, tsc),
+                  "error": {"rates": error_block(sample(m_r), rref, rsc, RATES_GROUPS),
+                            "transport": error_block(sample(m_t), tref, tsc, TRANSPORT_GROUPS)},
+                  "api": "cb_rates_transport_mixed"},
+        "errors": "against the FP64 oracle on 256 sampled cells; max_err values are condition-scaled",
+    }
+    if not with_learned:
+        return out
     sur = S.Surrogate(mech, width=512, hidden_layers=4, batch=65536, lr=1e-3, lr_final=1e-5, seed=3)
     t = time.perf_counter()
     sur.generate(1 << 23, S.distribution("k250", seed=2))
@@ -338,21 +383,13 @@ def run_large(args):
     s_out = torch.empty_like(t_out)
     st = sur.transport(cells, s_out, audit_stride=1024, timing=True)
     sur_ms = timed(lambda: (mech.rates(cells, m_r, mixed=True), sur.transport(cells, s_out, audit_stride=1024)), 2)
-    return {
-        "workload": "K=250 / R=1500 (1200 reversible, 180 three-body, 120 Troe), 2^20 cells, T~U[300,3000] K, "
-                    "P log-uniform [0.1,40] atm, X~Dirichlet(0.3) (device generator)",
-        "plain_f64": {"cells_per_s": n / (plain_ms * 1e-3), "ms": plain_ms,
-                      "max_err": max(cerr(r_out, rref, rsc), cerr(t_out, tref, tsc))},
-        "mixed": {"cells_per_s": n / (mixed_ms * 1e-3), "ms": mixed_ms,
-                  "rates_max_err": cerr(m_r, rref, rsc), "transport_max_err": cerr(m_t, tref, tsc)},
-        "mixed_surrogate": {"cells_per_s": n / (sur_ms * 1e-3), "ms": sur_ms,
-                            "network": "252 -> 512 x 4 -> 252, BF16 tcgen05 (per-layer GEMMs)",
-                            "training": {"cells": 1 << 23, "steps": args.large_steps, "generate_s": gen_s,
-                                         "train_s": train_s, "loss_last": float(np.mean(losses[-20:]))},
-                            "error_network_vs_plain_f64": rel_err_groups(s_out, t_out), "gate": st},
-        "reactors": large_reactors(args) if args.large_reactors > 0 else None,
-        "errors": "condition-scaled against the FP64 oracle on 256 sampled cells",
-    }
+    out["mixed_surrogate"] = {"cells_per_s": n / (sur_ms * 1e-3), "ms": sur_ms,
+                              "network": "252 -> 512 x 4 -> 252, BF16 tcgen05 (per-layer GEMMs)",
+                              "training": {"cells": 1 << 23, "steps": args.large_steps, "generate_s": gen_s,
+                                           "train_s": train_s, "loss_last": float(np.mean(losses[-20:]))},
+                              "error_network_vs_plain_f64": rel_err_groups(s_out, t_out), "gate": st}
+    out["reactors"] = large_reactors(args) if args.large_reactors > 0 else None
+    return out
 
 
 def large_reactors(args):
@@ -483,6 +520,9 @@ def run_ours(args):
     dom = max(kern, key=lambda k: kern[k][0])
     ms, work = kern[dom]
     achieved = algorithmic_flops(work) * n / (ms * 1e-3) / 1e12
+    # the same kernel with every division, exponential, logarithm and square root counted as one flop
+    unit_flops = work["flops"] + sum(work[k] for k in SLOT_COST)
+    achieved_unit = unit_flops * n / (ms * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(tpath):
@@ -495,7 +535,7 @@ def run_ours(args):
     reactors_form = None
     if not args.no_reactors and rank == 0:
         reactors_form = run_reactors(args, rank)
-    large_form = run_large(args) if (args.large and rank == 0) else None
+    large_form = run_large(args, args.large) if (rank == 0 and not args.no_large_cells) else None
 
     # Parity of this run's outputs on a sample of cells against the FP64 oracle.
     parity = None
@@ -512,29 +552,44 @@ def run_ours(args):
         ridx = torch.from_numpy(idx).cuda()
         gr = r_out.index_select(1, ridx).cpu().numpy()
         gt = t_out.index_select(1, ridx).cpu().numpy()
+        mr = m_r_out.index_select(1, ridx).cpu().numpy()
+        mt = m_t_out.index_select(1, ridx).cpu().numpy()
+        well = rsc <= 30.0 * np.abs(rref)  # rate outputs that cancel less than 30-fold
+        rel_r = np.abs(gr - rref) / np.maximum(np.abs(rref), 1e-300)
         parity = {"cells_checked": int(len(idx)),
                   "rates_max_err": float((np.abs(gr - rref) / np.maximum(rsc, 1e-300)).max()),
                   "transport_max_err": float((np.abs(gt - tref) / np.maximum(tsc, 1e-300)).max()),
-                  "tolerance": 1e-12, "metric": "|gpu - oracle| / condition scale of the output"}
-        mr = m_r_out.index_select(1, ridx).cpu().numpy()
-        mt = m_t_out.index_select(1, ridx).cpu().numpy()
+                  "tolerance": 1e-12, "metric": "|gpu - oracle| / condition scale of the output",
+                  "plain_f64": {"rates": error_block(gr, rref, rsc, RATES_GROUPS),
+                                "transport": error_block(gt, tref, tsc, TRANSPORT_GROUPS),
+                                "rates_well_conditioned": {"fraction": float(well.mean()),
+                                                           "rel_max": float(rel_r[well].max())},
+                                "rates_frac_rel_above_1e-12": float((rel_r > 1e-12).mean())},
+                  "mixed": {"rates": error_block(mr, rref, rsc, RATES_GROUPS),
+                            "transport": error_block(mt, tref, tsc, TRANSPORT_GROUPS)},
+                  "metrics": {"cond": "|x - r| / condition scale (sum of magnitudes of the output's terms)",
+                              "rel": "|x - r| / |r|", "floored": "|x - r| / max(r, 1e3), cantera.rs:147",
+                              "floored_abs": "|x - r| / max(|r|, 1e3)",
+                              "rates_well_conditioned": "condition scale <= 30 |r|"}}
         er = np.abs(mr - rref) / np.maximum(rsc, 1e-300)
         et = np.abs(mt - tref) / np.maximum(tsc, 1e-300)
         mixed_err = {"rates_max_err": float(er.max()), "rates_rms_err": float(np.sqrt((er ** 2).mean())),
                      "transport_max_err": float(et.max()), "transport_rms_err": float(np.sqrt((et ** 2).mean())),
-                     "tolerance": 1e-4}
+                     "tolerance": 1e-4, "metric": "condition-scaled; per group in parity.mixed"}
 
     # End to end through the public fused call with host buffers.
     h_ro = torch.empty((A + 2, n), dtype=torch.float64).pin_memory().numpy()
     h_to = torch.empty((K + 2, n), dtype=torch.float64).pin_memory().numpy()
     mech.rates_transport(host_in, h_ro, h_to)  # warm-up (staging buffers)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = args.steps
     if world > 1:
         torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        mech.rates_transport(host_in, h_ro, h_to)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    with ClockSampler(local) as e2e_clocks:
+        time.sleep(0.3)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            mech.rates_transport(host_in, h_ro, h_to)
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -575,10 +630,14 @@ def run_ours(args):
                          "peak_source": "measured FP64 FMA rate of this GPU (cb_device_fp64_peak), FMA = 2 flops",
                          "flops_per_cell": algorithmic_flops(work),
                          "flop_model": "reference program ops (+-x min max = 1) plus exp/log/div/sqrt at "
-                                       "2 x {10,12,4,4} FMA slots"},
+                                       "2 x {10,12,4,4} FMA slots",
+                         "unit_weight": {"flops_per_cell": unit_flops, "achieved": achieved_unit,
+                                         "frac": achieved_unit / peak,
+                                         "flop_model": "every op, exp, log, div and sqrt = 1 flop"}},
             "cpu_baseline": cpu,
             "e2e": {"value": world * n / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": (K + 3) * 8 * n,
-                    "d2h_bytes_per_step": (A + 2 + K + 2) * 8 * n, "api": "cb_rates_transport_f64, CB_HOST_MEMORY"},
+                    "d2h_bytes_per_step": (A + 2 + K + 2) * 8 * n, "api": "cb_rates_transport_f64, CB_HOST_MEMORY",
+                    "steps": e2e_steps, "clocks": e2e_clocks.summary()},
             "gpu_launches": 2 * args.steps,
             "clocks": clk,
             "parity": parity,
@@ -610,7 +669,9 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-reactors", action="store_true")
     ap.add_argument("--reactors", type=int, default=16384)
-    ap.add_argument("--large", action="store_true", help="also run the K = 250 configuration")
+    ap.add_argument("--large", action="store_true",
+                    help="also run the K = 250 surrogate and reactors (its plain and mixed cells always run)")
+    ap.add_argument("--no-large-cells", action="store_true", help="skip the K = 250 plain and mixed cells")
     ap.add_argument("--large-steps", type=int, default=6000)
     ap.add_argument("--large-reactors", type=int, default=4096, help="K = 250 reactors in --large (0: none)")
     ap.add_argument("--sur-train-cells", type=int, default=1 << 24)
@@ -620,6 +681,18 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    world_env = os.environ.get("WORLD_SIZE")
+    if world_env is None and args.gpus > 1:
+        # one process per GPU: launch this script again under torch.distributed.run
+        import socket
+        with socket.socket() as sock:
+            sock.bind(("127.0.0.1", 0))
+            port = sock.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
+    if world_env is not None and int(world_env) != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} does not match WORLD_SIZE={world_env}")
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -40,7 +40,7 @@ EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_que
            "cb_surrogate_get_params", "cb_surrogate_set_params", "cb_surrogate_normalisation",
            "cb_surrogate_evaluate", "cb_reactors_create", "cb_reactors_destroy", "cb_reactors_set_state",
            "cb_reactors_autotune", "cb_reactors_integrate", "cb_reactors_results", "cb_reactors_eval",
-           "cb_reactors_eval_noalloc", "cb_yaml_load", "cb_yaml_desc", "cb_yaml_free"]
+           "cb_reactors_eval_noalloc", "cb_yaml_load", "cb_yaml_desc", "cb_yaml_free", "cb_debug_stage_wait_polls"]
 
 
 class CombustionError(RuntimeError):
@@ -100,6 +100,7 @@ def lib():
         L.cb_version.restype = C.c_char_p
         L.cb_device_fp64_peak.argtypes = [C.POINTER(C.c_double)]
         L.cb_fp64_math.argtypes = [C.c_int, vp, vp, sz, vp]
+        L.cb_debug_stage_wait_polls.argtypes = [C.c_int64]
         _lib = L
     return _lib
 
@@ -296,6 +297,11 @@ def fp64_math(which: str, x):
     y = torch.empty_like(x)
     _check(lib().cb_fp64_math(code, x.data_ptr(), y.data_ptr(), x.numel(), torch.cuda.current_stream().cuda_stream))
     return y
+
+
+def debug_stage_wait_polls(polls: int) -> None:
+    """Test hook: polls of the plain FP64 kernels' first table-staging wait (negative: the default)."""
+    _check(lib().cb_debug_stage_wait_polls(int(polls)))
 
 
 def version() -> str:

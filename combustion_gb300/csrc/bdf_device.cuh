@@ -273,7 +273,7 @@ __device__ __forceinline__ void rates_group_warp(const Mech& m, const Work& w, c
     for (int r = (MODEL ? H.group_end[MODEL - 1] : 0) + lane; r < end; r += 32) {
         const Reaction& x = m.tb.reactions[r];
         ReactionParts pp;
-        w.cR[r] = reaction_eval<MODEL, PARTS>(m.tb, x, c, &pp);
+        w.cR[r] = reaction_eval<MODEL, PARTS>(m.tb, x, c, MODEL >= 2 ? c.M[x.eff_row] : 0.0, &pp);
         if (PARTS) {
             w.kf[r] = pp.kf;
             w.pK[r] = pp.pK;
@@ -384,8 +384,10 @@ struct WarpCellM {
 template <int MODEL>
 __device__ __forceinline__ void rates_group_warp_m(const RatesMixedTables& tm, const Work& w, const WarpCellM& c, int lane) {
     const int end = tm.H->group_end[MODEL];
-    for (int r = (MODEL ? tm.H->group_end[MODEL - 1] : 0) + lane; r < end; r += 32)
-        w.cR[r] = reaction_rate_m<MODEL>(tm, tm.reactions[r], c);
+    for (int r = (MODEL ? tm.H->group_end[MODEL - 1] : 0) + lane; r < end; r += 32) {
+        const ReactionF& x = tm.reactions[r];
+        w.cR[r] = reaction_rate_m<MODEL>(tm, x, c, MODEL >= 2 ? c.Mf[x.eff_row] : 0.f);
+    }
 }
 
 // du/dt by the mixed-precision rates program (the arithmetic of kernels_mixed.cu's rates_mixed_cell,

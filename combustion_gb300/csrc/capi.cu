@@ -543,6 +543,11 @@ int cb_fp64_math(int which, const double* x, double* y, size_t n, void* stream) 
     return e == cudaSuccess ? CB_OK : cuda_fail(e, "math check");
 }
 
+int cb_debug_stage_wait_polls(int64_t polls) {
+    CB_CUDA(cbg::set_stage_wait_polls((long long)polls));
+    return CB_OK;
+}
+
 int cb_synchronize(cb_mech* m, void* stream) {
     if (!m) return fail(CB_ERR_INVALID, "null mechanism");
     CB_CUDA(cudaSetDevice(m->device));

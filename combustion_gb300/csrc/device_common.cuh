@@ -11,6 +11,11 @@ enum DeviceStatus : int { kStatusStageTimeout = 1 };
 // Spin limits for every wait in these kernels: a wait that runs out sets a status bit and returns.
 constexpr long long kWaitLimit = 1ll << 24;
 
+// Polls of stage_to_shared's first wait (one copy per translation unit). Only a test hook lowers it
+// (cb_debug_stage_wait_polls, for the plain FP64 kernels): that wait then runs out while the second,
+// full-length wait still lets the copy land before the block exits.
+static __device__ long long g_stage_wait_polls = kWaitLimit;
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
@@ -46,7 +51,8 @@ __device__ inline bool stage_to_shared(void* dst, const void* src, uint32_t byte
         }
     }
     bool ok = false;
-    for (long long it = 0; it < kWaitLimit; ++it)
+    const long long polls = g_stage_wait_polls;
+    for (long long it = 0; it < polls; ++it)
         if (mbar_try_wait(b, 0)) { ok = true; break; }
     if (!ok) {
         atomicOr(status, kStatusStageTimeout);

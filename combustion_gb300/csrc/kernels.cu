@@ -21,7 +21,6 @@ struct Cell {
     double Ctot, C0, rcpC0, rcpC0sq;
     double C[KMAX];              // concentrations, bulk last
     double ex[KMAX], exn[KMAX];  // min(M3, exp(g_k)), min(cbrt(f32::MAX), exp(-g_k))
-    double M[4 * KMAX];          // third-body concentrations C + sum (e_k - 1) C_k, one per efficiency row
 };
 
 // Prologue of reaction.rs:362-373 and the Gibbs exponentials of reaction.rs:234-263.
@@ -57,39 +56,48 @@ __device__ __forceinline__ void cell_setup(const RatesTables& tb, double pressur
         if (s.need_exp) c.ex[k] = min_pos(H.M3, exp64(x));
         if (s.need_exp_neg) c.exn[k] = min_pos(H.cbrt_max, exp64(-x));
     }
-    // efficiency() of every third-body / falloff reaction (reaction.rs:141-145), four rows per pass over
-    // the concentrations (rows padded to a multiple of 4): one local load of C_k per four FMAs.
-    for (int e0 = 0; e0 < H.n_eff; e0 += 4) {
-        const double* E = tb.eff + (size_t)e0 * K;
+}
+
+// Reactions without a third body (models 0 and 1), one loop per model; emit(x, cR) takes each rate.
+template <int KMAX, int MODEL, class Emit>
+__device__ __forceinline__ void plain_group(const RatesTables& tb, const Cell<KMAX>& c, Emit emit) {
+    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
+        const Reaction& x = tb.reactions[r];
+        emit(x, reaction_rate<MODEL>(tb, x, c, 0.0));
+    }
+}
+
+// Reactions with a third body (models 2-5: consecutive in the tables, efficiency row e for reaction
+// group_end[1] + e). The third-body sums efficiency() (reaction.rs:141-145) of four consecutive rows
+// (padded to a multiple of 4) take one pass over the concentrations, one local load of C_k per four
+// FMAs, just before their reactions: no array of sums is kept. The model branch is uniform across the
+// warp (every lane is at the same reaction).
+template <int KMAX, class Emit>
+__device__ __forceinline__ void third_body_groups(const RatesTables& tb, const Cell<KMAX>& c, Emit emit) {
+    const RatesHeader& H = *tb.H;
+    const int K = H.K, r_begin = H.group_end[1], r_end = H.group_end[5];
+    for (int r0 = r_begin; r0 < r_end; r0 += 4) {
+        const double* E = tb.eff + (size_t)(r0 - r_begin) * K;
         double s[4] = {0.0, 0.0, 0.0, 0.0};
         for (int k = 0; k < K; k++) {
             const double ck = c.C[k];
 #pragma unroll
             for (int q = 0; q < 4; q++) s[q] = fma(E[q * K + k], ck, s[q]);
         }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (e0 + q < H.n_eff) c.M[e0 + q] = c.Ctot + s[q];
-    }
-}
-
-template <int KMAX, int MODEL>
-__device__ __forceinline__ void accumulate_group(const RatesTables& tb, const Cell<KMAX>& c, double* wdot) {
-    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
-        const Reaction& x = tb.reactions[r];
-        const double cR = reaction_rate<MODEL>(tb, x, c);
+        const double M0 = c.Ctot + s[0], M1 = c.Ctot + s[1], M2 = c.Ctot + s[2], M3 = c.Ctot + s[3];
+        const int rq = min(r_end - r0, 4);
 #pragma unroll 1
-        for (int q = 0; q < x.n_net; q++)
-            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
-    }
-}
-
-template <int KMAX, int MODEL>
-__device__ __forceinline__ void rates_of_group(const RatesTables& tb, const Cell<KMAX>& c,
-                                               const ReactionRatesArgs<KMAX>& io, size_t i) {
-    for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
-        const Reaction& x = tb.reactions[r];
-        io.out[x.orig][i] = reaction_rate<MODEL>(tb, x, c);
+        for (int q = 0; q < rq; q++) {
+            const int r = r0 + q;
+            const double M = q == 0 ? M0 : q == 1 ? M1 : q == 2 ? M2 : M3;  // integer selects
+            const Reaction& x = tb.reactions[r];
+            double cR;
+            if (r < H.group_end[2]) cR = reaction_rate<2>(tb, x, c, M);
+            else if (r < H.group_end[3]) cR = reaction_rate<3>(tb, x, c, M);
+            else if (r < H.group_end[4]) cR = reaction_rate<4>(tb, x, c, M);
+            else cR = reaction_rate<5>(tb, x, c, M);
+            emit(x, cR);
+        }
     }
 }
 
@@ -105,13 +113,15 @@ __device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, siz
     cell_setup<KMAX>(tb, pressure_R, T, V, io.in + 4, i, c);
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
-    // species_rates (reaction.rs:312-327), one loop per reaction model
-    accumulate_group<KMAX, 0>(tb, c, wdot);
-    accumulate_group<KMAX, 1>(tb, c, wdot);
-    accumulate_group<KMAX, 2>(tb, c, wdot);
-    accumulate_group<KMAX, 3>(tb, c, wdot);
-    accumulate_group<KMAX, 4>(tb, c, wdot);
-    accumulate_group<KMAX, 5>(tb, c, wdot);
+    // species_rates (reaction.rs:312-327), reactions grouped by model
+    auto accumulate = [&](const Reaction& x, double cR) {
+#pragma unroll 1
+        for (int q = 0; q < x.n_net; q++)
+            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
+    };
+    plain_group<KMAX, 0>(tb, c, accumulate);
+    plain_group<KMAX, 1>(tb, c, accumulate);
+    third_body_groups<KMAX>(tb, c, accumulate);
     // Energy and volume (reaction.rs:375-384).
     double E = 0.0;
     for (int k = 0; k < A; k++) {
@@ -139,12 +149,10 @@ template <int KMAX>
 __device__ void reaction_rates_cell(const RatesTables& tb, const ReactionRatesArgs<KMAX>& io, size_t i) {
     Cell<KMAX> c;
     cell_setup<KMAX>(tb, io.in[0][i], io.in[1][i], io.in[2][i], io.in + 3, i, c);
-    rates_of_group<KMAX, 0>(tb, c, io, i);
-    rates_of_group<KMAX, 1>(tb, c, io, i);
-    rates_of_group<KMAX, 2>(tb, c, io, i);
-    rates_of_group<KMAX, 3>(tb, c, io, i);
-    rates_of_group<KMAX, 4>(tb, c, io, i);
-    rates_of_group<KMAX, 5>(tb, c, io, i);
+    auto store = [&](const Reaction& x, double cR) { io.out[x.orig][i] = cR; };
+    plain_group<KMAX, 0>(tb, c, store);
+    plain_group<KMAX, 1>(tb, c, store);
+    third_body_groups<KMAX>(tb, c, store);
 }
 
 template <int KMAX, bool SMEM>
@@ -585,6 +593,12 @@ cudaError_t launch_math_check(const uint8_t* math, int which, const double* x, d
     if (grid > 4096) grid = 4096;
     math_check_kernel<<<(unsigned)grid, 256, kMathBytes, st>>>(math, which, x, y, n);
     return cudaGetLastError();
+}
+
+// Test hook: polls of the first staging wait of this file's kernels (negative: the default limit).
+cudaError_t set_stage_wait_polls(long long polls) {
+    const long long v = polls < 0 ? kWaitLimit : polls;
+    return cudaMemcpyToSymbol(g_stage_wait_polls, &v, sizeof v);
 }
 
 int max_table_smem() {

@@ -61,6 +61,7 @@ inline int kmax_for(int K, int n_eff) {
 }
 
 int max_table_smem();
+cudaError_t set_stage_wait_polls(long long polls);
 
 // Non-finite values (NaN, infinity) in up to kCountArrays arrays of n doubles, added to *count.
 constexpr int kCountArrays = 512;

@@ -33,7 +33,7 @@ template <int KMAX, int MODEL>
 __device__ __forceinline__ void accumulate_group_m(const RatesMixedTables& tb, const CellM<KMAX>& c, double* wdot) {
     for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
         const ReactionF& x = tb.reactions[r];
-        const double cR = reaction_rate_m<MODEL>(tb, x, c);
+        const double cR = reaction_rate_m<MODEL>(tb, x, c, MODEL >= 2 ? c.Mf[x.eff_row] : 0.f);
 #pragma unroll 1
         for (int q = 0; q < x.n_net; q++)
             wdot[x.net_k[q]] = fma(int_to_double_small(x.net_n[q]), cR, wdot[x.net_k[q]]);
@@ -76,7 +76,7 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
         const double x = fma(g[6], rcpT, fma(g[5], T4, fma(g[4], T3, fma(g[3], T2, fma(g[2], T, fma(g[1], lnT, g[0]))))));
         gibbs_exps(x, s.need_exp, s.need_exp_neg, H.M3, H.cbrt_max, c.C0, c.rcpC0, c.ex[k], c.exn[k]);
     }
-    // FP32 third-body sums, four rows per pass.
+    // FP32 third-body sums, four rows per pass (rows in reaction-group order, padded to a multiple of 4).
     for (int e0 = 0; e0 < H.n_eff; e0 += 4) {
         const float* E = tb.eff + (size_t)e0 * K;
         float s[4] = {0.f, 0.f, 0.f, 0.f};

@@ -479,6 +479,20 @@ int build_mechanism(const cb_mech_desc* d, HostMechanism& m, std::string& err) {
     std::vector<int> order(R);
     for (int r = 0; r < R; r++) order[r] = r;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reactions[a].model < reactions[b].model; });
+    // Efficiency rows renumbered in group order: the reactions with a third body (models 2-5) are
+    // consecutive in the grouped tables, so grouped reaction group_end[1] + e uses row e, and the kernels
+    // compute the sums of four consecutive rows in one pass over the concentrations as they reach them.
+    {
+        std::vector<double> rows(eff_rows.size(), 0.0);
+        int e = 0;
+        for (int i = 0; i < R; i++) {
+            Reaction& x = reactions[order[i]];
+            if (x.eff_row < 0) continue;
+            std::copy_n(&eff_rows[(size_t)x.eff_row * K], K, &rows[(size_t)e * K]);
+            x.eff_row = e++;
+        }
+        eff_rows.swap(rows);
+    }
     std::vector<Reaction> grouped(R);
     for (int i = 0; i < R; i++) {
         grouped[i] = reactions[order[i]];

@@ -1,8 +1,9 @@
 // Rates program pieces shared by the one-cell-per-thread kernels (kernels.cu) and the warp-per-reactor
 // integrator (bdf.cu): temperature powers, Arrhenius rate constants, table views, concentration
 // products and the evaluation of one reaction (reaction.rs:113-309). A "cell" type provides C[]
-// (concentrations, bulk last), ex[] / exn[] (clamped Gibbs exponentials), M[] (third-body sums), t (Temps)
-// and the scalars C0, rcpC0, rcpC0sq; arrays in thread-local memory and pointers into shared memory both fit.
+// (concentrations, bulk last), ex[] / exn[] (clamped Gibbs exponentials), t (Temps) and the scalars C0,
+// rcpC0, rcpC0sq; arrays in thread-local memory and pointers into shared memory both fit. The third-body
+// concentration of a reaction that has one comes as an argument (the caller keeps it where it suits).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -88,17 +89,17 @@ struct ReactionParts {
 };
 
 // cR of one reaction (reaction.rs:149-309): forward rate constant (with third-body efficiency and
-// falloff), rate of progress against the equilibrium constant, and their product.
+// falloff), rate of progress against the equilibrium constant, and their product. M: the reaction's
+// third-body concentration C + sum (e_k - 1) C_k (reaction.rs:141-145), unused by models 0 and 1.
 // MODEL is a compile-time constant: reactions are grouped by model, so no model branch (and no
 // predicated FP64 instruction of another model) is executed per reaction.
 template <int MODEL, bool PARTS, class CellT>
-__device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Reaction& x, const CellT& c,
+__device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Reaction& x, const CellT& c, double M,
                                                 ReactionParts* parts) {
     const RatesHeader& H = *tb.H;
     const Temps& t = c.t;
     double kf;  // forward rate coefficient: k, k M, or the falloff-blended value
     if constexpr (MODEL == 4) {  // Troe (reaction.rs:160-193)
-        const double M = c.M[x.eff_row];
         const Falloff& f = tb.falloff[x.falloff];
         const double k0 = arrhenius(f.k0, t);
         double Pr, kinf, dPr_dM;
@@ -136,7 +137,7 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
     } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
         const Falloff& f = tb.falloff[x.falloff];
         const double k0 = arrhenius(f.k0, t);
-        const double Ck0 = c.M[x.eff_row] * k0;
+        const double Ck0 = M * k0;
         const double ki = arrhenius(x.k, t);
         kf = div64(Ck0 * ki, (Ck0 + ki) + kF32MinPos);
         if constexpr (PARTS) {
@@ -147,7 +148,7 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
         const Falloff& f = tb.falloff[x.falloff];
         const double k0 = arrhenius(f.k0, t);
         const double ki = arrhenius(x.k, t);
-        const double Pr = div64(c.M[x.eff_row] * k0, ki + kF32MinPos);
+        const double Pr = div64(M * k0, ki + kF32MinPos);
         const double lP = log64(Pr + kF32MinPos);
         double base = exp64(f.smrC * t.T);
         if (f.sri_flags & kSriA) base = fma(f.sA, exp64(f.smB * t.rcpT), base);
@@ -161,7 +162,7 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
         }
     } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
         const double k = arrhenius(x.k, t);
-        kf = k * c.M[x.eff_row];
+        kf = k * M;
         if constexpr (PARTS) parts->dkf_dM = k;
     } else {  // elementary, irreversible
         kf = arrhenius(x.k, t);
@@ -206,8 +207,8 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
 }
 
 template <int MODEL, class CellT>
-__device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const CellT& c) {
-    return reaction_eval<MODEL, false>(tb, x, c, nullptr);
+__device__ __forceinline__ double reaction_rate(const RatesTables& tb, const Reaction& x, const CellT& c, double M) {
+    return reaction_eval<MODEL, false>(tb, x, c, M, nullptr);
 }
 
 }  // namespace cbg

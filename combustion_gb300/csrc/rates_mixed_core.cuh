@@ -70,17 +70,18 @@ __device__ __forceinline__ void gibbs_exps(double x, bool need_exp, bool need_ex
     if (need_exp_neg) exn = min_pos(cbrt_max, rcp64(e)) * C0;
 }
 
-// CellT: any cell view with C, ex, exn (FP64, indexable, from gibbs_exps), Mf (FP32 third-body sums), C0, rcpC0,
-// rcpC0sq and the FP32 temperatures Ctotf, Tf, lnTf, rcpTf (one thread's cell here, one warp's cell in
-// the batched reactors).
+// CellT: any cell view with C, ex, exn (FP64, indexable, from gibbs_exps), C0, rcpC0, rcpC0sq and the FP32
+// temperatures Ctotf, Tf, lnTf, rcpTf (one thread's cell here, one warp's cell in the batched reactors).
+// Mf: the reaction's FP32 third-body concentration (unused by models 0 and 1).
 template <int MODEL, class CellT>
-__device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, const ReactionF& x, const CellT& c) {
+__device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, const ReactionF& x, const CellT& c,
+                                                  float Mf) {
     const RatesMixedHeader& H = *tb.H;
     double kf;  // forward rate coefficient including third body and falloff
     if constexpr (MODEL == 4) {  // Troe, blending in FP32 (reaction.rs:160-193)
         const FalloffF& f = tb.falloff[x.falloff];
         const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
-        const double Md = flt_to_dbl(c.Mf[x.eff_row]);
+        const double Md = flt_to_dbl(Mf);
         double Pr, kinf;
         if (f.flags & kKinfConst) {
             Pr = Md * k0;
@@ -109,14 +110,14 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
         kf = (flt_to_dbl(Fb) * kinf) * (Pr * rcp64(Pr + 1.0));
     } else if constexpr (MODEL == 3) {  // Lindemann (reaction.rs:153-159)
         const FalloffF& f = tb.falloff[x.falloff];
-        const double Ck0 = flt_to_dbl(c.Mf[x.eff_row]) * arrhenius_f(f.k0, c.lnTf, c.rcpTf);
+        const double Ck0 = flt_to_dbl(Mf) * arrhenius_f(f.k0, c.lnTf, c.rcpTf);
         const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
         kf = (Ck0 * ki) * rcp64((Ck0 + ki) + kF32MinPos);
     } else if constexpr (MODEL == 5) {  // SRI (reaction.rs:194-203, commented formula), blending in FP32
         const FalloffF& f = tb.falloff[x.falloff];
         const double k0 = arrhenius_f(f.k0, c.lnTf, c.rcpTf);
         const double ki = arrhenius_f(x.k, c.lnTf, c.rcpTf);
-        const double Pr = (flt_to_dbl(c.Mf[x.eff_row]) * k0) * rcp64(ki + kF32MinPos);
+        const double Pr = (flt_to_dbl(Mf) * k0) * rcp64(ki + kF32MinPos);
         const float lP = log_dbl_f32(Pr + kF32MinPos);
         float base = expf(f.smrC * c.Tf);
         if (f.sri_flags & kSriA) base = fmaf(f.sA, expf(f.smB * c.rcpTf), base);
@@ -125,7 +126,7 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
         if (f.sri_flags & kSriE) F *= expf(f.sE * c.lnTf);
         kf = (flt_to_dbl(F) * ki) * (Pr * rcp64(Pr + 1.0));
     } else if constexpr (MODEL == 2) {  // three-body (reaction.rs:152)
-        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf) * flt_to_dbl(c.Mf[x.eff_row]);
+        kf = arrhenius_f(x.k, c.lnTf, c.rcpTf) * flt_to_dbl(Mf);
     } else {
         kf = arrhenius_f(x.k, c.lnTf, c.rcpTf);
     }

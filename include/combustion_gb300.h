@@ -171,6 +171,13 @@ int cb_fp64_math(int which, const double* x, double* y, size_t n, void* stream);
 /* Blocks until the mechanism's work on `stream` is done and reports any kernel-side failure. */
 int cb_synchronize(cb_mech* mech, void* stream);
 
+/* Test hook, no reference counterpart: the number of polls of the first bounded wait with which the
+ * plain FP64 kernels (rates, per-reaction rates, transport) wait for their table staging copy; negative
+ * restores the default. At 0 that wait runs out at once: the kernels set the staging-timeout status and
+ * wait again, with the full limit, for the copy to land, then return without computing, and the next
+ * synchronising call reports CB_ERR_DEVICE (and clears the status). For tests of that error path. */
+int cb_debug_stage_wait_polls(int64_t polls);
+
 /* ---- Seeded synthetic cells on the device ----------------------------------------------------------
  * No reference counterpart (the reference reads states from Cantera or its own reactor). T uniform on
  * [T_min, T_max] K, P log-uniform on [P_min, P_max] atm (fixed when equal), V = 1 m^3, mole fractions

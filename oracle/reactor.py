@@ -59,3 +59,23 @@ def integrate(o, pressure_R, y0, t_end, rtol=1e-9, atol=1e-14):
         raise RuntimeError(sol.message)
     g = rhs(o, pressure_R, sol.y)[0]
     return ignition_time(sol.t, g), sol.y[:, -1], len(sol.t) - 1
+
+
+def _integrate_job(args):
+    mech, pressure_R, y0, t_end, rtol, atol = args
+    import oracle
+    return integrate(oracle.Oracle(mech), pressure_R, y0, t_end, rtol=rtol, atol=atol)
+
+
+def integrate_batch(mech, pressure_R, Y0, t_end, rtol=1e-9, atol=1e-14, workers=0):
+    """integrate() of every reactor (pressure_R [n], initial states Y0 [n][N]) over a pool of spawned
+    processes (spawned, not forked: the caller may hold a CUDA context). Returns a list of
+    (ignition delay, final state, steps)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    workers = workers or min(16, os.cpu_count() or 1, len(Y0))
+    jobs = [(mech, float(pressure_R[i]), np.asarray(Y0[i], dtype=np.float64), t_end, rtol, atol)
+            for i in range(len(Y0))]
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_integrate_job, jobs))

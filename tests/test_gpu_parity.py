@@ -259,3 +259,33 @@ def test_count_nonfinite():
     assert mech.count_nonfinite(many) == 3
     host = dev.cpu().numpy()
     assert mech.count_nonfinite(host) == 3
+
+
+def test_staging_timeout_is_reported_and_cleared():
+    """The bounded wait on the table staging copy, made to run out (cb_debug_stage_wait_polls(0)):
+    the kernels return without computing, the call reports CB_ERR_DEVICE, and once the wait is back to
+    its default the next call on the same mechanism and context succeeds with the oracle's values. The
+    copy itself always lands (the second wait keeps the full limit), so no block exits with a copy in
+    flight."""
+    import combustion_gb300 as cb
+    from combustion_gb300 import synthetic
+    torch = _torch()
+    m = util.mechanism("k10")
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(m.K, 4096, "k10")
+    ins = _dev(o.rates_inputs(cells))
+    out = torch.full((mech.A + 2, cells.n), 7.0, dtype=torch.float64, device="cuda")
+    try:
+        cb.debug_stage_wait_polls(0)
+        mech.rates(ins, out)
+        with pytest.raises(cb.CombustionError) as e:
+            mech.synchronize()
+        assert e.value.code == cb.CB_ERR_DEVICE and "staging" in str(e.value)
+        assert (out.cpu().numpy() == 7.0).all()  # nothing was computed
+    finally:
+        cb.debug_stage_wait_polls(-1)
+    mech.rates(ins, out)
+    mech.synchronize()
+    ref, scale = o.rates(o.rates_inputs(cells), scale=True)
+    assert util.cond_err(out.cpu().numpy(), ref, scale).max() <= util.PLAIN_TOL
