@@ -40,7 +40,8 @@ EXPORTS = ["cb_mech_create", "cb_mech_validate", "cb_mech_destroy", "cb_mech_que
            "cb_surrogate_get_params", "cb_surrogate_set_params", "cb_surrogate_normalisation",
            "cb_surrogate_evaluate", "cb_reactors_create", "cb_reactors_destroy", "cb_reactors_set_state",
            "cb_reactors_autotune", "cb_reactors_integrate", "cb_reactors_results", "cb_reactors_eval",
-           "cb_reactors_eval_noalloc", "cb_yaml_load", "cb_yaml_desc", "cb_yaml_free", "cb_debug_stage_wait_polls"]
+           "cb_reactors_eval_noalloc", "cb_yaml_load", "cb_yaml_desc", "cb_yaml_free", "cb_debug_stage_wait_polls",
+           "cb_surrogate_transport_pair"]
 
 
 class CombustionError(RuntimeError):

@@ -306,6 +306,21 @@ int gather_launch(cb_mech* m, size_t n, const double* const* in, double* const* 
     return e == cudaSuccess ? CB_OK : cuda_fail(e, "transport kernel (gathered cells)");
 }
 
+template <int KM>
+int gather_launch_mixed(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
+                        const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st) {
+    cbg::TransportArgs<KM> a;
+    std::memset(&a, 0, sizeof a);
+    for (int q = 0; q < m->host.K + 3; q++) a.in[q] = in[q];
+    for (int q = 0; q < m->host.K + 2; q++) a.out[q] = out[q];
+    a.flags = (flags & CB_UNIFORM_PRESSURE) | cbg::kFromRates | (compact ? cbg::kCompactOut : 0u);
+    a.index = index;
+    a.count = count;
+    cudaError_t e = cbg::launch_transport_mixed(KM, m->d_transport_mixed, (uint32_t)m->host.transport_mixed_blob.size(),
+                                                &a, n, st, m->d_status);
+    return e == cudaSuccess ? CB_OK : cuda_fail(e, "mixed transport kernel (gathered cells)");
+}
+
 }  // namespace
 
 namespace cbi {
@@ -323,6 +338,17 @@ int transport_gather(cb_mech* m, size_t n, const double* const* in, double* cons
     case 16: return gather_launch<16>(m, n, in, out, index, count, compact, flags, st);
     case 64: return gather_launch<64>(m, n, in, out, index, count, compact, flags, st);
     case 256: return gather_launch<256>(m, n, in, out, index, count, compact, flags, st);
+    default: return ::fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
+    }
+}
+int transport_gather_mixed(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
+                           const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st) {
+    if (!m->host.transport_ready) return ::fail(CB_ERR_NOT_READY, "cb_transport_setup has not run");
+    if (n == 0) return CB_OK;
+    switch (m->kmax) {
+    case 16: return gather_launch_mixed<16>(m, n, in, out, index, count, compact, flags, st);
+    case 64: return gather_launch_mixed<64>(m, n, in, out, index, count, compact, flags, st);
+    case 256: return gather_launch_mixed<256>(m, n, in, out, index, count, compact, flags, st);
     default: return ::fail(CB_ERR_UNSUPPORTED, "species count outside the compiled capacities");
     }
 }

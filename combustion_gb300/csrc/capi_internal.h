@@ -1,5 +1,5 @@
 // Internal interface between the C ABI translation unit (capi.cu) and the transport surrogate
-// (surrogate.cu): error reporting and the plain transport kernel on gathered cells.
+// (surrogate.cu): error reporting and the plain and mixed transport kernels on gathered cells.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,6 +28,11 @@ MechView view(const cb_mech* m);
 // to the same cell or, with `compact`, to position j of the output arrays.
 int transport_gather(cb_mech* m, size_t n, const double* const* in, double* const* out, const uint32_t* index,
                      const uint32_t* count, bool compact, uint32_t flags, cudaStream_t st);
+
+// The same with the mixed-precision transport kernel (FP32 fits and mixing).
+int transport_gather_mixed(cb_mech* m, size_t n, const double* const* in, double* const* out,
+                           const uint32_t* index, const uint32_t* count, bool compact, uint32_t flags,
+                           cudaStream_t st);
 
 int check_status(cb_mech* m);
 

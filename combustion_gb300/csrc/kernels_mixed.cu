@@ -139,8 +139,9 @@ __global__ void __launch_bounds__(kBlock) rates_mixed_kernel(const uint8_t* __re
 }
 
 // ---------------------------------------------------------------------------------------------------
+// i: the cell's index in the inputs, o: in the outputs (they differ for gathered cells).
 template <int KMAX>
-__device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i) {
+__device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i, size_t o) {
     const TransportMixedHeader& H = *reinterpret_cast<const TransportMixedHeader*>(tab + kMathBytes);
     const float* cond = reinterpret_cast<const float*>(tab + H.off_cond);
     const float* visc = reinterpret_cast<const float*>(tab + H.off_visc);
@@ -185,7 +186,7 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
         Ac = fmaf(X[k], c, Ac);
         Bc = fmaf(X[k], rcp_f32(c), Bc);
     }
-    io.out[0][i] = flt_to_dbl((__fdividef(Ac, N) + __fdividef(N, Bc)) * VT);
+    io.out[0][o] = flt_to_dbl((__fdividef(Ac, N) + __fdividef(N, Bc)) * VT);
 
     for (int k = 0; k < K; k++) {
         v[k] = poly(visc + 5 * k);
@@ -213,7 +214,7 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
             if (k < K) mu = fmaf(X[k] * (v[k] * v[k]), rcp_f32(fmaf(v[k], fmaf(v[k], s3[q], s2[q]), s1[q])), mu);
         }
     }
-    io.out[1][i] = flt_to_dbl(VT * mu);
+    io.out[1][o] = flt_to_dbl(VT * mu);
 
     float* S = Y;
     for (int k = 0; k < K; k++) S[k] = 0.f;
@@ -243,7 +244,7 @@ __device__ void transport_mixed_cell(const uint8_t* tab, const TransportArgs<KMA
         }
         S[k] += sa + sb;
     }
-    for (int k = 0; k < K; k++) io.out[2 + k][i] = flt_to_dbl(__fdividef(fmaf(-(VT * W[k]), X[k], MVTN), S[k]));
+    for (int k = 0; k < K; k++) io.out[2 + k][o] = flt_to_dbl(__fdividef(fmaf(-(VT * W[k]), X[k], MVTN), S[k]));
 }
 
 template <int KMAX, bool SMEM>
@@ -259,8 +260,11 @@ __global__ void __launch_bounds__(kTransportMixedBlock) transport_mixed_kernel(c
     } else {  // tables read from global memory; only the math tables go to shared memory
         load_math(gtab);
     }
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        transport_mixed_cell<KMAX>(tab, io, i);
+    if (io.count) n = min(n, (size_t)*io.count);  // gathered cells: the count is known on the device only
+    for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = io.index ? (size_t)(io.index[j] & kIndexMask) : j;
+        transport_mixed_cell<KMAX>(tab, io, i, (io.flags & kCompactOut) ? j : i);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -281,18 +285,30 @@ size_t wave_of_m(KS ksmem, KG kglobal, uint32_t tab_bytes) {
     return (size_t)sm_count_m() * per_sm * BLOCK;
 }
 
+template <class Args>
+bool gathered_m(const Args&) { return false; }
+template <int KMAX>
+bool gathered_m(const TransportArgs<KMAX>& io) { return io.index != nullptr; }
+
 template <int BLOCK, class Args, class KS, class KG>
 cudaError_t launch_mixed(KS ksmem, KG kglobal, const uint8_t* tab, uint32_t tab_bytes, const Args& io, size_t n,
                          cudaStream_t st, int* status) {
     const bool smem = (int)tab_bytes <= max_table_smem();
-    int per_sm = 1;
-    const size_t want = (n + BLOCK - 1) / BLOCK;
+    // A gathered launch of fewer cells than one wave of full blocks (a trust gate's fallback) spreads
+    // them over every SM in one-warp blocks.
+    int block = BLOCK, per_sm = 1;
     cudaError_t e = table_kernel_occupancy(ksmem, kglobal, BLOCK, tab_bytes, kMathBytes, smem, &per_sm);
     if (e != cudaSuccess) return e;
+    if (gathered_m(io) && n < (size_t)sm_count_m() * per_sm * BLOCK) {
+        block = 32;
+        e = table_kernel_occupancy(ksmem, kglobal, block, tab_bytes, kMathBytes, smem, &per_sm);
+        if (e != cudaSuccess) return e;
+    }
+    const size_t want = (n + block - 1) / block;
     size_t grid = (size_t)sm_count_m() * per_sm;
     if (want < grid) grid = want ? want : 1;
-    if (smem) ksmem<<<(unsigned)grid, BLOCK, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
-    else kglobal<<<(unsigned)grid, BLOCK, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
+    if (smem) ksmem<<<(unsigned)grid, block, tab_bytes, st>>>(tab, tab_bytes, io, n, status);
+    else kglobal<<<(unsigned)grid, block, kMathBytes, st>>>(tab, tab_bytes, io, n, status);
     return cudaGetLastError();
 }
 }  // namespace

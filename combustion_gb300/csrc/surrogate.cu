@@ -136,6 +136,9 @@ struct cb_surrogate {
     uint32_t *fail_idx = nullptr, *audit_idx = nullptr, *gate_count = nullptr;
     double* audit_plain = nullptr;
     size_t fail_cap = 0, audit_cap = 0;  // grown to the largest call
+    uint8_t* outside = nullptr;          // ensemble calls: trust-region flags of the call's cells
+    float* disagreement = nullptr;       // ensemble calls: the networks' disagreement per cell
+    size_t cell_cap = 0;
     unsigned* err_max = nullptr;
     double* err_sq = nullptr;
     int* status = nullptr;
@@ -276,7 +279,7 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
     if (update) {
         SUR_CUDA(adam(adam_args(s, total_steps), st));
         const int n_batches = (int)(s->n_train / s->batch);
-        SUR_CUDA(finish_step(s->loss_part, 4 * rows / kBM, 1.0f / ((float)rows * (float)s->n_feat), s->losses, s->counters,
+        SUR_CUDA(finish_step(s->loss_part, kEpiWarps * rows / kBM, 1.0f / ((float)rows * (float)s->n_feat), s->losses, s->counters,
                              s->counters + 1, s->batch, n_batches, st));
     }
     return CB_OK;
@@ -286,7 +289,7 @@ int free_all(cb_surrogate* s) {
     void* ptrs[] = {s->p, s->g, s->m1, s->m2, s->norm, s->X, s->XT, s->Y, s->dY, s->dYT, s->dZ[0], s->dZ[1],
                     s->dZT[0], s->dZT[1], s->ws, s->loss_part, s->losses, s->counters, s->Xs, s->XTs, s->Ys, s->Xi, s->Hi[0],
                     s->Hi[1], s->Yi, s->fail_idx, s->audit_idx, s->gate_count, s->audit_plain, s->err_max,
-                    s->err_sq, s->status};
+                    s->err_sq, s->status, s->outside, s->disagreement};
     for (void* q : ptrs) cudaFree(q);
     for (int l = 0; l < kMaxLayers; l++) {
         cudaFree(s->W[l]);
@@ -486,7 +489,7 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     }
     rc = rc ? rc : dalloc(&s->ws, ws);
     rc = rc ? rc : dalloc(&s->losses, kMaxSteps);
-    rc = rc ? rc : dalloc(&s->loss_part, 4 * B / kBM);
+    rc = rc ? rc : dalloc(&s->loss_part, kEpiWarps * B / kBM);
     rc = rc ? rc : dalloc(&s->counters, 2);
     rc = rc ? rc : dalloc(&s->Xs, B * s->n_in);
     rc = rc ? rc : dalloc(&s->XTs, B * s->n_in);
@@ -819,7 +822,7 @@ int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features_h
     SUR_CUDA(cudaMemcpyAsync(s->XTs, xt.data(), xt.size() * sizeof(bf16), cudaMemcpyHostToDevice, st));
     SUR_CUDA(cudaMemcpyAsync(s->Ys, targets_h, (size_t)rows * n_out * sizeof(float), cudaMemcpyHostToDevice, st));
     SUR_RC(run_pass(s, rows, s->mXs, s->mXTs, s->Ys, false, true, false, 1, st));
-    std::vector<float> lp(4 * rows / kBM);
+    std::vector<float> lp(kEpiWarps * rows / kBM);
     SUR_CUDA(cudaMemcpyAsync(lp.data(), s->loss_part, lp.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (grads) SUR_CUDA(cudaMemcpyAsync(grads, s->g, s->n_params * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (outputs_h) {
@@ -1007,6 +1010,220 @@ int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* input
         stats->ms_gate = ms[3];
     }
     return check_device_status(s);
+}
+
+int cb_surrogate_transport_pair(cb_surrogate* a, cb_surrogate* b, size_t n, const double* const* inputs,
+                                double* const* outputs, uint32_t flags, const cb_surrogate_gate* gate,
+                                cb_surrogate_stats* stats, void* stream) {
+    if (!a || !b || !inputs || !outputs || !gate) return cbi::fail(CB_ERR_INVALID, "null argument");
+    if (a == b) return cbi::fail(CB_ERR_INVALID, "the two networks must be different objects");
+    if (flags & ~(CB_UNIFORM_PRESSURE | CB_SURROGATE_TIMING)) return cbi::fail(CB_ERR_INVALID, "unknown flag");
+    if (a->mech != b->mech || a->n_feat != b->n_feat || a->n_in != b->n_in || a->n_out != b->n_out ||
+        a->device != b->device)
+        return cbi::fail(CB_ERR_INVALID, "the two networks must belong to the same mechanism and device");
+    if (gate->fallback != CB_FALLBACK_MIXED && gate->fallback != CB_FALLBACK_PLAIN)
+        return cbi::fail(CB_ERR_INVALID, "unknown fallback kernel");
+    if (!a->have_norm || !b->have_norm) return cbi::fail(CB_ERR_NOT_READY, "cb_surrogate_generate has not run");
+    if (n >= ((size_t)1 << 31)) return cbi::fail(CB_ERR_INVALID, "at most 2^31 - 1 cells per call");
+    if (std::isnan(gate->threshold)) return cbi::fail(CB_ERR_INVALID, "NaN threshold");
+    const int K = a->K, nf = a->n_feat;
+    for (int q = 0; q < K + 3; q++)
+        if (!inputs[q]) return cbi::fail(CB_ERR_INVALID, "null input array");
+    for (int q = 0; q < K + 2; q++)
+        if (!outputs[q]) return cbi::fail(CB_ERR_INVALID, "null output array");
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    if (n == 0) return CB_OK;
+    SUR_CUDA(cudaSetDevice(a->device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool uniform = flags & CB_UNIFORM_PRESSURE;
+    if (gate->threshold < 0.0) {  // every cell falls back: the fallback kernel alone, no network, no audit
+        const uint32_t pflags = uniform ? CB_UNIFORM_PRESSURE : 0;
+        if (gate->fallback == CB_FALLBACK_MIXED)
+            SUR_RC(cbi::transport_gather_mixed(a->mech, n, inputs, outputs, nullptr, nullptr, false, pflags, st));
+        else
+            SUR_RC(cbi::transport_gather(a->mech, n, inputs, outputs, nullptr, nullptr, false, pflags, st));
+        SUR_CUDA(cudaStreamSynchronize(st));
+        if (stats) {
+            stats->cells = n;
+            stats->fallback_cells = n;
+        }
+        return cbi::check_status(a->mech);
+    }
+    SUR_RC(ensure_inference(a, kInferChunk));
+    SUR_RC(ensure_inference(b, kInferChunk));
+    const double T0 = cbi::view(a->mech).T0;
+    const uint32_t audit_stride = gate->audit_stride;
+    const size_t audit_cap = audit_stride ? n / audit_stride + 1 : 0;
+    // every cell may fall back; the lists and per-cell arrays live in the first network's object
+    if (n > a->fail_cap) {
+        cudaFree(a->fail_idx);
+        a->fail_idx = nullptr;
+        a->fail_cap = 0;
+        SUR_RC(dalloc(&a->fail_idx, n));
+        a->fail_cap = n;
+    }
+    if (n > a->cell_cap) {
+        cudaFree(a->outside);
+        cudaFree(a->disagreement);
+        a->outside = nullptr;
+        a->disagreement = nullptr;
+        a->cell_cap = 0;
+        SUR_RC(dalloc(&a->outside, n));
+        SUR_RC(dalloc(&a->disagreement, n));
+        a->cell_cap = n;
+    }
+    if (audit_cap > a->audit_cap) {
+        cudaFree(a->audit_idx);
+        cudaFree(a->audit_plain);
+        a->audit_idx = nullptr;
+        a->audit_plain = nullptr;
+        a->audit_cap = 0;
+        SUR_RC(dalloc(&a->audit_idx, audit_cap));
+        SUR_RC(dalloc(&a->audit_plain, audit_cap * (size_t)(K + 2)));
+        a->audit_cap = audit_cap;
+    }
+    const bool timing = flags & CB_SURROGATE_TIMING;
+    cudaEvent_t ev[5] = {};
+    double ms[4] = {0, 0, 0, 0};
+    struct EventGuard {
+        cudaEvent_t* ev;
+        ~EventGuard() {
+            for (int i = 0; i < 5; i++)
+                if (ev[i]) cudaEventDestroy(ev[i]);
+        }
+    } guard{ev};
+    if (timing)
+        for (auto& e : ev) SUR_CUDA(cudaEventCreate(&e));
+    auto mark = [&](int i) { return timing ? cudaEventRecord(ev[i], st) : cudaSuccess; };
+    auto elapsed = [&](int i, int j) -> cudaError_t {
+        if (!timing) return cudaSuccess;
+        cudaError_t e = cudaEventSynchronize(ev[j]);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[i], ev[j]);
+        ms[i] += t;
+        return e;
+    };
+    SUR_CUDA(cudaMemsetAsync(a->err_max, 0, 3 * sizeof(unsigned), st));
+    SUR_CUDA(cudaMemsetAsync(a->err_sq, 0, 3 * sizeof(double), st));
+    SUR_CUDA(cudaMemsetAsync(a->gate_count, 0, 2 * sizeof(uint32_t), st));
+    for (size_t lo = 0; lo < n; lo += kInferChunk) {
+        const size_t len = std::min(kInferChunk, n - lo);
+        const int rows = (int)((len + kBM - 1) / kBM * kBM);
+        SUR_CUDA(mark(0));
+        for (cb_surrogate* s : {a, b}) {  // each network's own normalisation of the same cells
+            FeatureArgs f;
+            std::memset(&f, 0, sizeof f);
+            for (int q = 0; q < K + 3; q++) f.in[q] = (uniform && q < 2) ? inputs[q] : inputs[q] + lo;
+            f.n = len;
+            f.rows = rows;
+            f.K = K;
+            f.n_feat = nf;
+            f.n_in = s->n_in;
+            f.uniform_pressure = uniform;
+            f.T0 = T0;
+            f.R_over_P0 = kR / 101325.0;
+            f.mean = nrm(s, kInMean);
+            f.rstd = nrm(s, kInRstd);
+            f.X = s->Xi;
+            if (s == a) {  // the first network's training range is the trust region
+                f.lo = nrm(a, kLo);
+                f.hi = nrm(a, kHi);
+                f.outside = a->outside;
+                f.idx_base = (uint32_t)lo;
+            }
+            SUR_CUDA(features(f, st));
+        }
+        SUR_CUDA(mark(1));
+        SUR_RC(infer_rows(a, rows, a->mXi, st));
+        SUR_RC(infer_rows(b, rows, b->mXi, st));
+        SUR_CUDA(mark(2));
+        CombineArgs c;
+        std::memset(&c, 0, sizeof c);
+        c.Ya = a->Yi;
+        c.Yb = b->Yi;
+        c.ldY = a->n_out;
+        c.n = len;
+        c.n_feat = nf;
+        c.mean_a = nrm(a, kOutMean);
+        c.std_a = nrm(a, kOutStd);
+        c.mean_b = nrm(b, kOutMean);
+        c.std_b = nrm(b, kOutStd);
+        for (int q = 0; q < K + 2; q++) c.out[q] = outputs[q] + lo;
+        c.threshold = (float)gate->threshold;
+        c.outside = a->outside;
+        c.disagreement = a->disagreement;
+        c.fail_idx = a->fail_idx;
+        c.fail_count = a->gate_count;
+        c.audit_idx = a->audit_idx;
+        c.audit_count = a->gate_count + 1;
+        c.audit_stride = audit_stride;
+        c.audit_phase = audit_stride ? (uint32_t)(7919u % audit_stride) : 0u;
+        c.audit_cap = (uint32_t)audit_cap;
+        c.idx_base = (uint32_t)lo;
+        SUR_CUDA(combine(c, st));
+        SUR_CUDA(mark(3));
+        SUR_CUDA(elapsed(0, 1));
+        SUR_CUDA(elapsed(1, 2));
+        SUR_CUDA(elapsed(2, 3));
+    }
+    if (gate->disagreement)
+        SUR_CUDA(cudaMemcpyAsync(gate->disagreement, a->disagreement, n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    uint32_t cnt[2];
+    SUR_CUDA(cudaMemcpyAsync(cnt, a->gate_count, sizeof cnt, cudaMemcpyDeviceToHost, st));
+    SUR_CUDA(cudaStreamSynchronize(st));
+    const uint64_t n_fail = cnt[0], n_audit = std::min<uint64_t>(cnt[1], audit_cap);
+    SUR_CUDA(mark(3));
+    const uint32_t pflags = uniform ? CB_UNIFORM_PRESSURE : 0;
+    if (n_fail) {  // the fallback kernel writes the rejected cells' outputs in place
+        if (gate->fallback == CB_FALLBACK_MIXED)
+            SUR_RC(cbi::transport_gather_mixed(a->mech, n_fail, inputs, outputs, a->fail_idx, a->gate_count, false,
+                                               pflags, st));
+        else
+            SUR_RC(cbi::transport_gather(a->mech, n_fail, inputs, outputs, a->fail_idx, a->gate_count, false, pflags,
+                                         st));
+    }
+    if (n_audit) {  // the audit's judge is the plain FP64 kernel
+        std::vector<double*> aud(K + 2);
+        for (int q = 0; q < K + 2; q++) aud[q] = a->audit_plain + (size_t)q * audit_cap;
+        SUR_RC(cbi::transport_gather(a->mech, n_audit, inputs, aud.data(), a->audit_idx, a->gate_count + 1, true,
+                                     pflags, st));
+        AuditArgs au;
+        std::memset(&au, 0, sizeof au);
+        au.idx = a->audit_idx;
+        au.count = a->gate_count + 1;
+        au.plain = a->audit_plain;
+        au.cap = audit_cap;
+        for (int q = 0; q < K + 2; q++) au.out[q] = outputs[q];
+        au.n_feat = nf;
+        au.max_err = a->err_max;
+        au.sum_sq = a->err_sq;
+        SUR_CUDA(audit(au, n_audit, st));
+    }
+    SUR_CUDA(mark(4));
+    SUR_CUDA(elapsed(3, 4));
+    unsigned em[3];
+    double es[3];
+    SUR_CUDA(cudaMemcpyAsync(em, a->err_max, sizeof em, cudaMemcpyDeviceToHost, st));
+    SUR_CUDA(cudaMemcpyAsync(es, a->err_sq, sizeof es, cudaMemcpyDeviceToHost, st));
+    SUR_CUDA(cudaStreamSynchronize(st));
+    if (stats) {
+        stats->cells = n;
+        stats->fallback_cells = n_fail;
+        stats->audited_cells = n_audit;
+        const double counts[3] = {(double)n_audit, (double)n_audit, (double)n_audit * K};
+        for (int gI = 0; gI < 3; gI++) {
+            float v;
+            std::memcpy(&v, &em[gI], sizeof v);
+            stats->audit_max_rel_err[gI] = v;
+            stats->audit_rms_rel_err[gI] = n_audit ? std::sqrt(es[gI] / counts[gI]) : 0.0;
+        }
+        stats->ms_features = ms[0];
+        stats->ms_network = ms[1];
+        stats->ms_outputs = ms[2];
+        stats->ms_gate = ms[3];
+    }
+    SUR_RC(check_device_status(b));
+    return check_device_status(a);
 }
 
 }  // extern "C"

@@ -2,9 +2,10 @@
 //
 // The GEMM is D[M][N] = A[M][K] B[N][K]^T over BF16 operands with an FP32 accumulator in tensor memory:
 // one 128 x BN output tile per block, operands streamed through a ring of shared-memory stages by TMA
-// (128-byte swizzle, K-major), tcgen05.mma issued by one thread, the accumulator read back by four
-// epilogue warps (one TMEM lane, i.e. one output row, per thread) which apply the layer's element-wise
-// work before anything is written to global memory. Every mbarrier wait is bounded: a wait that runs
+// (128-byte swizzle, K-major), tcgen05.mma issued by one thread, the accumulator read back by eight
+// epilogue warps (one TMEM lane, i.e. one output row, per thread; two warps per lane quarter, each on
+// half of the columns) which apply the layer's element-wise work before anything is written to global
+// memory. Every mbarrier wait is bounded: a wait that runs
 // out sets a status bit, lets in-flight copies land and the block still frees its tensor memory.
 #include <cuda_bf16.h>
 
@@ -43,21 +44,35 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* base, int ld, int 
                             pack_bf16(a[8 * j + 4], a[8 * j + 5]), pack_bf16(a[8 * j + 6], a[8 * j + 7]));
 }
 
-// The same values into the transposed matrix: consecutive threads hold consecutive rows, so each of
-// the 32 stores of a warp covers 64 contiguous bytes.
-__device__ __forceinline__ void store_col_bf16(__nv_bfloat16* base, int ld, int row, int n, const float* a) {
+// The same values into the transposed matrix (rows row0 .. row0 + 31 of the warp, one per lane),
+// staged through the warp's 2 KB of shared memory: the 32 x 32 chunk is written column by column (lane
+// = row, 64 contiguous bytes per column), then each lane stores 16 bytes (8 rows of one column), eight
+// columns per instruction; each column is a 64-byte run of the transposed matrix's row. Four global
+// stores per chunk instead of 32 two-byte ones.
+__device__ __forceinline__ void store_col_bf16(__nv_bfloat16* base, int ld, int row0, int n, int lane,
+                                               const float* a, __nv_bfloat16* stage) {
 #pragma unroll
-    for (int j = 0; j < 32; j++) base[(size_t)(n + j) * ld + row] = __float2bfloat16_rn(a[j]);
+    for (int j = 0; j < 32; j++) stage[j * 32 + lane] = __float2bfloat16_rn(a[j]);
+    __syncwarp();
+    const uint4* s4 = reinterpret_cast<const uint4*>(stage);
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+        const int j = it * 8 + (lane >> 2), piece = lane & 3;
+        *reinterpret_cast<uint4*>(base + (size_t)(n + j) * ld + row0 + piece * 8) = s4[j * 4 + piece];
+    }
+    __syncwarp();  // the next chunk rewrites the stage
 }
 
 template <int BN, int EPI>
-__device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int warp, int lane, int m0, int n0) {
-    const int q = warp & 3;  // the TMEM lane quarter this warp may read
+__device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int warp, int lane, int m0, int n0,
+                                         __nv_bfloat16* stage) {
+    const int q = warp & 3;          // the TMEM lane quarter this warp may read
+    const int h = (warp - 2) >> 2;   // and its half of the tile's columns
     const int row = m0 + q * 32 + lane;
     const int trow0 = (p.dyn & kDynTarget) ? *p.row0 : 0;
     float lsum = 0.f;
 #pragma unroll 1
-    for (int c = 0; c < BN; c += 32) {
+    for (int c = h * (BN / 2); c < (h + 1) * (BN / 2); c += 32) {
         float v[32];
         umma::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
         const int n = n0 + c;
@@ -81,7 +96,7 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
             }
             if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
             store_row_bf16(p.out2, p.ld_out2, row, n, a);
-            if (p.outT) store_col_bf16(p.outT, p.ld_outT, row, n, a);
+            if (p.outT) store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
         } else if constexpr (EPI == kEpiLoss) {
             const float* t = p.target + (size_t)(trow0 + row) * p.ld_target;
             float a[32];
@@ -93,7 +108,7 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
                 a[j] = d * p.grad_scale;
             }
             store_row_bf16(p.out, p.ld_out, row, n, a);
-            store_col_bf16(p.outT, p.ld_outT, row, n, a);
+            store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
         } else if constexpr (EPI == kEpiDgrad) {
             const uint4* zp = reinterpret_cast<const uint4*>(p.zin + (size_t)row * p.ld_zin + n);
             float a[32];
@@ -112,13 +127,13 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
                 }
             }
             store_row_bf16(p.out, p.ld_out, row, n, a);
-            store_col_bf16(p.outT, p.ld_outT, row, n, a);
+            store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
         }
     }
     if constexpr (EPI == kEpiLoss) {  // one partial per warp: no barrier among the epilogue warps
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-        if (lane == 0) p.loss[blockIdx.x * 4 + q] = lsum;
+        if (lane == 0) p.loss[blockIdx.x * kEpiWarps + h * 4 + q] = lsum;
     }
 }
 
@@ -199,7 +214,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     } else {  // epilogue warps (the wait's outcome made warp-uniform: tcgen05.ld needs the whole warp)
         ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full), 0));
         umma::fence_after_sync();
-        if (ok) epilogue<BN, EPI>(p, tmem, warp, lane, m0, n0);
+        // Every MMA has completed (so every operand stage was consumed): the ring is free, and each
+        // epilogue warp stages its transposed chunks in 2 KB of it.
+        __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(dsm + (base - smem_u32(dsm)) + (warp - 2) * 2048);
+        if (ok) epilogue<BN, EPI>(p, tmem, warp, lane, m0, n0, stage);
     }
     if (!ok) atomicOr(p.status, kStatusGemmTimeout);
     umma::fence_before_sync();
@@ -523,6 +541,7 @@ __global__ void features_kernel(const FeatureArgs a) {
 #pragma unroll
                 for (int h = 0; h < 8; h++) a.XT[(size_t)(j0 + h) * a.ldXT + a.row0 + c] = __float2bfloat16_rn(x[h]);
         }
+        if (a.outside) a.outside[a.idx_base + c] = inside ? 0 : 1;
         if (a.fail_idx) {
             const uint32_t cell = a.idx_base + (uint32_t)c;
             if (!inside) {
@@ -601,6 +620,50 @@ cudaError_t outputs(const OutputArgs& a, cudaStream_t st) {
     size_t grid = (a.n + 127) / 128;
     if (grid > 152 * 8) grid = 152 * 8;
     outputs_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+// The ensemble: outputs exp((l_a + l_b) / 2) of the two networks' log outputs, the disagreement
+// max_j |l_a,j - l_b,j| as the cell's error estimate, and the gate lists.
+__global__ void combine_kernel(const CombineArgs a) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.n; c += (size_t)gridDim.x * blockDim.x) {
+        const float* ya = a.Ya + c * a.ldY;
+        const float* yb = a.Yb + c * a.ldY;
+        float d = 0.f;
+        for (int j0 = 0; j0 < a.n_feat; j0 += 4) {
+            const float4 va = *reinterpret_cast<const float4*>(ya + j0);
+            const float4 vb = *reinterpret_cast<const float4*>(yb + j0);
+            const float as[4] = {va.x, va.y, va.z, va.w}, bs[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int j = j0 + h;
+                if (j < a.n_feat) {
+                    const float la = fmaf(a.std_a[j], as[h], a.mean_a[j]);
+                    const float lb = fmaf(a.std_b[j], bs[h], a.mean_b[j]);
+                    d = fmaxf(d, fabsf(la - lb));
+                    a.out[j][c] = (double)__expf(0.5f * (la + lb));
+                }
+            }
+        }
+        const uint32_t cell = a.idx_base + (uint32_t)c;
+        if (a.disagreement) a.disagreement[cell] = d;
+        if (a.fail_idx) {
+            const bool out = (a.outside && a.outside[cell]) || !(d <= a.threshold);
+            if (out) {
+                a.fail_idx[atomicAdd(a.fail_count, 1u)] = cell;
+            } else if (a.audit_stride && cell % a.audit_stride == a.audit_phase) {
+                const uint32_t slot = atomicAdd(a.audit_count, 1u);
+                if (slot < a.audit_cap) a.audit_idx[slot] = cell;
+            }
+        }
+    }
+}
+
+cudaError_t combine(const CombineArgs& a, cudaStream_t st) {
+    if (a.n == 0) return cudaSuccess;
+    size_t grid = (a.n + 127) / 128;
+    if (grid > 152 * 8) grid = 152 * 8;
+    combine_kernel<<<(unsigned)grid, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 

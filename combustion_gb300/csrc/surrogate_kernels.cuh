@@ -10,7 +10,10 @@
 namespace cbg {
 namespace sur {
 
-constexpr int kGemmThreads = 192;  // warp 0: TMA producer, warp 1: TMEM owner + MMA issuer, warps 2-5: epilogue
+// warp 0: TMA producer, warp 1: TMEM owner + MMA issuer, warps 2-9: epilogue (two per TMEM lane quarter,
+// each taking half of the tile's columns)
+constexpr int kGemmThreads = 320;
+constexpr int kEpiWarps = 8;       // loss partials per 128-row tile: one per epilogue warp
 constexpr int kBM = 128;           // rows per tile (one M = 128 MMA, one TMEM lane per row)
 constexpr int kBK = 64;            // K per pipeline stage: one 128-byte swizzle row of BF16
 constexpr int kGemmSmem = 193 * 1024;  // operand ring (stages x (A + B tile)) + alignment; one block per SM
@@ -40,7 +43,7 @@ struct GemmParams {
     __nv_bfloat16* outT; int ld_outT;  // transposed BF16 [N][ld]
     const __nv_bfloat16* zin; int ld_zin;  // pre-activations for the SiLU backward
     const float* target; int ld_target; int n_valid; float grad_scale;
-    float* loss;            // one partial per epilogue warp: [row tile][4]
+    float* loss;            // one partial per epilogue warp: [row tile][kEpiWarps]
     float* outf; int ld_outf;  // FP32 output
     int* status;
 };
@@ -68,6 +71,25 @@ struct FeatureArgs {
     int* hull_lo; int* hull_hi;             // order-preserving integer min / max of raw features (optional)
     const float* lo; const float* hi;       // trust region (inference gate, optional)
     uint32_t* fail_idx; uint32_t* fail_count;  // cells idx_base + c outside the trust region
+    uint32_t* audit_idx; uint32_t* audit_count; uint32_t audit_stride, audit_phase, audit_cap;
+    uint32_t idx_base;
+    uint8_t* outside;                       // per cell of the call: 1 outside the trust region (optional)
+};
+
+// Two networks' normalised outputs of the same cells -> transport properties (their mean in log space)
+// and the ensemble gate: a cell falls back when it lies outside the trust region or when the networks'
+// log outputs differ by more than `threshold` (max over outputs); every audit_stride-th other cell is
+// audited.
+struct CombineArgs {
+    const float* Ya; const float* Yb; int ldY;
+    size_t n;
+    int n_feat;
+    const float* mean_a; const float* std_a; const float* mean_b; const float* std_b;
+    double* out[kMaxOut];
+    float threshold;                  // +inf: the trust region alone; negative: every cell falls back
+    const uint8_t* outside;           // per cell of the call (optional)
+    float* disagreement;              // per cell of the call (optional)
+    uint32_t* fail_idx; uint32_t* fail_count;
     uint32_t* audit_idx; uint32_t* audit_count; uint32_t audit_stride, audit_phase, audit_cap;
     uint32_t idx_base;
 };
@@ -143,6 +165,7 @@ cudaError_t generate_cells(const CellGenArgs& a, cudaStream_t st);
 cudaError_t features(const FeatureArgs& a, cudaStream_t st);
 cudaError_t targets(const TargetArgs& a, cudaStream_t st);
 cudaError_t outputs(const OutputArgs& a, cudaStream_t st);
+cudaError_t combine(const CombineArgs& a, cudaStream_t st);
 cudaError_t audit(const AuditArgs& a, size_t cap, cudaStream_t st);
 
 }  // namespace sur

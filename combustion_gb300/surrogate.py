@@ -47,6 +47,14 @@ class cb_surrogate_stats(C.Structure):
                        "gate": self.ms_gate}}
 
 
+class cb_surrogate_gate(C.Structure):
+    _fields_ = [("threshold", C.c_double), ("audit_stride", C.c_uint32), ("fallback", C.c_uint32),
+                ("disagreement", C.c_void_p)]
+
+
+CB_FALLBACK_MIXED, CB_FALLBACK_PLAIN = 0, 1
+
+
 # Cell distributions of the named workloads (T in K, P in atm, Dirichlet alpha).
 DISTRIBUTIONS = {
     "k10": dict(T_min=800.0, T_max=2800.0, P_min=1.0, P_max=1.0, alpha=0.5),
@@ -74,6 +82,8 @@ def _bind():
     L.cb_surrogate_set_params.argtypes = [vp, vp]
     L.cb_surrogate_normalisation.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.cb_surrogate_evaluate.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp]
+    L.cb_surrogate_transport_pair.argtypes = [vp, vp, sz, vp, vp, C.c_uint32, C.POINTER(cb_surrogate_gate),
+                                              C.POINTER(cb_surrogate_stats), vp]
     _bound = True
     return L
 
@@ -186,4 +196,51 @@ class Surrogate:
         return st.as_dict()
 
 
-__all__ = ["Surrogate", "generate_cells", "distribution", "DISTRIBUTIONS", "CombustionError"]
+def transport_pair(a: Surrogate, b: Surrogate, inputs, outputs, threshold: float, audit_stride=1024,
+                   fallback="mixed", disagreement=None, uniform_pressure=False, stream=None, timing=False):
+    """Ensemble-gated transport (cb_surrogate_transport_pair): rates-layout inputs [K+3, n] -> outputs
+    [K+2, n] (torch CUDA float64); cells whose networks disagree by more than `threshold` (or outside
+    the training range) go to the mixed ("mixed") or plain ("plain") kernel. `disagreement` (torch CUDA
+    float32 [n]) receives each cell's estimate. Returns the stats."""
+    L = _bind()
+    ins, _ = Mechanism._rows(inputs)
+    outs, n = Mechanism._rows(outputs)
+    flags = (CB_UNIFORM_PRESSURE if uniform_pressure else 0) | (CB_SURROGATE_TIMING if timing else 0)
+    d_ptr = None
+    if disagreement is not None:
+        import torch
+        assert disagreement.dtype == torch.float32 and disagreement.is_contiguous() and disagreement.numel() >= n
+        d_ptr = disagreement.data_ptr()
+    g = cb_surrogate_gate(float(threshold), int(audit_stride),
+                          {"mixed": CB_FALLBACK_MIXED, "plain": CB_FALLBACK_PLAIN}[fallback], d_ptr)
+    st = cb_surrogate_stats()
+    _check(L.cb_surrogate_transport_pair(a.h, b.h, n, _ptr_array(ins), _ptr_array(outs), flags, C.byref(g),
+                                         C.byref(st), Mechanism._stream(stream)))
+    return st.as_dict()
+
+
+def max_rel_err_per_cell(x, ref):
+    """max_j |x_j - r_j| / |r_j| per cell (column) of two [K+2, n] torch tensors."""
+    return ((x - ref).abs() / ref.abs()).amax(dim=0)
+
+
+def calibrate_threshold(disagreement, err, tol: float) -> float:
+    """The largest disagreement threshold t such that every calibration cell with disagreement <= t has
+    a max relative error <= tol (cells sorted by disagreement; the longest prefix whose running maximum
+    of the error stays within tol). Returns -inf when even the most confident cell misses tol (every
+    cell then falls back)."""
+    import torch
+    d = disagreement.double()
+    order = torch.argsort(d)
+    run = torch.cummax(err.double()[order], dim=0).values
+    ok = int((run <= tol).sum())  # running maximum is monotone: the prefix length
+    if ok == 0:
+        return float("-inf")
+    t = float(d[order[ok - 1]])
+    if ok < len(order) and float(d[order[ok]]) == t:  # ties at the boundary: step below the tied value
+        t = float(np.nextafter(np.float32(t), np.float32(-np.inf)))
+    return t
+
+
+__all__ = ["Surrogate", "generate_cells", "distribution", "DISTRIBUTIONS", "CombustionError", "transport_pair",
+           "calibrate_threshold", "max_rel_err_per_cell"]

@@ -241,6 +241,29 @@ int cb_surrogate_train(cb_surrogate* s, int32_t steps, float* losses);
  * final. */
 int cb_surrogate_transport(cb_surrogate* s, size_t n, const double* const* inputs, double* const* outputs,
                            uint32_t flags, uint32_t audit_stride, cb_surrogate_stats* stats, void* stream);
+/* Ensemble-gated transport (no reference counterpart): two networks of the same mechanism and shape,
+ * trained from different initial weights, evaluate every cell; the outputs are the mean of their logs.
+ * Their disagreement max_j |ln y_a,j - ln y_b,j| is the cell's error estimate: a cell whose
+ * disagreement exceeds `threshold`, or whose raw inputs leave the first network's training range, is
+ * recomputed by the fallback kernel (CB_FALLBACK_MIXED: the mixed-precision transport kernel, about 1e-6;
+ * CB_FALLBACK_PLAIN: the plain FP64 kernel). threshold = +inf gates on the training range alone; a
+ * negative threshold sends every cell to the fallback kernel, which then runs alone (no network, no
+ * audit, `disagreement` untouched). Every
+ * audit_stride-th other cell is recomputed by the plain kernel, which judges the reported error, and
+ * keeps the plain values. `disagreement` (device, n floats, may be NULL) receives every cell's estimate,
+ * from which a caller calibrates the threshold for a stated error on cells of its own. Flags:
+ * CB_UNIFORM_PRESSURE, CB_SURROGATE_TIMING. Returns when the outputs and `stats` are final. */
+typedef struct cb_surrogate_gate {
+    double threshold;
+    uint32_t audit_stride;  /* 0: no audit */
+    uint32_t fallback;      /* CB_FALLBACK_MIXED or CB_FALLBACK_PLAIN */
+    float* disagreement;
+} cb_surrogate_gate;
+#define CB_FALLBACK_MIXED 0u
+#define CB_FALLBACK_PLAIN 1u
+int cb_surrogate_transport_pair(cb_surrogate* a, cb_surrogate* b, size_t n, const double* const* inputs,
+                                double* const* outputs, uint32_t flags, const cb_surrogate_gate* gate,
+                                cb_surrogate_stats* stats, void* stream);
 /* Parameters (FP32 master copy, layout of cb_surrogate_info) and normalisation (host arrays of
  * n_features floats each; any may be NULL). Setting parameters resets the Adam moments. */
 int cb_surrogate_get_params(const cb_surrogate* s, float* params);

@@ -1,6 +1,7 @@
 """The learned transport surrogate through the C ABI: the device cell generator against the host one,
 the tcgen05 GEMM forward and backward against the FP64 network restatement (oracle/mlp.py), training,
-the trust gate and audit, and what the trained network gains over the plain transport kernel.
+the trust gate and audit, the ensemble gate with a calibrated error bound, and what the trained network
+gains over the plain and mixed-precision transport kernels.
 
 Stated error bars: network outputs within 2e-3 and gradients within 1e-2 (norm-relative, per layer) of
 the restatement that rounds the same values to BF16; within 3e-2 / 6e-2 of the unrounded FP64 network.
@@ -175,9 +176,22 @@ def test_gate_fallback_warp_per_cell_matches_plain_kernel(config, width):
     assert st["audit_max_rel_err"][2] <= float(err[2:].max()) * (1 + 1e-6)
 
 
-def test_trained_network_gain_over_plain_kernel():
+def _timed(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t) / reps
+
+
+def test_trained_network_gain_over_plain_and_mixed_kernels():
     """What the trained network gains: transport cells/s through the gated surrogate against the plain
-    FP64 kernel on the same cells (53 species), at the error the audit reports."""
+    FP64 kernel and the mixed-precision kernel on the same cells (53 species), with its error against the
+    plain kernel over every cell. The single-network gate (training range only) bounds nothing: the
+    error is reported, and test_ensemble_gate_calibrated_bound states a bound."""
     import torch
     from combustion_gb300 import surrogate as S
     mech, s, _, losses = _trained("k53", 1 << 18, 300, 16384)
@@ -190,22 +204,64 @@ def test_trained_network_gain_over_plain_kernel():
     tin[0] = cells[0] * cells[3] / cells[2]
     tin[1] = cells[2] / T0
     tin[2:] = cells[4:]
-    plain = torch.empty_like(out)
-
-    def timed(fn, reps=3):
-        fn()
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        for _ in range(reps):
-            fn()
-        torch.cuda.synchronize()
-        return (time.perf_counter() - t) / reps
-
-    t_plain = timed(lambda: mech.transport(tin, plain))
+    plain, mixed = torch.empty_like(out), torch.empty_like(out)
+    t_plain = _timed(lambda: mech.transport(tin, plain))
+    t_mixed = _timed(lambda: mech.transport(tin, mixed, mixed=True))
     stats = {}
-    t_sur = timed(lambda: stats.update(s.transport(cells, out, audit_stride=1024)))
-    err = ((out - plain).abs() / plain.abs())
-    print(f"plain {n / t_plain:.3e} cells/s, surrogate {n / t_sur:.3e} cells/s ({t_plain / t_sur:.1f}x); "
-          f"rms rel err {float(err.pow(2).mean().sqrt()):.2e}, audit {stats}")
+    t_sur = _timed(lambda: stats.update(s.transport(cells, out, audit_stride=1024)))
+    err = (out - plain).abs() / plain.abs()
+    err_mixed = float(((mixed - plain).abs() / plain.abs()).max())
+    print(f"plain {n / t_plain:.3e} cells/s, mixed {n / t_mixed:.3e} cells/s (max rel err {err_mixed:.1e}), "
+          f"surrogate {n / t_sur:.3e} cells/s ({t_plain / t_sur:.1f}x plain, {t_mixed / t_sur:.2f}x mixed); "
+          f"rms rel err {float(err.pow(2).mean().sqrt()):.2e}, max {float(err.max()):.2e}, audit {stats}")
     assert t_sur < t_plain
+    assert err_mixed < 1e-5
     assert stats["audited_cells"] > 0
+
+
+def test_ensemble_gate_calibrated_bound():
+    """Two networks trained from different initial weights; their disagreement is each cell's error
+    estimate. A threshold calibrated on 2^20 cells for half the stated error (0.2 here, for networks
+    trained 1,500 steps) keeps every one of 2^18 fresh cells within the stated error: the cells above it
+    go to the mixed-precision kernel. At 1e-4 (the mixed form's bar) no calibration cell of these
+    networks is accurate enough: every cell falls back, the networks are skipped, and the outputs are the
+    mixed kernel's, bit for bit."""
+    import torch
+    from combustion_gb300 import surrogate as S
+    mech, a, _, _ = _trained("k53", 1 << 20, 1500, 16384, seed=3)
+    b = S.Surrogate(mech, width=256, hidden_layers=4, batch=16384, lr=2e-3, lr_final=1e-4, seed=4)  # same mechanism
+    b.generate(1 << 20, S.distribution("k53", seed=2))
+    b.train(1500)
+    K = mech.K
+
+    def reference(cells, mixed):
+        tr = torch.empty((K + 2, cells.shape[1]), dtype=torch.float64, device="cuda")
+        rr = torch.empty((mech.A + 2, cells.shape[1]), dtype=torch.float64, device="cuda")
+        mech.rates_transport(cells, rr, tr, mixed=mixed)
+        return tr
+
+    cal = S.generate_cells(mech, 1 << 20, S.distribution("k53", seed=11))
+    out = torch.empty((K + 2, cal.shape[1]), dtype=torch.float64, device="cuda")
+    d = torch.empty(cal.shape[1], dtype=torch.float32, device="cuda")
+    st = S.transport_pair(a, b, cal, out, float("inf"), audit_stride=0, disagreement=d)
+    err = S.max_rel_err_per_cell(out, reference(cal, False))
+    assert bool(err.isfinite().all()) and bool(d.isfinite().all())
+    print(f"calibration: median max rel err {float(err.median()):.2e}, disagreement median {float(d.median()):.2e}, "
+          f"correlation of logs {float(torch.corrcoef(torch.stack([d.double().log(), err.log()]))[0, 1]):.2f}, "
+          f"range fallbacks {st['fallback_cells']}")
+    test = S.generate_cells(mech, 1 << 18, S.distribution("k53", seed=13))
+    plain = reference(test, False)
+    for tol in (0.2, 1e-4):
+        t = S.calibrate_threshold(d, err, tol / 2)
+        res = torch.empty_like(plain)
+        st = S.transport_pair(a, b, test, res, t, audit_stride=256)
+        e = S.max_rel_err_per_cell(res, plain)
+        frac = st["fallback_cells"] / test.shape[1]
+        print(f"stated {tol:g}: threshold {t:.3e}, fallback {100 * frac:.3f}%, max rel err {float(e.max()):.2e}, "
+              f"audit {st['audit_max_rel_err']}")
+        assert float(e.max()) <= tol
+        if tol == 1e-4:
+            assert t == float("-inf") and st["fallback_cells"] == test.shape[1]
+            assert torch.equal(res, reference(test, True))
+        else:
+            assert 0.0 < frac < 1.0
