@@ -121,6 +121,7 @@ struct cb_surrogate {
     bf16 *Z[kMaxLayers] = {}, *Act[kMaxLayers] = {}, *ActT[kMaxLayers] = {};
     bf16 *dY = nullptr, *dYT = nullptr, *dZ[2] = {}, *dZT[2] = {};
     CUtensorMap mAct_A[kMaxLayers], mActT_B[kMaxLayers], mActT_A, mdYT_B, mdY_A, mdZT_A[2], mdZ_A[2];
+    CUtensorMap mZ_S[kMaxLayers], mAct_S[kMaxLayers], mdZ_S[2];  // TMA store maps (32-row boxes) of the epilogues
     float* ws = nullptr;
     float* loss_part = nullptr;
     float* losses = nullptr;  // mean squared error of every step since the parameters were set
@@ -132,7 +133,7 @@ struct cb_surrogate {
     // inference buffers
     bf16 *Xi = nullptr, *Hi[2] = {};
     float* Yi = nullptr;
-    CUtensorMap mXi, mHi[2];
+    CUtensorMap mXi, mHi[2], mHi_S[2];
     uint32_t *fail_idx = nullptr, *audit_idx = nullptr, *gate_count = nullptr;
     double* audit_plain = nullptr;
     size_t fail_cap = 0, audit_cap = 0;  // grown to the largest call
@@ -228,7 +229,10 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
             p.ld_outf = s->n_out;
         }
         const CUtensorMap& a = l == 0 ? mX : s->mAct_A[l - 1];
-        SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st));
+        if (epi == kEpiHidden)
+            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st, backward ? &s->mZ_S[l] : nullptr, &s->mAct_S[l]));
+        else
+            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st));
     }
     if (!backward) return CB_OK;
     for (int l = L - 1; l >= 0; l--) {
@@ -274,7 +278,7 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         q.outT = s->dZT[(l - 1) % 2];
         q.ld_outT = s->batch;
         const CUtensorMap& a = l == L - 1 ? s->mdY_A : s->mdZ_A[l % 2];
-        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mWT[l], q, st));
+        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mWT[l], q, st, &s->mdZ_S[(l - 1) % 2], nullptr));
     }
     if (update) {
         SUR_CUDA(adam(adam_args(s, total_steps), st));
@@ -326,6 +330,8 @@ int ensure_inference(cb_surrogate* s, size_t rows) {
     SUR_RC(make_map(&s->mXi, s->Xi, s->n_in, rows, kBM));
     SUR_RC(make_map(&s->mHi[0], s->Hi[0], s->width, rows, kBM));
     SUR_RC(make_map(&s->mHi[1], s->Hi[1], s->width, rows, kBM));
+    SUR_RC(make_map(&s->mHi_S[0], s->Hi[0], s->width, rows, 32));
+    SUR_RC(make_map(&s->mHi_S[1], s->Hi[1], s->width, rows, 32));
     return CB_OK;
 }
 
@@ -367,7 +373,10 @@ int infer_rows(cb_surrogate* s, int rows, const CUtensorMap& mX, cudaStream_t st
             p.ld_outf = s->n_out;
         }
         const CUtensorMap& a = l == 0 ? mX : s->mHi[(l - 1) % 2];
-        SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st));
+        if (epi == kEpiHidden)
+            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st, nullptr, &s->mHi_S[l % 2]));
+        else
+            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st));
     }
     return CB_OK;
 }
@@ -505,6 +514,8 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     for (int l = 0; l < s->hidden && !rc; l++) {
         rc = make_map(&s->mAct_A[l], s->Act[l], Wd, B, kBM);
         rc = rc ? rc : make_map(&s->mActT_B[l], s->ActT[l], B, Wd, bn_for((int)Wd));
+        rc = rc ? rc : make_map(&s->mZ_S[l], s->Z[l], Wd, B, 32);
+        rc = rc ? rc : make_map(&s->mAct_S[l], s->Act[l], Wd, B, 32);
     }
     rc = rc ? rc : make_map(&s->mActT_A, s->ActT[s->hidden - 1], B, Wd, kBM);
     rc = rc ? rc : make_map(&s->mdYT_B, s->dYT, B, s->n_out, bn_for(s->n_out));
@@ -512,6 +523,7 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     for (int h = 0; h < 2 && !rc; h++) {
         rc = make_map(&s->mdZT_A[h], s->dZT[h], B, Wd, kBM);
         rc = rc ? rc : make_map(&s->mdZ_A[h], s->dZ[h], Wd, B, kBM);
+        rc = rc ? rc : make_map(&s->mdZ_S[h], s->dZ[h], Wd, B, 32);
     }
     rc = rc ? rc : make_map(&s->mXs, s->Xs, s->n_in, B, kBM);
     rc = rc ? rc : make_map(&s->mXTs, s->XTs, B, s->n_in, bn_for(s->n_in));

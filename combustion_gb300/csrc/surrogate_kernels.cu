@@ -1,13 +1,16 @@
 // Kernels of the learned transport surrogate (declarations and roles in surrogate_kernels.cuh).
 //
 // The GEMM is D[M][N] = A[M][K] B[N][K]^T over BF16 operands with an FP32 accumulator in tensor memory:
-// one 128 x BN output tile per block, operands streamed through a ring of shared-memory stages by TMA
+// 128 x BN output tiles taken in turn by a persistent block per SM (two accumulators in tensor memory,
+// so that one tile's epilogue runs under the next tile's MMAs), operands streamed through a ring of shared-memory stages by TMA
 // (128-byte swizzle, K-major), tcgen05.mma issued by one thread, the accumulator read back by eight
 // epilogue warps (one TMEM lane, i.e. one output row, per thread; two warps per lane quarter, each on
 // half of the columns) which apply the layer's element-wise work before anything is written to global
 // memory. Every mbarrier wait is bounded: a wait that runs
 // out sets a status bit, lets in-flight copies land and the block still frees its tensor memory.
 #include <cuda_bf16.h>
+
+#include <cstring>
 
 #include "device_common.cuh"
 #include "device_math.cuh"
@@ -63,9 +66,28 @@ __device__ __forceinline__ void store_col_bf16(__nv_bfloat16* base, int ld, int 
     __syncwarp();  // the next chunk rewrites the stage
 }
 
+// Row r (this lane) of a 32 x 64 BF16 box in the 128-byte swizzle of its TMA store map: columns
+// [32 half, 32 half + 32) are the 16-byte chunks 4 half .. 4 half + 3, chunk c of row r stored at
+// chunk position c ^ (r % 8) (eight consecutive rows hit eight different bank groups).
+__device__ __forceinline__ void stage_row_half(uint8_t* box, int r, int half, const float* a) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int c = 4 * half + j;
+        *reinterpret_cast<uint4*>(box + r * 128 + ((c ^ (r & 7)) << 4)) =
+            make_uint4(pack_bf16(a[8 * j], a[8 * j + 1]), pack_bf16(a[8 * j + 2], a[8 * j + 3]),
+                       pack_bf16(a[8 * j + 4], a[8 * j + 5]), pack_bf16(a[8 * j + 6], a[8 * j + 7]));
+    }
+}
+
+// The epilogue of one tile for one warp: its 32 rows (TMEM lane quarter q) and its half h of the columns,
+// 32 columns per TMEM load. The hidden-layer and data-gradient epilogues (tiles at least 128 wide) put
+// their row-major BF16 outputs into 32 x 64 boxes in shared memory and store each box with one TMA store
+// (lane 0); the other outputs are written directly.
 template <int BN, int EPI>
-__device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int warp, int lane, int m0, int n0,
-                                         __nv_bfloat16* stage) {
+__device__ __forceinline__ void epilogue(const GemmParams& p, const RowMaps& rm, uint32_t tmem, int warp, int lane,
+                                         int m0, int n0, int z, int mt, __nv_bfloat16* stage, uint8_t* box0,
+                                         uint8_t* box1) {
+    constexpr bool kTmaRows = (EPI == kEpiHidden || EPI == kEpiDgrad) && BN >= 128;
     const int q = warp & 3;          // the TMEM lane quarter this warp may read
     const int h = (warp - 2) >> 2;   // and its half of the tile's columns
     const int row = m0 + q * 32 + lane;
@@ -73,11 +95,18 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
     float lsum = 0.f;
 #pragma unroll 1
     for (int c = h * (BN / 2); c < (h + 1) * (BN / 2); c += 32) {
+        const int half = (c >> 5) & 1;  // which half of its 64-column box (BN / 2 is a multiple of 64)
+        if constexpr (kTmaRows) {
+            if (half == 0) {  // the boxes' previous stores have read them
+                if (lane == 0) umma::bulk_wait_read();
+                __syncwarp();
+            }
+        }
         float v[32];
         umma::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
         const int n = n0 + c;
         if constexpr (EPI == kEpiPartial) {
-            float4* dst = reinterpret_cast<float4*>(p.outf + ((size_t)blockIdx.z * p.M + row) * p.ld_outf + n);
+            float4* dst = reinterpret_cast<float4*>(p.outf + ((size_t)z * p.M + row) * p.ld_outf + n);
 #pragma unroll
             for (int j = 0; j < 8; j++) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         } else if constexpr (EPI == kEpiLinear) {
@@ -94,8 +123,13 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
                 v[j] = z;
                 a[j] = siluf_(z);
             }
-            if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
-            store_row_bf16(p.out2, p.ld_out2, row, n, a);
+            if constexpr (kTmaRows) {
+                if (p.out) stage_row_half(box0, lane, half, v);
+                stage_row_half(box1, lane, half, a);
+            } else {
+                if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
+                store_row_bf16(p.out2, p.ld_out2, row, n, a);
+            }
             if (p.outT) store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
         } else if constexpr (EPI == kEpiLoss) {
             const float* t = p.target + (size_t)(trow0 + row) * p.ld_target;
@@ -126,38 +160,63 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, uint32_t tmem, int
                     a[k + 1] = v[k + 1] * (s1 * fmaf(z1, 1.f - s1, 1.f));
                 }
             }
-            store_row_bf16(p.out, p.ld_out, row, n, a);
+            if constexpr (kTmaRows) stage_row_half(box0, lane, half, a);
+            else store_row_bf16(p.out, p.ld_out, row, n, a);
             store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
+        }
+        if constexpr (kTmaRows) {
+            if (half == 1) {  // the box is complete: one TMA store per output
+                umma::fence_async_shared();
+                __syncwarp();
+                if (lane == 0) {
+                    const int x = n0 + c - 32, y = m0 + q * 32;
+                    if (EPI == kEpiHidden) {
+                        if (p.out) umma::tma_store_2d(&rm.out, smem_u32(box0), x, y);
+                        umma::tma_store_2d(&rm.out2, smem_u32(box1), x, y);
+                    } else {
+                        umma::tma_store_2d(&rm.out, smem_u32(box0), x, y);
+                    }
+                    umma::bulk_commit();
+                }
+            }
         }
     }
     if constexpr (EPI == kEpiLoss) {  // one partial per warp: no barrier among the epilogue warps
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-        if (lane == 0) p.loss[blockIdx.x * kEpiWarps + h * 4 + q] = lsum;
+        if (lane == 0) p.loss[mt * kEpiWarps + h * 4 + q] = lsum;
     }
 }
 
+// Persistent: block b takes work items b, b + gridDim.x, ... (item = row tile + Mt (column tile + Nt
+// split)). The ring's stage index and phase run on across items, and the accumulator alternates between
+// two TMEM buffers, so that the producer and the MMA issuer start the next item while the epilogue
+// warps drain the last one (acc_full[b]: MMAs of buffer b done; acc_empty[b]: its epilogue done).
 template <int BN, int EPI>
 __global__ void __launch_bounds__(kGemmThreads, 1)
-    gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmParams p) {
+    gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmParams p,
+                const __grid_constant__ RowMaps rm) {
     constexpr uint32_t kA = kBM * 128, kB = BN * 128, kStage = kA + kB;
-    constexpr int STAGES = (kGemmSmem - 1024) / (int)kStage;
+    constexpr int STAGES = kGemmRing / (int)kStage;
     static_assert(STAGES >= 2, "operand ring needs two stages");
-    constexpr uint32_t kCols = BN;  // TMEM columns: a power of two >= 32
+    constexpr uint32_t kCols = 2 * BN;  // two accumulators; TMEM columns: a power of two >= 32
     extern __shared__ uint8_t dsm[];
-    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full;
+    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], mma_done;
     __shared__ uint32_t tmem_s;
     const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
-    const int kb0 = (int)(((long long)blockIdx.z * p.k_blocks) / p.splits);
-    const int nkb = (int)(((long long)(blockIdx.z + 1) * p.k_blocks) / p.splits) - kb0;
+    const int Mt = p.M / kBM, Nt = p.N / BN;
+    const int n_items = Mt * Nt * p.splits;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             umma::mbar_init(smem_u32(&full[s]), 1);
             umma::mbar_init(smem_u32(&empty[s]), 1);
         }
-        umma::mbar_init(smem_u32(&acc_full), 1);
+        for (int b = 0; b < 2; b++) {
+            umma::mbar_init(smem_u32(&acc_full[b]), 1);
+            umma::mbar_init(smem_u32(&acc_empty[b]), kEpiWarps);
+        }
+        umma::mbar_init(smem_u32(&mma_done), 1);
         umma::fence_mbar_init();
     }
     if (warp == 1) {
@@ -172,52 +231,85 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     if (warp == 0) {
         if (lane == 0) {  // TMA producer
             const int off = p.dyn ? *p.row0 : 0;
-            const int ay = p.a_y0 + m0 + ((p.dyn & kDynAy) ? off : 0);
-            const int bx = p.b_x0 + ((p.dyn & kDynBx) ? off : 0);
-            int issued = 0;
-            for (int i = 0; i < nkb; i++) {
-                const int s = i % STAGES;
-                if (i >= STAGES && !umma::mbar_wait(smem_u32(&empty[s]), ((i / STAGES) & 1) ^ 1)) {
-                    ok = false;
-                    break;
+            int it = 0;  // k blocks issued by this block, over all its items
+            for (int w = blockIdx.x; w < n_items && ok; w += gridDim.x) {
+                const int mt = w % Mt, nt = (w / Mt) % Nt, z = w / (Mt * Nt);
+                const int kb0 = (int)(((long long)z * p.k_blocks) / p.splits);
+                const int nkb = (int)(((long long)(z + 1) * p.k_blocks) / p.splits) - kb0;
+                const int ay = p.a_y0 + mt * kBM + ((p.dyn & kDynAy) ? off : 0);
+                const int bx = p.b_x0 + ((p.dyn & kDynBx) ? off : 0);
+                for (int i = 0; i < nkb; i++, it++) {
+                    const int s = it % STAGES;
+                    if (it >= STAGES && !umma::mbar_wait(smem_u32(&empty[s]), ((it / STAGES) & 1) ^ 1)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t bar = smem_u32(&full[s]), sa = base + (uint32_t)s * kStage;
+                    const int kx = (kb0 + i) * kBK;
+                    umma::mbar_expect_tx(bar, kStage);
+                    umma::tma_load_2d(sa, &ta, bar, p.a_x0 + kx, ay);
+                    umma::tma_load_2d(sa + kA, &tb, bar, bx + kx, p.b_y0 + nt * BN);
                 }
-                const uint32_t bar = smem_u32(&full[s]), sa = base + (uint32_t)s * kStage;
-                const int kx = (kb0 + i) * kBK;
-                umma::mbar_expect_tx(bar, kStage);
-                umma::tma_load_2d(sa, &ta, bar, p.a_x0 + kx, ay);
-                umma::tma_load_2d(sa + kA, &tb, bar, bx + kx, p.b_y0 + n0);
-                issued = i + 1;
             }
             if (!ok)  // let the copies already issued land before the block exits
-                for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; i++)
+                for (int i = it > STAGES ? it - STAGES : 0; i < it; i++)
                     umma::mbar_wait(smem_u32(&full[i % STAGES]), (i / STAGES) & 1);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
             constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN);
-            for (int i = 0; i < nkb; i++) {
-                const int s = i % STAGES;
-                if (!umma::mbar_wait(smem_u32(&full[s]), (i / STAGES) & 1)) {
+            int it = 0, t = 0;
+            for (int w = blockIdx.x; w < n_items && ok; w += gridDim.x, t++) {
+                const int z = w / (Mt * Nt);
+                const int nkb = (int)(((long long)(z + 1) * p.k_blocks) / p.splits) -
+                                (int)(((long long)z * p.k_blocks) / p.splits);
+                const int b = t & 1;
+                // buffer b is free once the epilogue of item t - 2 has read it
+                if (t >= 2 && !umma::mbar_wait(smem_u32(&acc_empty[b]), ((t >> 1) & 1) ^ 1)) {
                     ok = false;
                     break;
                 }
                 umma::fence_after_sync();
-                const uint32_t sa = base + (uint32_t)s * kStage, sb = sa + kA;
+                const uint32_t acc = tmem + (uint32_t)(b * BN);
+                for (int i = 0; i < nkb; i++, it++) {
+                    const int s = it % STAGES;
+                    if (!umma::mbar_wait(smem_u32(&full[s]), (it / STAGES) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    umma::fence_after_sync();
+                    const uint32_t sa = base + (uint32_t)s * kStage, sb = sa + kA;
 #pragma unroll
-                for (int k = 0; k < kBK / 16; k++)
-                    umma::mma_bf16(tmem, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k), idesc,
-                                   (i | k) != 0);
-                umma::mma_commit(smem_u32(&empty[s]));  // frees the stage once these MMAs are done
+                    for (int k = 0; k < kBK / 16; k++)
+                        umma::mma_bf16(acc, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k), idesc,
+                                       (i | k) != 0);
+                    umma::mma_commit(smem_u32(&empty[s]));  // frees the stage once these MMAs are done
+                }
+                if (ok) umma::mma_commit(smem_u32(&acc_full[b]));  // the item's MMAs have completed
             }
-            umma::mma_commit(smem_u32(&acc_full));  // every MMA issued above has completed
+            // every MMA issued above has completed before tensor memory is freed
+            umma::mma_commit(smem_u32(&mma_done));
+            umma::mbar_wait(smem_u32(&mma_done), 0);
         }
-    } else {  // epilogue warps (the wait's outcome made warp-uniform: tcgen05.ld needs the whole warp)
-        ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full), 0));
-        umma::fence_after_sync();
-        // Every MMA has completed (so every operand stage was consumed): the ring is free, and each
-        // epilogue warp stages its transposed chunks in 2 KB of it.
-        __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(dsm + (base - smem_u32(dsm)) + (warp - 2) * 2048);
-        if (ok) epilogue<BN, EPI>(p, tmem, warp, lane, m0, n0, stage);
+    } else {  // epilogue warps (each wait's outcome made warp-uniform: tcgen05.ld needs the whole warp)
+        uint8_t* after_ring = dsm + (base - smem_u32(dsm)) + kGemmRing;
+        __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(after_ring + (warp - 2) * kStageT);
+        uint8_t* box0 = after_ring + kEpiWarps * kStageT + (warp - 2) * 2 * kStageBox;  // 1024-byte aligned
+        uint8_t* box1 = box0 + kStageBox;
+        int t = 0;
+        for (int w = blockIdx.x; w < n_items; w += gridDim.x, t++) {
+            const int mt = w % Mt, nt = (w / Mt) % Nt, z = w / (Mt * Nt);
+            const int b = t & 1;
+            ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full[b]), (t >> 1) & 1));
+            if (!ok) break;
+            umma::fence_after_sync();
+            epilogue<BN, EPI>(p, rm, tmem + (uint32_t)(b * BN), warp, lane, mt * kBM, nt * BN, z, mt, stage, box0,
+                              box1);
+            umma::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) umma::mbar_arrive(smem_u32(&acc_empty[b]));
+        }
+        if (lane == 0) umma::bulk_wait_all();  // this warp's TMA stores have completed
     }
     if (!ok) atomicOr(p.status, kStatusGemmTimeout);
     umma::fence_before_sync();
@@ -229,19 +321,32 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
 }
 
+int sm_count_g() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
 template <int BN, int EPI>
-cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
-    dim3 grid(p.M / kBM, p.N / BN, p.splits);
-    gemm_kernel<BN, EPI><<<grid, kGemmThreads, kGemmSmem, st>>>(a, b, p);
+cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, const RowMaps& rm,
+                        cudaStream_t st) {
+    const int items = (p.M / kBM) * (p.N / BN) * p.splits;  // one block per SM at most, persistent
+    gemm_kernel<BN, EPI><<<items < sm_count_g() ? items : sm_count_g(), kGemmThreads, kGemmSmem, st>>>(a, b, p, rm);
     return cudaGetLastError();
 }
 
 template <int EPI>
-cudaError_t gemm_bn(int BN, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
+cudaError_t gemm_bn(int BN, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, const RowMaps& rm,
+                    cudaStream_t st) {
     switch (BN) {
-    case 64: return launch_gemm<64, EPI>(a, b, p, st);
-    case 128: return launch_gemm<128, EPI>(a, b, p, st);
-    case 256: return launch_gemm<256, EPI>(a, b, p, st);
+    case 64: return launch_gemm<64, EPI>(a, b, p, rm, st);
+    case 128: return launch_gemm<128, EPI>(a, b, p, rm, st);
+    case 256: return launch_gemm<256, EPI>(a, b, p, rm, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -265,34 +370,69 @@ cudaError_t gemm_setup() {
     return e;
 }
 
-cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st) {
+cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st,
+                 const CUtensorMap* out_map, const CUtensorMap* out2_map) {
     if (p.M % kBM || p.N % BN || p.splits < 1 || p.splits > p.k_blocks) return cudaErrorInvalidValue;
+    RowMaps rm;
+    std::memset(&rm, 0, sizeof rm);
+    if (BN >= 128 && (epi == kEpiHidden || epi == kEpiDgrad)) {  // these epilogues store through the maps
+        if ((p.out && !out_map) || (epi == kEpiHidden && !out2_map)) return cudaErrorInvalidValue;
+        if (out_map) rm.out = *out_map;
+        if (out2_map) rm.out2 = *out2_map;
+    }
     switch (epi) {
-    case kEpiPartial: return gemm_bn<kEpiPartial>(BN, a, b, p, st);
-    case kEpiHidden: return gemm_bn<kEpiHidden>(BN, a, b, p, st);
-    case kEpiLoss: return gemm_bn<kEpiLoss>(BN, a, b, p, st);
-    case kEpiDgrad: return gemm_bn<kEpiDgrad>(BN, a, b, p, st);
-    case kEpiLinear: return gemm_bn<kEpiLinear>(BN, a, b, p, st);
+    case kEpiPartial: return gemm_bn<kEpiPartial>(BN, a, b, p, rm, st);
+    case kEpiHidden: return gemm_bn<kEpiHidden>(BN, a, b, p, rm, st);
+    case kEpiLoss: return gemm_bn<kEpiLoss>(BN, a, b, p, rm, st);
+    case kEpiDgrad: return gemm_bn<kEpiDgrad>(BN, a, b, p, rm, st);
+    case kEpiLinear: return gemm_bn<kEpiLinear>(BN, a, b, p, rm, st);
     default: return cudaErrorInvalidValue;
     }
 }
 
 // ---------------------------------------------------------------------------------------------------
 // Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients).
+// Four consecutive outputs per thread (16-byte loads), the splits loaded eight at a time ahead of their
+// additions; each output still adds its partials in split order.
 __global__ void reduce_partials_kernel(const float* __restrict__ ws, int splits, int M, int N, int transpose,
                                        float* __restrict__ grad) {
-    const size_t MN = (size_t)M * N;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN; i += (size_t)gridDim.x * blockDim.x) {
-        float s = 0.f;
-        for (int z = 0; z < splits; z++) s += ws[z * MN + i];
-        const size_t m = i / N, n = i % N;
-        grad[transpose ? n * M + m : i] = s;
+    const size_t MN = (size_t)M * N, MN4 = MN / 4;
+    const float4* w4 = reinterpret_cast<const float4*>(ws);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN4; i += (size_t)gridDim.x * blockDim.x) {
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        int z = 0;
+        for (; z + 8 <= splits; z += 8) {
+            float4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = w4[(size_t)(z + u) * MN4 + i];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                s.x += v[u].x;
+                s.y += v[u].y;
+                s.z += v[u].z;
+                s.w += v[u].w;
+            }
+        }
+        for (; z < splits; z++) {
+            const float4 v = w4[(size_t)z * MN4 + i];
+            s.x += v.x;
+            s.y += v.y;
+            s.z += v.z;
+            s.w += v.w;
+        }
+        const float r[4] = {s.x, s.y, s.z, s.w};
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+            const size_t e = 4 * i + h, m = e / N, n = e % N;
+            grad[transpose ? n * M + m : e] = r[h];
+        }
     }
 }
 
 cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st) {
     const size_t MN = (size_t)M * N;
-    reduce_partials_kernel<<<(unsigned)((MN + 255) / 256), 256, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0, grad);
+    if (MN % 4) return cudaErrorInvalidValue;
+    reduce_partials_kernel<<<(unsigned)((MN / 4 + 63) / 64), 64, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0, grad);
     return cudaGetLastError();
 }
 

@@ -16,7 +16,11 @@ constexpr int kGemmThreads = 320;
 constexpr int kEpiWarps = 8;       // loss partials per 128-row tile: one per epilogue warp
 constexpr int kBM = 128;           // rows per tile (one M = 128 MMA, one TMEM lane per row)
 constexpr int kBK = 64;            // K per pipeline stage: one 128-byte swizzle row of BF16
-constexpr int kGemmSmem = 193 * 1024;  // operand ring (stages x (A + B tile)) + alignment; one block per SM
+constexpr int kGemmRing = 144 * 1024;  // operand ring: stages x (A + B tile)
+// Shared memory after the ring, per epilogue warp: 2 KB for transposed stores, then two 4 KB boxes
+// (32 rows x 64 BF16, 128-byte swizzle) for the TMA stores of row-major outputs.
+constexpr int kStageT = 2048, kStageBox = 4096;
+constexpr int kGemmSmem = kGemmRing + 8 * (kStageT + 2 * kStageBox) + 1024;  // + alignment; one block per SM
 constexpr int kMaxIn = 259;        // rates-layout inputs for up to 256 species
 constexpr int kMaxOut = 258;       // transport outputs for up to 256 species
 constexpr int kMaxLayers = 8;
@@ -46,6 +50,12 @@ struct GemmParams {
     float* loss;            // one partial per epilogue warp: [row tile][kEpiWarps]
     float* outf; int ld_outf;  // FP32 output
     int* status;
+};
+
+// TMA store maps of the row-major BF16 outputs out and out2 (boxes of 64 columns x 32 rows, 128-byte
+// swizzle): the hidden-layer (Z, silu(Z)) and data-gradient (dZ) epilogues write through them.
+struct RowMaps {
+    CUtensorMap out, out2;
 };
 
 enum SurStatus : int { kStatusGemmTimeout = 2 };
@@ -154,7 +164,10 @@ cudaError_t mlp_infer(const CUtensorMap& tx, const FusedMaps& maps, const FusedP
 // Launchers (surrogate_kernels.cu). gemm_setup() raises the GEMM's shared-memory limit on the current
 // device; it runs before the first GEMM (and outside any stream capture).
 cudaError_t gemm_setup();
-cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st);
+// out_map / out2_map: store maps of p.out / p.out2 (required where the epilogue writes them: hidden layers
+// and data gradients, whose width is a multiple of 256).
+cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st,
+                 const CUtensorMap* out_map = nullptr, const CUtensorMap* out2_map = nullptr);
 cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st);
 cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st);
 cudaError_t adam(const AdamArgs& a, cudaStream_t st);

@@ -1,4 +1,4 @@
-// Blackwell (sm_103a) tensor-core primitives in inline PTX: mbarriers, 2-D TMA tile loads, TMEM
+// Blackwell (sm_103a) tensor-core primitives in inline PTX: mbarriers, 2-D TMA tile loads and stores, TMEM
 // allocation, tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in TMEM), tcgen05.commit and
 // tcgen05.ld. Operand tiles are K-major with the 128-byte swizzle that TMA writes.
 //
@@ -55,6 +55,20 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
         : "memory");
 }
+
+// 2-D tiled TMA store of a shared-memory box to global memory (bulk async group of this thread); x,
+// the inner coordinate in elements, a multiple of 64 BF16 here (16-byte aligned), y >= 0.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(src), "r"(x), "r"(y)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// This thread's bulk stores have read their shared-memory sources (which may then be rewritten).
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// This thread's bulk stores have completed.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
