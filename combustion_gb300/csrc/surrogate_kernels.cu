@@ -392,35 +392,53 @@ cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, co
 
 // ---------------------------------------------------------------------------------------------------
 // Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients).
-// Four consecutive outputs per thread (16-byte loads), the splits loaded eight at a time ahead of their
-// additions; each output still adds its partials in split order.
-__global__ void reduce_partials_kernel(const float* __restrict__ ws, int splits, int M, int N, int transpose,
-                                       float* __restrict__ grad) {
-    const size_t MN = (size_t)M * N, MN4 = MN / 4;
+// Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients): a block
+// covers 32 groups of four consecutive outputs (16-byte loads) with eight threads per group, thread g
+// summing splits g, g + 8, ... in order; the eight sums are then added in g order. Many threads per
+// output keep enough loads in flight: the partials are L2-resident and the sum is latency-bound.
+constexpr int kRedOut4 = 32, kRedGroups = 8;
+__global__ void __launch_bounds__(kRedOut4 * kRedGroups)
+    reduce_partials_kernel(const float* __restrict__ ws, int splits, int M, int N, int transpose,
+                           float* __restrict__ grad) {
+    __shared__ float4 part[kRedGroups][kRedOut4];
+    const size_t MN4 = (size_t)M * N / 4;
+    const int o = threadIdx.x % kRedOut4, g = threadIdx.x / kRedOut4;
+    const size_t i = (size_t)blockIdx.x * kRedOut4 + o;
     const float4* w4 = reinterpret_cast<const float4*>(ws);
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < MN4; i += (size_t)gridDim.x * blockDim.x) {
-        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-        int z = 0;
-        for (; z + 8 <= splits; z += 8) {
-            float4 v[8];
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < MN4) {
+        int z = g;
+        for (; z + 3 * kRedGroups < splits; z += 4 * kRedGroups) {
+            float4 v[4];
 #pragma unroll
-            for (int u = 0; u < 8; u++) v[u] = w4[(size_t)(z + u) * MN4 + i];
+            for (int u = 0; u < 4; u++) v[u] = w4[(size_t)(z + u * kRedGroups) * MN4 + i];
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
+            for (int u = 0; u < 4; u++) {
                 s.x += v[u].x;
                 s.y += v[u].y;
                 s.z += v[u].z;
                 s.w += v[u].w;
             }
         }
-        for (; z < splits; z++) {
+        for (; z < splits; z += kRedGroups) {
             const float4 v = w4[(size_t)z * MN4 + i];
             s.x += v.x;
             s.y += v.y;
             s.z += v.z;
             s.w += v.w;
         }
-        const float r[4] = {s.x, s.y, s.z, s.w};
+    }
+    part[g][o] = s;
+    __syncthreads();
+    if (g == 0 && i < MN4) {
+        float4 t = part[0][o];
+        for (int k = 1; k < kRedGroups; k++) {
+            t.x += part[k][o].x;
+            t.y += part[k][o].y;
+            t.z += part[k][o].z;
+            t.w += part[k][o].w;
+        }
+        const float r[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
         for (int h = 0; h < 4; h++) {
             const size_t e = 4 * i + h, m = e / N, n = e % N;
@@ -432,28 +450,39 @@ __global__ void reduce_partials_kernel(const float* __restrict__ ws, int splits,
 cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st) {
     const size_t MN = (size_t)M * N;
     if (MN % 4) return cudaErrorInvalidValue;
-    reduce_partials_kernel<<<(unsigned)((MN / 4 + 63) / 64), 64, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0, grad);
+    const size_t blocks = (MN / 4 + kRedOut4 - 1) / kRedOut4;
+    reduce_partials_kernel<<<(unsigned)blocks, kRedOut4 * kRedGroups, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0,
+                                                                             grad);
     return cudaGetLastError();
 }
 
 // out[r] = sum of row r of a BF16 matrix (bias gradients from the transposed output gradients), one
-// block per row, fixed reduction order.
-__global__ void row_sums_kernel(const __nv_bfloat16* __restrict__ T, int cols, int ld, float* __restrict__ out) {
-    __shared__ float part[256];
+// block of 1024 threads per row (eight 16-byte loads in flight per thread), fixed reduction order.
+__global__ void __launch_bounds__(1024) row_sums_kernel(const __nv_bfloat16* __restrict__ T, int cols, int ld,
+                                                        float* __restrict__ out) {
+    __shared__ float part[1024];
     const __nv_bfloat16* r = T + (size_t)blockIdx.x * ld;
     float s = 0.f;
-    for (int c = threadIdx.x * 8; c < cols; c += 256 * 8) {
-        const uint4 w = *reinterpret_cast<const uint4*>(r + c);
-        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+    for (int c0 = threadIdx.x * 8; c0 < cols; c0 += 1024 * 8 * 4) {
+        uint4 w[4];
 #pragma unroll
-        for (int h = 0; h < 4; h++) {
-            const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
-            s += __low2float(b) + __high2float(b);
+        for (int u = 0; u < 4; u++) {
+            const int c = c0 + u * 1024 * 8;
+            w[u] = c < cols ? *reinterpret_cast<const uint4*>(r + c) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t ws[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
+                s += __low2float(b) + __high2float(b);
+            }
         }
     }
     part[threadIdx.x] = s;
     __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
+    for (int o = 512; o > 0; o >>= 1) {
         if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
         __syncthreads();
     }
@@ -462,7 +491,7 @@ __global__ void row_sums_kernel(const __nv_bfloat16* __restrict__ T, int cols, i
 
 cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st) {
     if (cols % 8 || ld % 8) return cudaErrorInvalidValue;
-    row_sums_kernel<<<rows, 256, 0, st>>>(T, cols, ld, out);
+    row_sums_kernel<<<rows, 1024, 0, st>>>(T, cols, ld, out);
     return cudaGetLastError();
 }
 
