@@ -12,6 +12,7 @@ LIB = os.path.join(HERE, "libcombustion_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["mechanism.cpp", "kernels.cu", "kernels_mixed.cu", "capi.cu", "diagnostics.cu", "surrogate.cu",
            "surrogate_kernels.cu", "bdf.cu", "bdf_slice.cu", "bdf_slice_global.cu", "bdf_slice_global_wide.cu",
+           "bdf_slice_global_mid.cu",
            "yaml_reader.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

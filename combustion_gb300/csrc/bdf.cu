@@ -92,7 +92,8 @@ struct cb_reactors {
     // ws_slots per-warp workspaces, and per reactor its factorisation, transpose, row order and 1 / U_kk.
     bool global = false;
     bool smem_ok = false;  // one workspace fits in shared memory and CB_BDF_GLOBAL_MEMORY is not set
-    bool wide = false;     // global memory: the 128-register kernel (two blocks per SM) instead of 64
+    int regs = 64;         // global memory: the slice kernel's register cap (64: four blocks of 256 threads per
+                           // SM, 80: three, 128: two)
     uint8_t* ws = nullptr;
     size_t ws_slots = 0;
     double *LUr = nullptr, *LUt = nullptr, *rdiag_r = nullptr;
@@ -231,7 +232,8 @@ cudaError_t ensure_global(cb_reactors* s) {
 SliceFn slice_fn(const cb_reactors* s) {
     const bool mixed = (s->opt.flags & CB_BDF_MIXED_RHS) != 0;
     if (!s->global) return slice_kernel_fn(mixed);
-    return s->wide ? slice_kernel_global_wide_fn(mixed) : slice_kernel_global_fn(mixed);
+    return s->regs == 128 ? slice_kernel_global_wide_fn(mixed)
+                          : s->regs == 80 ? slice_kernel_global_mid_fn(mixed) : slice_kernel_global_fn(mixed);
 }
 
 // Shared-memory limit and grid of a launch shape (outside any stream capture).
@@ -493,16 +495,20 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     BDF_CUDA(cudaSetDevice(s->device));
     // candidates: workspaces in shared or global memory, reactors in flight per block, tables in shared
     // memory or read through L1
-    struct Cand { int warps, tables, global, wide; };
+    struct Cand { int warps, tables, global, regs; };
     std::vector<Cand> cands;
-    const bool placement = s->global, wide = s->wide;
+    const bool placement = s->global;
+    const int regs = s->regs;
     for (int g = s->smem_ok ? 0 : 1; g <= 1; g++) {
         s->global = g != 0;
         for (int tables = 1; tables >= 0; tables--)
             for (int w = 1; w <= 8; w++)
                 if (shape_fits(s, w, tables) && (!g || (w & (w - 1)) == 0)) {
-                    cands.push_back({w, tables, g, 0});
-                    if (g && w >= 4) cands.push_back({w, tables, g, 1});  // 128 registers: full blocks only
+                    cands.push_back({w, tables, g, 64});
+                    if (g && w >= 4) {  // 80 and 128 registers: full blocks only
+                        cands.push_back({w, tables, g, 80});
+                        cands.push_back({w, tables, g, 128});
+                    }
                 }
     }
     s->global = placement;
@@ -521,16 +527,17 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         size_t n;
         int steps, peak;
         double* traj;
-        bool global, wide;
+        bool global;
+        int regs;
         ~Restore() {
             s->n = n;
             s->opt.slice_steps = steps;
             s->traj = traj;
             s->peak_k = peak;
             s->global = global;
-            s->wide = wide;
+            s->regs = regs;
         }
-    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj, placement, wide};
+    } restore{s, s->n, s->opt.slice_steps, s->peak_k, s->traj, placement, regs};
     s->traj = nullptr;
     s->peak_k = -1;
     s->n = n_cal;
@@ -546,7 +553,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         cudaMemcpy(s->D, d0.data(), n_cal * kDRows * (size_t)s->N * sizeof(double), cudaMemcpyHostToDevice);
         cudaMemset(s->counters, 0, 4 * sizeof(int));
         s->global = c.global != 0;
-        s->wide = c.wide != 0;
+        s->regs = c.regs;
         if (s->global && ensure_global(s) != cudaSuccess) {
             cudaGetLastError();  // out of memory for the global placement: its candidates are skipped
             continue;
@@ -566,7 +573,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
             out->candidates[tried].warps_per_block = c.warps;
             out->candidates[tried].tables_in_shared = c.tables;
             out->candidates[tried].global_memory = c.global;
-            out->candidates[tried].register_cap = c.global ? (c.wide ? 128 : 64) : 0;
+            out->candidates[tried].register_cap = c.global ? c.regs : 0;
             out->candidates[tried].ms = ms;
         }
         tried++;
@@ -582,9 +589,9 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
     s->traj = restore.traj;
     s->peak_k = restore.peak;
     restore.global = pick.global != 0;
-    restore.wide = pick.wide != 0;
+    restore.regs = pick.regs;
     s->global = restore.global;
-    s->wide = restore.wide;
+    s->regs = restore.regs;
     BDF_CUDA(cudaMemcpy(s->head, h0.data(), hb, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemcpy(s->D, d0.data(), db, cudaMemcpyHostToDevice));
     BDF_CUDA(cudaMemset(s->counters, 0, 4 * sizeof(int)));
@@ -595,7 +602,7 @@ int cb_reactors_autotune(cb_reactors* s, int32_t calib_reactors, cb_reactor_tuni
         out->warps_per_block = pick.warps;
         out->tables_in_shared = pick.tables;
         out->global_memory = pick.global;
-        out->register_cap = pick.global ? (pick.wide ? 128 : 64) : 0;
+        out->register_cap = pick.global ? pick.regs : 0;
         out->n_candidates = std::min(tried, 32);
         out->calib_reactors = (int32_t)n_cal;
     }
@@ -678,7 +685,7 @@ int cb_reactors_integrate(cb_reactors* s, cb_reactor_stats* stats) {
         stats->warps_per_block = s->warps;
         stats->tables_in_shared = s->smem_tables;
         stats->global_memory = s->global ? 1 : 0;
-        stats->register_cap = s->global ? (s->wide ? 128 : 64) : 0;
+        stats->register_cap = s->global ? s->regs : 0;
         stats->graph_replays = replays;
         stats->slices = replays * G;
     }

@@ -910,34 +910,49 @@ __device__ __forceinline__ double rms_scaled(const double* x, const double* rsca
     return sqrt(warp_sum(s) / N);
 }
 
-// D[0..q] <- (R U)^T D[0..q], R = R(q, factor), U = R(q, 1) (step size change by `factor`).
+// D[0..q] <- (R U)^T D[0..q], R = R(q, factor), U = R(q, 1) (step size change by `factor`), in registers:
+// lane j computes column j of R and of U (R[i][j] = R[i-1][j] ((i-1) - factor j) / i), then column j of
+// R U from row i of R broadcast by shuffles; the columns of D then take (R U)[m][i] from lane i the same
+// way. The products and sums are the textbook ones in the same order (sum over k, then over m, by FMAs).
+// Loops are unrolled to the largest order with the entries beyond q masked out, so no array goes to
+// local memory.
 __device__ inline void change_D(double* D, int N, int q, double factor, int lane) {
-    double R[kMaxOrder + 1][kMaxOrder + 1], U[kMaxOrder + 1][kMaxOrder + 1];
-    for (int j = 0; j <= q; j++) {
-        R[0][j] = 1.0;
-        U[0][j] = 1.0;
+    const int j = lane;
+    double Rc[kMaxOrder + 1], Uc[kMaxOrder + 1], RUc[kMaxOrder + 1];
+    Rc[0] = 1.0;
+    Uc[0] = 1.0;
+#pragma unroll
+    for (int i = 1; i <= kMaxOrder; i++) {
+        const double mr = j == 0 ? 0.0 : ((double)(i - 1) - factor * j) * kRcpInt[i];
+        const double mu = j == 0 ? 0.0 : ((double)(i - 1) - (double)j) * kRcpInt[i];
+        Rc[i] = Rc[i - 1] * mr;
+        Uc[i] = Uc[i - 1] * mu;
     }
-    for (int i = 1; i <= q; i++)
-        for (int j = 0; j <= q; j++) {
-            const double mr = j == 0 ? 0.0 : ((double)(i - 1) - factor * j) * kRcpInt[i];
-            const double mu = j == 0 ? 0.0 : ((double)(i - 1) - (double)j) * kRcpInt[i];
-            R[i][j] = R[i - 1][j] * mr;
-            U[i][j] = U[i - 1][j] * mu;
+#pragma unroll
+    for (int i = 0; i <= kMaxOrder; i++) {  // lane j: (R U)[i][j] = sum_k R[i][k] U[k][j]
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k <= kMaxOrder; k++) {
+            const double rik = __shfl_sync(0xffffffffu, Rc[i], k);
+            if (k <= q) s = fma(rik, Uc[k], s);
         }
-    double RU[kMaxOrder + 1][kMaxOrder + 1];
-    for (int i = 0; i <= q; i++)
-        for (int j = 0; j <= q; j++) {
-            double s = 0.0;
-            for (int k = 0; k <= q; k++) s = fma(R[i][k], U[k][j], s);
-            RU[i][j] = s;
-        }
-    for (int col = lane; col < N; col += 32) {
+        RUc[i] = s;
+    }
+    for (int c0 = 0; c0 < N; c0 += 32) {  // warp-uniform loop: the shuffles need every lane
+        const int col = c0 + lane;
+        const bool in = col < N;
         double old[kMaxOrder + 1];
-        for (int m = 0; m <= q; m++) old[m] = D[(size_t)m * N + col];
-        for (int i = 0; i <= q; i++) {
+#pragma unroll
+        for (int m = 0; m <= kMaxOrder; m++) old[m] = (in && m <= q) ? D[(size_t)m * N + col] : 0.0;
+#pragma unroll
+        for (int i = 0; i <= kMaxOrder; i++) {
             double s = 0.0;
-            for (int m = 0; m <= q; m++) s = fma(RU[m][i], old[m], s);
-            D[(size_t)i * N + col] = s;
+#pragma unroll
+            for (int m = 0; m <= kMaxOrder; m++) {
+                const double rum = __shfl_sync(0xffffffffu, RUc[m], i);  // (R U)[m][i]
+                if (m <= q) s = fma(rum, old[m], s);
+            }
+            if (in && i <= q) D[(size_t)i * N + col] = s;
         }
     }
     __syncwarp();
@@ -1296,10 +1311,17 @@ __global__ void __launch_bounds__(256, 2) slice_kernel_global_wide(const Params 
     slice_body<MIXED, true>(p);
 }
 
+// And with three (80 registers a thread).
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 3) slice_kernel_global_mid(const Params p) {
+    slice_body<MIXED, true>(p);
+}
+
 using SliceFn = void (*)(Params);
 SliceFn slice_kernel_fn(bool mixed);              // bdf_slice.cu: workspaces in shared memory
 SliceFn slice_kernel_global_fn(bool mixed);       // bdf_slice_global.cu: workspaces in global memory
 SliceFn slice_kernel_global_wide_fn(bool mixed);  // bdf_slice_global_wide.cu: the same, 128 registers
+SliceFn slice_kernel_global_mid_fn(bool mixed);   // bdf_slice_global_mid.cu: the same, 80 registers
 
 }  // namespace bdf
 }  // namespace cbg

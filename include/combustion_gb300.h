@@ -337,7 +337,7 @@ typedef struct cb_reactor_stats {
     double ms;                  /* device time of the integration */
     int32_t warps_per_block, tables_in_shared, graph_replays, slices;
     int32_t global_memory;       /* workspaces in global (1) or shared (0) memory */
-    int32_t register_cap;        /* global memory: the kernel's registers a thread, 64 or 128 */
+    int32_t register_cap;        /* global memory: the kernel's registers a thread, 64, 80 or 128 */
 } cb_reactor_stats;
 typedef struct cb_reactor_tuning {
     int32_t warps_per_block, tables_in_shared, n_candidates, calib_reactors;
