@@ -408,6 +408,21 @@ def run_large(args, with_learned):
 
     plain_ms = timed(lambda: mech.rates_transport(cells, r_out, t_out), 2)
     mixed_ms = timed(lambda: mech.rates_transport(cells, m_r, m_t, mixed=True), 3)
+    # the two plain kernels apart (transport on its own inputs) and their FP64 roofline
+    t_in = torch.empty((K + 1, n), dtype=torch.float64, device="cuda")
+    t_in[0] = (cells[0] * cells[3]) / cells[2]
+    t_in[1] = cells[2] / scales[0]
+    t_in[2:] = cells[4:]
+    t_chk = torch.empty_like(t_out)
+    rates_ms = timed(lambda: mech.rates(cells, r_out), 2)
+    transport_ms = timed(lambda: mech.transport(t_in, t_chk), 2)
+    del t_in, t_chk
+    work_r, work_t = mech.work_model()
+    peak = 2.0 * cb.device_fp64_peak() / 1e12
+    kernel_roofline = {name: {"ms": ms_k, "achieved": algorithmic_flops(w) * n / (ms_k * 1e-3) / 1e12,
+                              "frac": algorithmic_flops(w) * n / (ms_k * 1e-3) / 1e12 / peak,
+                              "flops_per_cell": algorithmic_flops(w)}
+                       for name, ms_k, w in (("rates_f64", rates_ms, work_r), ("transport_f64", transport_ms, work_t))}
     o = oracle.Oracle(m)
     o.set_transport(*scales, *mech.transport_coefficients())
     idx = torch.arange(0, n, n // 256, device="cuda")
@@ -430,6 +445,7 @@ def run_large(args, with_learned):
                       "max_err": max(cerr(r_out, rref, rsc), cerr(t_out, tref, tsc)),
                       "error": {"rates": error_block(sample(r_out), rref, rsc, RATES_GROUPS),
                                 "transport": error_block(sample(t_out), tref, tsc, TRANSPORT_GROUPS)},
+                      "kernels": kernel_roofline,
                       "api": "cb_rates_transport_f64 (tables read through L1: KMAX 256)"},
         "mixed": {"cells_per_s": n / (mixed_ms * 1e-3), "ms": mixed_ms,
                   "rates_max_err": cerr(m_r, rref, rsc), "transport_max_err": cerr(m_t, tref, tsc),
