@@ -41,7 +41,7 @@ namespace cbg {
 namespace bdf {
 
 // Evaluation hook: f and J at given states, one warp per state.
-__global__ void eval_kernel(const Params p, int count) {
+__global__ void eval_kernel(const __grid_constant__ Params p, int count) {
     const uint8_t* tab = p.tab;
     __shared__ uint64_t bar;
     if (p.smem_tables) {

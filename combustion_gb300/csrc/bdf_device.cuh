@@ -105,7 +105,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // trajectory points in (t_new - h, t_new] from the interpolating polynomial through the last q + 1
 // points (Newton's backward-difference form, y(t) = sum_j D_j prod_{m<j} (t - t_new + m h) / ((m+1) h),
 // the dense output of the BDF method), and the peak of the chosen species' mole fraction.
-__device__ inline void record_outputs(const Params& p, Head& hd, int r, const double* D, double t_new, double h, int q,
+static __device__ __noinline__ void record_outputs(const Params& p, Head& hd, int r, const double* D, double t_new, double h, int q,
                                int lane) {
     const int N = p.N;
     if (p.traj) {
@@ -284,7 +284,7 @@ __device__ __forceinline__ void rates_group_warp(const Mech& m, const Work& w, c
 
 // du/dt of the reactor: the outputs of reaction.rs:356-391 at state y = [T, V, n_0 .. n_{A-1}].
 template <bool PARTS>
-__device__ inline RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
+__device__ __noinline__ RhsOut rhs_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
                            double* f, int lane) {
     const RatesHeader& H = *m.tb.H;
     const int K = p.K, A = p.A;
@@ -394,7 +394,7 @@ __device__ __forceinline__ void rates_group_warp_m(const RatesMixedTables& tm, c
 // warp-cooperative as rhs_warp): FP64 concentrations, Gibbs polynomials and exponentials, rates of
 // progress, accumulation and energy sums; FP32 Arrhenius terms, third-body sums, falloff blending and
 // h/RT, cp/R polynomials. w.M holds the FP32 third-body sums.
-__device__ inline void rhs_warp_mixed(const Params& p, const Mech& m, const RatesMixedTables& tm, const Work& w, double pR,
+static __device__ __noinline__ void rhs_warp_mixed(const Params& p, const Mech& m, const RatesMixedTables& tm, const Work& w, double pR,
                                double rP, const double* y, double* f, int lane) {
     const RatesMixedHeader& H = *tm.H;
     const int K = p.K, A = p.A;
@@ -481,7 +481,7 @@ __device__ __forceinline__ double deriv_product(const double* C, const uint16_t*
 }
 
 // Jacobian of du/dt at y into Jm (N rows of LD), also stored to Jg [N][N]; w.f receives f(y).
-__device__ inline void jacobian_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
+static __device__ __noinline__ void jacobian_warp(const Params& p, const Mech& m, const Work& w, double pR, double rP, const double* y,
                               double* Jg, double* Jm, int lane) {
     const int K = p.K, A = p.A, N = p.N, LD = p.LD;
     const RhsOut o = rhs_warp<true>(p, m, w, pR, rP, y, w.f, lane);
@@ -871,7 +871,7 @@ __device__ inline void lu_solve_t_warp(const T* At, int N, int LD, const int* pe
 // solves. With CB_BDF_LU32 (GLOBAL only) the factors are FP32 and both they and their transpose live in
 // LUt's bytes (LU stays the FP64 Jacobian scratch).
 template <bool GLOBAL>
-__device__ inline bool build_lu(const Params& p, double* LU, int* piv, double* rdiag, const double* Jg, double c, bool fresh,
+__device__ __noinline__ bool build_lu(const Params& p, double* LU, int* piv, double* rdiag, const double* Jg, double c, bool fresh,
                          double* LUt, int lane) {
     const int N = p.N, LD = p.LD;
     for (int idx = lane; idx < N * N; idx += 32) {
@@ -916,7 +916,7 @@ __device__ __forceinline__ double rms_scaled(const double* x, const double* rsca
 // way. The products and sums are the textbook ones in the same order (sum over k, then over m, by FMAs).
 // Loops are unrolled to the largest order with the entries beyond q masked out, so no array goes to
 // local memory.
-__device__ inline void change_D(double* D, int N, int q, double factor, int lane) {
+static __device__ __noinline__ void change_D(double* D, int N, int q, double factor, int lane) {
     const int j = lane;
     double Rc[kMaxOrder + 1], Uc[kMaxOrder + 1], RUc[kMaxOrder + 1];
     Rc[0] = 1.0;
@@ -1293,7 +1293,7 @@ __device__ __forceinline__ void slice_body(const Params& p) {
 }
 
 template <bool MIXED>
-__global__ void slice_kernel(const Params p) {
+__global__ void slice_kernel(const __grid_constant__ Params p) {
     slice_body<MIXED, false>(p);
 }
 
@@ -1301,19 +1301,19 @@ __global__ void slice_kernel(const Params p) {
 // latency of workspaces that live in L2 and HBM (measured at 250 species, 4096 reactors: 17.3 s against
 // 20.6 s with two blocks and 20.0 s with three).
 template <bool MIXED>
-__global__ void __launch_bounds__(256, 4) slice_kernel_global(const Params p) {
+__global__ void __launch_bounds__(256, 4) slice_kernel_global(const __grid_constant__ Params p) {
     slice_body<MIXED, true>(p);
 }
 
 // The same with two blocks per SM (128 registers a thread, fewer spills, half the warps).
 template <bool MIXED>
-__global__ void __launch_bounds__(256, 2) slice_kernel_global_wide(const Params p) {
+__global__ void __launch_bounds__(256, 2) slice_kernel_global_wide(const __grid_constant__ Params p) {
     slice_body<MIXED, true>(p);
 }
 
 // And with three (80 registers a thread).
 template <bool MIXED>
-__global__ void __launch_bounds__(256, 3) slice_kernel_global_mid(const Params p) {
+__global__ void __launch_bounds__(256, 3) slice_kernel_global_mid(const __grid_constant__ Params p) {
     slice_body<MIXED, true>(p);
 }
 

@@ -1065,6 +1065,11 @@ int cb_surrogate_transport_pair(cb_surrogate* a, cb_surrogate* b, size_t n, cons
     SUR_RC(ensure_inference(b, kInferChunk));
     const double T0 = cbi::view(a->mech).T0;
     const uint32_t audit_stride = gate->audit_stride;
+    // Networks trained on the same cell distribution share their input normalisation: the features are
+    // then computed once and both networks read them.
+    const bool same_inputs =
+        a->n_in == b->n_in && a->h_norm.size() == b->h_norm.size() &&
+        std::memcmp(a->h_norm.data(), b->h_norm.data(), 2 * (size_t)a->n_out * sizeof(float)) == 0;
     const size_t audit_cap = audit_stride ? n / audit_stride + 1 : 0;
     // every cell may fall back; the lists and per-cell arrays live in the first network's object
     if (n > a->fail_cap) {
@@ -1123,6 +1128,7 @@ int cb_surrogate_transport_pair(cb_surrogate* a, cb_surrogate* b, size_t n, cons
         const int rows = (int)((len + kBM - 1) / kBM * kBM);
         SUR_CUDA(mark(0));
         for (cb_surrogate* s : {a, b}) {  // each network's own normalisation of the same cells
+            if (s == b && same_inputs) break;
             FeatureArgs f;
             std::memset(&f, 0, sizeof f);
             for (int q = 0; q < K + 3; q++) f.in[q] = (uniform && q < 2) ? inputs[q] : inputs[q] + lo;
@@ -1147,7 +1153,7 @@ int cb_surrogate_transport_pair(cb_surrogate* a, cb_surrogate* b, size_t n, cons
         }
         SUR_CUDA(mark(1));
         SUR_RC(infer_rows(a, rows, a->mXi, st));
-        SUR_RC(infer_rows(b, rows, b->mXi, st));
+        SUR_RC(infer_rows(b, rows, same_inputs ? a->mXi : b->mXi, st));
         SUR_CUDA(mark(2));
         CombineArgs c;
         std::memset(&c, 0, sizeof c);
