@@ -265,3 +265,33 @@ def test_ensemble_gate_calibrated_bound():
             assert torch.equal(res, reference(test, True))
         else:
             assert 0.0 < frac < 1.0
+
+
+def test_ensemble_rejects_bad_arguments():
+    """cb_surrogate_transport_pair refuses one network twice, networks of two mechanisms, a NaN
+    threshold and an unknown fallback kernel, with CB_ERR_INVALID and a message; nothing is launched."""
+    import ctypes as C
+    import torch
+    import combustion_gb300 as cb
+    from combustion_gb300 import surrogate as S
+    mech = _mech("k10")
+    a = S.Surrogate(mech, width=256, hidden_layers=2, batch=1024, seed=3)
+    a.generate(1 << 12, S.distribution("k10", seed=2))
+    b = S.Surrogate(mech, width=256, hidden_layers=2, batch=1024, seed=4)
+    b.generate(1 << 12, S.distribution("k10", seed=2))
+    other = S.Surrogate(_mech("k10"), width=256, hidden_layers=2, batch=1024, seed=5)
+    other.generate(1 << 12, S.distribution("k10", seed=2))
+    cells = S.generate_cells(mech, 256, S.distribution("k10", seed=7))
+    out = torch.zeros((mech.K + 2, 256), dtype=torch.float64, device="cuda")
+    for x, y, thr, fb in ((a, a, 1.0, "mixed"), (a, other, 1.0, "mixed"), (a, b, float("nan"), "mixed")):
+        with pytest.raises(cb.CombustionError) as e:
+            S.transport_pair(x, y, cells, out, thr, fallback=fb)
+        assert e.value.code == cb.CB_ERR_INVALID, str(e.value)
+    L = S._bind()
+    ins, _ = cb.Mechanism._rows(cells)
+    outs, n = cb.Mechanism._rows(out)
+    g = S.cb_surrogate_gate(1.0, 0, 7, None)  # no such fallback kernel
+    rc = L.cb_surrogate_transport_pair(a.h, b.h, n, cb._ptr_array(ins), cb._ptr_array(outs), 0, C.byref(g), None,
+                                       None)
+    assert rc == cb.CB_ERR_INVALID and b"fallback" in L.cb_last_error()
+    assert bool((out == 0).all())
