@@ -114,22 +114,24 @@ struct cb_surrogate {
     bool have_norm = false;
     // training set
     size_t n_train = 0;
-    bf16 *X = nullptr, *XT = nullptr;
+    bf16* X = nullptr;
     float* Y = nullptr;
-    CUtensorMap mX, mXT;
+    CUtensorMap mX, mX_K;  // A operand of the first layer (128-row boxes); MN-major B of its weight gradient
     // per-step buffers (batch rows)
-    bf16 *Z[kMaxLayers] = {}, *Act[kMaxLayers] = {}, *ActT[kMaxLayers] = {};
-    bf16 *dY = nullptr, *dYT = nullptr, *dZ[2] = {}, *dZT[2] = {};
-    CUtensorMap mAct_A[kMaxLayers], mActT_B[kMaxLayers], mActT_A, mdYT_B, mdY_A, mdZT_A[2], mdZ_A[2];
-    CUtensorMap mZ_S[kMaxLayers], mAct_S[kMaxLayers], mdZ_S[2];  // TMA store maps (32-row boxes) of the epilogues
+    bf16 *Sd[kMaxLayers] = {}, *Act[kMaxLayers] = {};  // silu'(Z_l) (backward) and silu(Z_l) of each hidden layer
+    bf16 *dY = nullptr, *dZ[2] = {};
+    CUtensorMap mAct_A[kMaxLayers], mdY_A, mdZ_A[2];         // K-major A operands (128-row boxes)
+    CUtensorMap mAct_K[kMaxLayers], mdY_K, mdZ_K[2];         // MN-major weight-gradient operands (64-row boxes)
+    CUtensorMap mSd_S[kMaxLayers], mAct_S[kMaxLayers], mdZ_S[2];  // TMA maps (32-row boxes) of the epilogues
+    float* colsum = nullptr;  // column sums of the output gradient dY per 32 rows [batch / 32][n_out]
     float* ws = nullptr;
     float* loss_part = nullptr;
     float* losses = nullptr;  // mean squared error of every step since the parameters were set
     int* counters = nullptr;  // [0] step, [1] batch row offset
     // evaluation scratch (rows <= batch)
-    bf16 *Xs = nullptr, *XTs = nullptr;
+    bf16* Xs = nullptr;
     float* Ys = nullptr;
-    CUtensorMap mXs, mXTs;
+    CUtensorMap mXs, mXs_K;
     // inference buffers
     bf16 *Xi = nullptr, *Hi[2] = {};
     float* Yi = nullptr;
@@ -184,8 +186,10 @@ int wgrad_splits(int M, int N, int BN, int k_blocks) {
     return std::min(s, k_blocks);
 }
 
-// Forward (and, with `backward`, backward + optional Adam) over `rows` rows.
-int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap& mXT, const float* Y, bool dyn,
+// Forward (and, with `backward`, backward + optional Adam) over `rows` rows. mX: the first layer's input
+// with 128-row boxes (A operand), mX_K: the same matrix with 64-row boxes (MN-major B operand of the first
+// layer's weight gradient).
+int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap& mX_K, const float* Y, bool dyn,
              bool backward, bool update, int total_steps, cudaStream_t st) {
     const int L = s->L;
     // forward
@@ -202,12 +206,10 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         int epi;
         if (l < L - 1) {
             epi = kEpiHidden;
-            p.out = backward ? s->Z[l] : nullptr;
+            p.out = backward ? s->Sd[l] : nullptr;
             p.ld_out = s->width;
             p.out2 = s->Act[l];
             p.ld_out2 = s->width;
-            p.outT = backward ? s->ActT[l] : nullptr;
-            p.ld_outT = s->batch;
         } else if (backward) {
             epi = kEpiLoss;
             p.target = Y;
@@ -216,8 +218,8 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
             p.grad_scale = 2.0f / ((float)rows * (float)s->n_feat);
             p.out = s->dY;
             p.ld_out = s->n_out;
-            p.outT = s->dYT;
-            p.ld_outT = s->batch;
+            p.colsum = s->colsum;
+            p.ld_colsum = s->n_out;
             p.loss = s->loss_part;
             if (dyn) {
                 p.row0 = s->counters + 1;
@@ -230,28 +232,31 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         }
         const CUtensorMap& a = l == 0 ? mX : s->mAct_A[l - 1];
         if (epi == kEpiHidden)
-            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st, backward ? &s->mZ_S[l] : nullptr, &s->mAct_S[l]));
+            SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st, backward ? &s->mSd_S[l] : nullptr, &s->mAct_S[l]));
         else
             SUR_CUDA(gemm(bn_for(p.N), epi, a, s->mW[l], p, st));
     }
     if (!backward) return CB_OK;
     for (int l = L - 1; l >= 0; l--) {
-        // weight gradient (split K over the rows), reduced in a fixed order
+        // weight gradient (split K over the rows, operands MN-major from the row-major activations) and,
+        // for the hidden layers, the bias gradient (row sums of dZ_l^T by the tensor core), reduced in a
+        // fixed order
         GemmParams p = base_params(s);
         const CUtensorMap *ma, *mb;
         bool transpose;
         if (l == L - 1) {  // W_L^T = A_{L-1}^T dY: M = width, N = n_out
             p.M = s->dims[l];
             p.N = s->dims[l + 1];
-            ma = &s->mActT_A;
-            mb = &s->mdYT_B;
+            ma = &s->mAct_K[l - 1];
+            mb = &s->mdY_K;
             transpose = true;
         } else {  // W_l = dZ_l^T A_{l-1}: M = dims[l+1], N = dims[l]
             p.M = s->dims[l + 1];
             p.N = s->dims[l];
-            ma = &s->mdZT_A[l % 2];
-            mb = l == 0 ? &mXT : &s->mActT_B[l - 1];
+            ma = &s->mdZ_K[l % 2];
+            mb = l == 0 ? &mX_K : &s->mAct_K[l - 1];
             transpose = false;
+            p.bias_part = 1;
             if (l == 0 && dyn) {
                 p.row0 = s->counters + 1;
                 p.dyn = kDynBx;
@@ -262,24 +267,32 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         p.splits = wgrad_splits(p.M, p.N, BN, p.k_blocks);
         p.outf = s->ws;
         p.ld_outf = p.N;
+        const int nb = p.bias_part ? p.M : 0;
+        p.split_stride = (long long)p.M * p.N + nb;
         SUR_CUDA(gemm(BN, kEpiPartial, *ma, *mb, p, st));
-        SUR_CUDA(reduce_partials(s->ws, p.splits, p.M, p.N, transpose, s->g + s->w_off[l], st));
-        SUR_CUDA(row_sums(l == L - 1 ? s->dYT : s->dZT[l % 2], s->dims[l + 1], rows, s->batch, s->g + s->b_off[l], st));
+        SUR_CUDA(reduce_partials(s->ws, p.splits, p.split_stride, p.M, p.N, transpose, s->g + s->w_off[l], nb,
+                                 s->g + s->b_off[l], st));
         if (l == 0) break;
         // data gradient through W_l, times silu'(Z_{l-1})
         GemmParams q = base_params(s);
         q.M = rows;
         q.N = s->dims[l];
         q.k_blocks = s->dims[l + 1] / kBK;
-        q.zin = s->Z[l - 1];
-        q.ld_zin = s->width;
         q.out = s->dZ[(l - 1) % 2];
         q.ld_out = s->width;
-        q.outT = s->dZT[(l - 1) % 2];
-        q.ld_outT = s->batch;
         const CUtensorMap& a = l == L - 1 ? s->mdY_A : s->mdZ_A[l % 2];
-        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mWT[l], q, st, &s->mdZ_S[(l - 1) % 2], nullptr));
+        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mWT[l], q, st, &s->mdZ_S[(l - 1) % 2], nullptr, &s->mSd_S[l - 1]));
     }
+    // the output layer's bias gradient from the loss epilogue's column sums
+    ColumnReduceArgs cr;
+    std::memset(&cr, 0, sizeof cr);
+    cr.n_layers = 1;
+    cr.groups = rows / 32;
+    cr.part[0] = s->colsum;
+    cr.cols[0] = s->n_out;
+    cr.out[0] = s->g + s->b_off[L - 1];
+    cr.block0[1] = s->n_out / 32;
+    SUR_CUDA(column_reduce(cr, st));
     if (update) {
         SUR_CUDA(adam(adam_args(s, total_steps), st));
         const int n_batches = (int)(s->n_train / s->batch);
@@ -290,18 +303,18 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
 }
 
 int free_all(cb_surrogate* s) {
-    void* ptrs[] = {s->p, s->g, s->m1, s->m2, s->norm, s->X, s->XT, s->Y, s->dY, s->dYT, s->dZ[0], s->dZ[1],
-                    s->dZT[0], s->dZT[1], s->ws, s->loss_part, s->losses, s->counters, s->Xs, s->XTs, s->Ys, s->Xi, s->Hi[0],
+    void* ptrs[] = {s->p, s->g, s->m1, s->m2, s->norm, s->X, s->Y, s->dY, s->dZ[0], s->dZ[1],
+                    s->ws, s->loss_part, s->losses, s->counters, s->Xs, s->Ys, s->Xi, s->Hi[0],
                     s->Hi[1], s->Yi, s->fail_idx, s->audit_idx, s->gate_count, s->audit_plain, s->err_max,
                     s->err_sq, s->status, s->outside, s->disagreement};
     for (void* q : ptrs) cudaFree(q);
     for (int l = 0; l < kMaxLayers; l++) {
         cudaFree(s->W[l]);
         cudaFree(s->WT[l]);
-        cudaFree(s->Z[l]);
+        cudaFree(s->Sd[l]);
         cudaFree(s->Act[l]);
-        cudaFree(s->ActT[l]);
     }
+    cudaFree(s->colsum);
     if (s->stream) cudaStreamDestroy(s->stream);
     return CB_OK;
 }
@@ -480,28 +493,23 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
         rc = rc ? rc : dalloc(&s->WT[l], (size_t)s->dims[l] * s->dims[l + 1]);
     }
     for (int l = 0; l < s->hidden && !rc; l++) {
-        rc = dalloc(&s->Z[l], B * Wd);
+        rc = dalloc(&s->Sd[l], B * Wd);
         rc = rc ? rc : dalloc(&s->Act[l], B * Wd);
-        rc = rc ? rc : dalloc(&s->ActT[l], B * Wd);
     }
+    rc = rc ? rc : dalloc(&s->colsum, B / 32 * s->n_out);
     rc = rc ? rc : dalloc(&s->dY, B * s->n_out);
-    rc = rc ? rc : dalloc(&s->dYT, B * s->n_out);
-    for (int h = 0; h < 2 && !rc; h++) {
-        rc = dalloc(&s->dZ[h], B * Wd);
-        rc = rc ? rc : dalloc(&s->dZT[h], B * Wd);
-    }
+    for (int h = 0; h < 2 && !rc; h++) rc = dalloc(&s->dZ[h], B * Wd);
     // weight-gradient partials: the largest splits x M x N of any layer
     size_t ws = 0;
     for (int l = 0; l < s->L; l++) {
         const int M = l == s->L - 1 ? s->dims[l] : s->dims[l + 1], N = l == s->L - 1 ? s->dims[l + 1] : s->dims[l];
-        ws = std::max(ws, (size_t)wgrad_splits(M, N, bn_for(N), s->batch / kBK) * M * N);
+        ws = std::max(ws, (size_t)wgrad_splits(M, N, bn_for(N), s->batch / kBK) * (M * N + M));
     }
     rc = rc ? rc : dalloc(&s->ws, ws);
     rc = rc ? rc : dalloc(&s->losses, kMaxSteps);
     rc = rc ? rc : dalloc(&s->loss_part, kEpiWarps * B / kBM);
     rc = rc ? rc : dalloc(&s->counters, 2);
     rc = rc ? rc : dalloc(&s->Xs, B * s->n_in);
-    rc = rc ? rc : dalloc(&s->XTs, B * s->n_in);
     rc = rc ? rc : dalloc(&s->Ys, B * s->n_out);
     rc = rc ? rc : dalloc(&s->status, 1);
     if (rc) return fail_free(rc);
@@ -513,20 +521,19 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     }
     for (int l = 0; l < s->hidden && !rc; l++) {
         rc = make_map(&s->mAct_A[l], s->Act[l], Wd, B, kBM);
-        rc = rc ? rc : make_map(&s->mActT_B[l], s->ActT[l], B, Wd, bn_for((int)Wd));
-        rc = rc ? rc : make_map(&s->mZ_S[l], s->Z[l], Wd, B, 32);
+        rc = rc ? rc : make_map(&s->mAct_K[l], s->Act[l], Wd, B, kBK);
+        rc = rc ? rc : make_map(&s->mSd_S[l], s->Sd[l], Wd, B, 32);
         rc = rc ? rc : make_map(&s->mAct_S[l], s->Act[l], Wd, B, 32);
     }
-    rc = rc ? rc : make_map(&s->mActT_A, s->ActT[s->hidden - 1], B, Wd, kBM);
-    rc = rc ? rc : make_map(&s->mdYT_B, s->dYT, B, s->n_out, bn_for(s->n_out));
     rc = rc ? rc : make_map(&s->mdY_A, s->dY, s->n_out, B, kBM);
+    rc = rc ? rc : make_map(&s->mdY_K, s->dY, s->n_out, B, kBK);
     for (int h = 0; h < 2 && !rc; h++) {
-        rc = make_map(&s->mdZT_A[h], s->dZT[h], B, Wd, kBM);
-        rc = rc ? rc : make_map(&s->mdZ_A[h], s->dZ[h], Wd, B, kBM);
+        rc = make_map(&s->mdZ_A[h], s->dZ[h], Wd, B, kBM);
+        rc = rc ? rc : make_map(&s->mdZ_K[h], s->dZ[h], Wd, B, kBK);
         rc = rc ? rc : make_map(&s->mdZ_S[h], s->dZ[h], Wd, B, 32);
     }
     rc = rc ? rc : make_map(&s->mXs, s->Xs, s->n_in, B, kBM);
-    rc = rc ? rc : make_map(&s->mXTs, s->XTs, B, s->n_in, bn_for(s->n_in));
+    rc = rc ? rc : make_map(&s->mXs_K, s->Xs, s->n_in, B, kBK);
     if (rc) return fail_free(rc);
     // He-uniform weights over the real fan-in, zero biases; padding rows / columns stay zero.
     std::vector<float> h(s->n_params, 0.f);
@@ -620,16 +627,14 @@ int cb_surrogate_generate(cb_surrogate* s, size_t n_train, const cb_cell_distrib
     cudaStream_t st = s->stream;
     SUR_CUDA(cudaStreamSynchronize(st));
     cudaFree(s->X);
-    cudaFree(s->XT);
     cudaFree(s->Y);
-    s->X = s->XT = nullptr;
+    s->X = nullptr;
     s->Y = nullptr;
     s->n_train = 0;
     SUR_RC(dalloc(&s->X, n_train * s->n_in));
-    SUR_RC(dalloc(&s->XT, n_train * s->n_in));
     SUR_RC(dalloc(&s->Y, n_train * s->n_out));
     SUR_RC(make_map(&s->mX, s->X, s->n_in, n_train, kBM));
-    SUR_RC(make_map(&s->mXT, s->XT, n_train, s->n_in, bn_for(s->n_in)));
+    SUR_RC(make_map(&s->mX_K, s->X, s->n_in, n_train, kBK));
     const int K = s->K, nf = s->n_feat;
     const size_t C = std::min(n_train, (size_t)1 << 20);
     double* cells = nullptr;
@@ -738,8 +743,6 @@ int cb_surrogate_generate(cb_surrogate* s, size_t n_train, const cb_cell_distrib
         f.rstd = nrm(s, kInRstd);
         f.X = s->X;
         f.row0 = lo;
-        f.XT = s->XT;
-        f.ldXT = n_train;
         f.hull_lo = hull;
         f.hull_hi = hull + nf;
         TargetArgs t;
@@ -793,7 +796,7 @@ int cb_surrogate_train(cb_surrogate* s, int32_t steps, float* losses) {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     SUR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    int rc = run_pass(s, s->batch, s->mX, s->mXT, s->Y, true, true, true, (int)(s->steps_done + steps), st);
+    int rc = run_pass(s, s->batch, s->mX, s->mX_K, s->Y, true, true, true, (int)(s->steps_done + steps), st);
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (rc) {
         if (graph) cudaGraphDestroy(graph);
@@ -823,17 +826,11 @@ int cb_surrogate_evaluate(cb_surrogate* s, int32_t rows, const float* features_h
     SUR_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = s->stream;
     const int n_in = s->n_in, n_out = s->n_out;
-    std::vector<bf16> xb((size_t)rows * n_in), xt((size_t)n_in * s->batch, __float2bfloat16(0.f));
-    for (int r = 0; r < rows; r++)
-        for (int j = 0; j < n_in; j++) {
-            const bf16 b = __float2bfloat16(features_h[(size_t)r * n_in + j]);
-            xb[(size_t)r * n_in + j] = b;
-            xt[(size_t)j * s->batch + r] = b;
-        }
+    std::vector<bf16> xb((size_t)rows * n_in);
+    for (size_t e = 0; e < xb.size(); e++) xb[e] = __float2bfloat16(features_h[e]);
     SUR_CUDA(cudaMemcpyAsync(s->Xs, xb.data(), xb.size() * sizeof(bf16), cudaMemcpyHostToDevice, st));
-    SUR_CUDA(cudaMemcpyAsync(s->XTs, xt.data(), xt.size() * sizeof(bf16), cudaMemcpyHostToDevice, st));
     SUR_CUDA(cudaMemcpyAsync(s->Ys, targets_h, (size_t)rows * n_out * sizeof(float), cudaMemcpyHostToDevice, st));
-    SUR_RC(run_pass(s, rows, s->mXs, s->mXTs, s->Ys, false, true, false, 1, st));
+    SUR_RC(run_pass(s, rows, s->mXs, s->mXs_K, s->Ys, false, true, false, 1, st));
     std::vector<float> lp(kEpiWarps * rows / kBM);
     SUR_CUDA(cudaMemcpyAsync(lp.data(), s->loss_part, lp.size() * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (grads) SUR_CUDA(cudaMemcpyAsync(grads, s->g, s->n_params * sizeof(float), cudaMemcpyDeviceToHost, st));

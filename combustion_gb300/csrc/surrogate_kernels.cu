@@ -27,10 +27,16 @@ __device__ __forceinline__ float tanh_approx(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float sigmoidf_(float z) { return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f); }
 __device__ __forceinline__ float siluf_(float z) {
     const float h = 0.5f * z;
     return fmaf(h, tanh_approx(h), h);
+}
+// silu(z) and silu'(z) from one tanh: with h = z / 2 and t = tanh(h), sigmoid(z) = (1 + t) / 2, so
+// silu(z) = h (1 + t) and silu'(z) = sigmoid(z) (1 + z (1 - sigmoid(z))) = (1 + t + h (1 - t^2)) / 2.
+__device__ __forceinline__ void silu_and_derivative(float z, float& s, float& d) {
+    const float h = 0.5f * z, t = tanh_approx(h);
+    s = fmaf(h, t, h);
+    d = fmaf(0.5f, fmaf(h, fmaf(-t, t, 1.f), t), 0.5f);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -47,23 +53,36 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* base, int ld, int 
                             pack_bf16(a[8 * j + 4], a[8 * j + 5]), pack_bf16(a[8 * j + 6], a[8 * j + 7]));
 }
 
-// The same values into the transposed matrix (rows row0 .. row0 + 31 of the warp, one per lane),
-// staged through the warp's 2 KB of shared memory: the 32 x 32 chunk is written column by column (lane
-// = row, 64 contiguous bytes per column), then each lane stores 16 bytes (8 rows of one column), eight
-// columns per instruction; each column is a 64-byte run of the transposed matrix's row. Four global
-// stores per chunk instead of 32 two-byte ones.
-__device__ __forceinline__ void store_col_bf16(__nv_bfloat16* base, int ld, int row0, int n, int lane,
-                                               const float* a, __nv_bfloat16* stage) {
+// Column sums of a warp's 32 x 32 chunk (lane = row, a[j] = column j): returns to lane j the sum of
+// column j over the 32 rows. Five exchange rounds halve the columns each lane carries (16 + 8 + 4 + 2 + 1
+// shuffles); the order of the additions is fixed.
+__device__ __forceinline__ float column_sums32(const float* a, int lane) {
+    float b[16];
+    {
+        const bool up = lane & 16;
 #pragma unroll
-    for (int j = 0; j < 32; j++) stage[j * 32 + lane] = __float2bfloat16_rn(a[j]);
-    __syncwarp();
-    const uint4* s4 = reinterpret_cast<const uint4*>(stage);
-#pragma unroll
-    for (int it = 0; it < 4; it++) {
-        const int j = it * 8 + (lane >> 2), piece = lane & 3;
-        *reinterpret_cast<uint4*>(base + (size_t)(n + j) * ld + row0 + piece * 8) = s4[j * 4 + piece];
+        for (int j = 0; j < 16; j++) {
+            const float keep = up ? a[j + 16] : a[j], send = up ? a[j] : a[j + 16];
+            b[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+        }
     }
-    __syncwarp();  // the next chunk rewrites the stage
+#pragma unroll
+    for (int w = 8; w >= 1; w >>= 1) {
+        const bool up = lane & w;
+#pragma unroll
+        for (int j = 0; j < w; j++) {
+            const float keep = up ? b[j + w] : b[j], send = up ? b[j] : b[j + w];
+            b[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+        }
+    }
+    return b[0];
+}
+
+// Rounds to the nearest BF16 value in place (the value that is stored), so that sums over the stored
+// matrix are formed from the same numbers.
+__device__ __forceinline__ void round_bf16(float* a) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) a[j] = __bfloat162float(__float2bfloat16_rn(a[j]));
 }
 
 // Row r (this lane) of a 32 x 64 BF16 box in the 128-byte swizzle of its TMA store map: columns
@@ -79,20 +98,40 @@ __device__ __forceinline__ void stage_row_half(uint8_t* box, int r, int half, co
     }
 }
 
+// SiLU-derivative tiles of the data-gradient epilogue: one 32-row x 64-column box per warp, loaded by TMA
+// into the warp's second box one 64-column pair ahead of its use (the first pair of an item while the
+// item's MMAs run), completing on the warp's mbarrier.
+struct DLoad {
+    uint32_t bar, phase;
+    bool pending;
+};
+
+__device__ __forceinline__ void d_issue(DLoad& dl, const RowMaps& rm, uint8_t* box, int lane, int x, int y) {
+    if (lane == 0) {
+        umma::mbar_expect_tx(dl.bar, 32 * 128);
+        umma::tma_load_2d(smem_u32(box), &rm.dact, dl.bar, x, y);
+    }
+    dl.pending = true;
+}
+
 // The epilogue of one tile for one warp: its 32 rows (TMEM lane quarter q) and its half h of the columns,
 // 32 columns per TMEM load. The hidden-layer and data-gradient epilogues (tiles at least 128 wide) put
 // their row-major BF16 outputs into 32 x 64 boxes in shared memory and store each box with one TMA store
-// (lane 0); the other outputs are written directly.
+// (lane 0); the other outputs are written directly. The loss and data-gradient epilogues also leave the
+// column sums of their 32 rows (the bias gradient, reduced over the row groups by column_reduce).
+// (nm0, nn0): the origin of the warp's next item (nm0 < 0: none), where the data-gradient epilogue's
+// SiLU-derivative prefetch goes after the item's last pair. False when a wait ran out.
 template <int BN, int EPI>
-__device__ __forceinline__ void epilogue(const GemmParams& p, const RowMaps& rm, uint32_t tmem, int warp, int lane,
-                                         int m0, int n0, int z, int mt, __nv_bfloat16* stage, uint8_t* box0,
-                                         uint8_t* box1) {
+__device__ __forceinline__ bool epilogue(const GemmParams& p, const RowMaps& rm, uint32_t tmem, int warp, int lane,
+                                         int m0, int n0, int z, int mt, uint8_t* box0, uint8_t* box1, DLoad& dl,
+                                         int nm0, int nn0) {
     constexpr bool kTmaRows = (EPI == kEpiHidden || EPI == kEpiDgrad) && BN >= 128;
     const int q = warp & 3;          // the TMEM lane quarter this warp may read
     const int h = (warp - 2) >> 2;   // and its half of the tile's columns
     const int row = m0 + q * 32 + lane;
     const int trow0 = (p.dyn & kDynTarget) ? *p.row0 : 0;
     float lsum = 0.f;
+    uint4 dr[EPI == kEpiDgrad ? 8 : 1];  // the pair's SiLU derivatives (BF16), 16-byte chunks in column order
 #pragma unroll 1
     for (int c = h * (BN / 2); c < (h + 1) * (BN / 2); c += 32) {
         const int half = (c >> 5) & 1;  // which half of its 64-column box (BN / 2 is a multiple of 64)
@@ -106,22 +145,26 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, const RowMaps& rm,
         umma::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
         const int n = n0 + c;
         if constexpr (EPI == kEpiPartial) {
-            float4* dst = reinterpret_cast<float4*>(p.outf + ((size_t)z * p.M + row) * p.ld_outf + n);
+            float4* dst = reinterpret_cast<float4*>(p.outf + (size_t)z * p.split_stride + (size_t)row * p.ld_outf + n);
 #pragma unroll
             for (int j = 0; j < 8; j++) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
         } else if constexpr (EPI == kEpiLinear) {
             float4* dst = reinterpret_cast<float4*>(p.outf + (size_t)row * p.ld_outf + n);
+            const float4* b4 = reinterpret_cast<const float4*>(p.bias + n);
 #pragma unroll
-            for (int j = 0; j < 8; j++)
-                dst[j] = make_float4(v[4 * j] + p.bias[n + 4 * j], v[4 * j + 1] + p.bias[n + 4 * j + 1],
-                                     v[4 * j + 2] + p.bias[n + 4 * j + 2], v[4 * j + 3] + p.bias[n + 4 * j + 3]);
-        } else if constexpr (EPI == kEpiHidden) {
+            for (int j = 0; j < 8; j++) {
+                const float4 b = b4[j];
+                dst[j] = make_float4(v[4 * j] + b.x, v[4 * j + 1] + b.y, v[4 * j + 2] + b.z, v[4 * j + 3] + b.w);
+            }
+        } else if constexpr (EPI == kEpiHidden) {  // a = silu(z); v = silu'(z) for the backward
+            const float4* b4 = reinterpret_cast<const float4*>(p.bias + n);  // 16-byte aligned: n % 32 == 0
             float a[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const float z = v[j] + p.bias[n + j];
-                v[j] = z;
-                a[j] = siluf_(z);
+            for (int j = 0; j < 8; j++) {
+                const float4 b = b4[j];
+                const float bb[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) silu_and_derivative(v[4 * j + e] + bb[e], a[4 * j + e], v[4 * j + e]);
             }
             if constexpr (kTmaRows) {
                 if (p.out) stage_row_half(box0, lane, half, v);
@@ -130,39 +173,53 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, const RowMaps& rm,
                 if (p.out) store_row_bf16(p.out, p.ld_out, row, n, v);
                 store_row_bf16(p.out2, p.ld_out2, row, n, a);
             }
-            if (p.outT) store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
         } else if constexpr (EPI == kEpiLoss) {
-            const float* t = p.target + (size_t)(trow0 + row) * p.ld_target;
+            const float4* t4 = reinterpret_cast<const float4*>(p.target + (size_t)(trow0 + row) * p.ld_target + n);
+            const float4* b4 = reinterpret_cast<const float4*>(p.bias + n);
             float a[32];
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const float y = v[j] + p.bias[n + j];
-                const float d = (n + j < p.n_valid) ? y - t[n + j] : 0.f;
-                lsum = fmaf(d, d, lsum);
-                a[j] = d * p.grad_scale;
+            for (int j = 0; j < 8; j++) {
+                const float4 b = b4[j], t = t4[j];
+                const float bb[4] = {b.x, b.y, b.z, b.w}, tt[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int k = 4 * j + e;
+                    const float d = (n + k < p.n_valid) ? (v[k] + bb[e]) - tt[e] : 0.f;
+                    lsum = fmaf(d, d, lsum);
+                    a[k] = d * p.grad_scale;
+                }
             }
+            round_bf16(a);
             store_row_bf16(p.out, p.ld_out, row, n, a);
-            store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
+            p.colsum[(size_t)((m0 + q * 32) >> 5) * p.ld_colsum + n + lane] = column_sums32(a, lane);
         } else if constexpr (EPI == kEpiDgrad) {
-            const uint4* zp = reinterpret_cast<const uint4*>(p.zin + (size_t)row * p.ld_zin + n);
+            static_assert(BN >= 128, "data gradients stage through 64-column boxes");
+            if (half == 0) {  // this pair's SiLU derivatives have landed: into registers, then the next pair's load
+                if (!__all_sync(0xffffffffu, umma::mbar_wait(dl.bar, dl.phase))) return false;
+                dl.phase ^= 1;
+                dl.pending = false;
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    dr[j] = *reinterpret_cast<const uint4*>(box1 + lane * 128 + ((j ^ (lane & 7)) << 4));
+                umma::fence_async_shared();  // the reads above come before the next TMA write of the box
+                __syncwarp();
+                if (c + 64 < (h + 1) * (BN / 2)) d_issue(dl, rm, box1, lane, n0 + c + 64, m0 + q * 32);
+                else if (nm0 >= 0) d_issue(dl, rm, box1, lane, nn0 + h * (BN / 2), nm0 + q * 32);
+            }
             float a[32];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const uint4 w = zp[j];
+                const uint4 w = half ? dr[4 + j] : dr[j];
                 const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
-                    const float z0 = __low2float(b), z1 = __high2float(b);
-                    const float s0 = sigmoidf_(z0), s1 = sigmoidf_(z1);
-                    const int k = 8 * j + 2 * h;
-                    a[k] = v[k] * (s0 * fmaf(z0, 1.f - s0, 1.f));
-                    a[k + 1] = v[k + 1] * (s1 * fmaf(z1, 1.f - s1, 1.f));
+                for (int e = 0; e < 4; e++) {
+                    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[e]);
+                    const int k = 8 * j + 2 * e;
+                    a[k] = v[k] * __low2float(b);
+                    a[k + 1] = v[k + 1] * __high2float(b);
                 }
             }
-            if constexpr (kTmaRows) stage_row_half(box0, lane, half, a);
-            else store_row_bf16(p.out, p.ld_out, row, n, a);
-            store_col_bf16(p.outT, p.ld_outT, m0 + q * 32, n, lane, a, stage);
+            stage_row_half(box0, lane, half, a);
         }
         if constexpr (kTmaRows) {
             if (half == 1) {  // the box is complete: one TMA store per output
@@ -181,27 +238,41 @@ __device__ __forceinline__ void epilogue(const GemmParams& p, const RowMaps& rm,
             }
         }
     }
+    if constexpr (EPI == kEpiPartial) {  // row sums of A (bias-gradient partial): one TMEM column, first half
+        if (p.bias_part && h == 0 && n0 == 0)
+            p.outf[(size_t)z * p.split_stride + (size_t)p.M * p.ld_outf + row] =
+                umma::tmem_ld1(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)BN);
+    }
     if constexpr (EPI == kEpiLoss) {  // one partial per warp: no barrier among the epilogue warps
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
         if (lane == 0) p.loss[mt * kEpiWarps + h * 4 + q] = lsum;
     }
+    return true;
 }
 
 // Persistent: block b takes work items b, b + gridDim.x, ... (item = row tile + Mt (column tile + Nt
 // split)). The ring's stage index and phase run on across items, and the accumulator alternates between
 // two TMEM buffers, so that the producer and the MMA issuer start the next item while the epilogue
 // warps drain the last one (acc_full[b]: MMAs of buffer b done; acc_empty[b]: its epilogue done).
+// The weight-gradient items (kEpiPartial) read both operands MN-major: A = dZ^T and B = A_in^T straight
+// from the row-major activations [rows][width] (the batch is K), 64 x 64 boxes (2 for A, BN / 64 for B).
+// With bias_part, each K step also multiplies A by a 16-column tile of ones (N = 16, B K-major) into the
+// TMEM columns after the accumulator: every column of that product is the row sum of A over the split,
+// the bias-gradient partial. These items use one accumulator (a block takes one item on a full GPU).
 template <int BN, int EPI>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmParams p,
                 const __grid_constant__ RowMaps rm) {
+    constexpr bool kMN = EPI == kEpiPartial;
     constexpr uint32_t kA = kBM * 128, kB = BN * 128, kStage = kA + kB;
     constexpr int STAGES = kGemmRing / (int)kStage;
     static_assert(STAGES >= 2, "operand ring needs two stages");
-    constexpr uint32_t kCols = 2 * BN;  // two accumulators; TMEM columns: a power of two >= 32
+    constexpr int kBufs = kMN ? 1 : 2;  // accumulators in TMEM
+    // TMEM columns (a power of two >= 32): two accumulators, or one plus the 16 bias columns
+    constexpr uint32_t kCols = kMN ? (BN == 64 ? 128u : BN == 128 ? 256u : 512u) : 2u * BN;
     extern __shared__ uint8_t dsm[];
-    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], mma_done;
+    __shared__ uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], mma_done, zbar[kEpiWarps];
     __shared__ uint32_t tmem_s;
     const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -217,11 +288,19 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
             umma::mbar_init(smem_u32(&acc_empty[b]), kEpiWarps);
         }
         umma::mbar_init(smem_u32(&mma_done), 1);
+        for (int e = 0; e < kEpiWarps; e++) umma::mbar_init(smem_u32(&zbar[e]), 1);
         umma::fence_mbar_init();
     }
     if (warp == 1) {
         umma::tmem_alloc(smem_u32(&tmem_s), kCols);
         umma::tmem_relinquish();
+    }
+    const uint32_t ones = base + kGemmRing + kEpiWarps * 2 * kStageBox;  // 16 x 64 BF16 ones, K-major
+    if (kMN && p.bias_part && warp >= 2) {
+        uint4* o = reinterpret_cast<uint4*>(dsm + (ones - smem_u32(dsm)));
+        for (int i = threadIdx.x - 64; i < kOnesTile / 16; i += kGemmThreads - 64)
+            o[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+        umma::fence_async_shared();  // generic writes before the tensor core's reads
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -236,8 +315,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                 const int mt = w % Mt, nt = (w / Mt) % Nt, z = w / (Mt * Nt);
                 const int kb0 = (int)(((long long)z * p.k_blocks) / p.splits);
                 const int nkb = (int)(((long long)(z + 1) * p.k_blocks) / p.splits) - kb0;
-                const int ay = p.a_y0 + mt * kBM + ((p.dyn & kDynAy) ? off : 0);
-                const int bx = p.b_x0 + ((p.dyn & kDynBx) ? off : 0);
+                const int a_off = (p.dyn & kDynAy) ? off : 0, b_off = (p.dyn & kDynBx) ? off : 0;
                 for (int i = 0; i < nkb; i++, it++) {
                     const int s = it % STAGES;
                     if (it >= STAGES && !umma::mbar_wait(smem_u32(&empty[s]), ((it / STAGES) & 1) ^ 1)) {
@@ -247,8 +325,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                     const uint32_t bar = smem_u32(&full[s]), sa = base + (uint32_t)s * kStage;
                     const int kx = (kb0 + i) * kBK;
                     umma::mbar_expect_tx(bar, kStage);
-                    umma::tma_load_2d(sa, &ta, bar, p.a_x0 + kx, ay);
-                    umma::tma_load_2d(sa + kA, &tb, bar, bx + kx, p.b_y0 + nt * BN);
+                    if constexpr (kMN) {  // x: MN element (multiple of 64), y: K row
+#pragma unroll
+                        for (int j = 0; j < kBM / 64; j++)
+                            umma::tma_load_2d(sa + j * umma::kMnBlockBytes, &ta, bar, mt * kBM + 64 * j, kx + a_off);
+#pragma unroll
+                        for (int j = 0; j < BN / 64; j++)
+                            umma::tma_load_2d(sa + kA + j * umma::kMnBlockBytes, &tb, bar, nt * BN + 64 * j,
+                                              kx + b_off);
+                    } else {  // x: K element (multiple of 64), y: row
+                        umma::tma_load_2d(sa, &ta, bar, kx, mt * kBM + a_off);
+                        umma::tma_load_2d(sa + kA, &tb, bar, kx, nt * BN);
+                    }
                 }
             }
             if (!ok)  // let the copies already issued land before the block exits
@@ -257,15 +345,17 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
-            constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN);
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN, kMN, kMN);
+            constexpr uint32_t idesc_ones = umma::idesc_bf16_f32(kBM, 16, true, false);
+            const bool bias = kMN && p.bias_part;
             int it = 0, t = 0;
             for (int w = blockIdx.x; w < n_items && ok; w += gridDim.x, t++) {
                 const int z = w / (Mt * Nt);
                 const int nkb = (int)(((long long)(z + 1) * p.k_blocks) / p.splits) -
                                 (int)(((long long)z * p.k_blocks) / p.splits);
-                const int b = t & 1;
-                // buffer b is free once the epilogue of item t - 2 has read it
-                if (t >= 2 && !umma::mbar_wait(smem_u32(&acc_empty[b]), ((t >> 1) & 1) ^ 1)) {
+                const int b = t % kBufs;
+                // buffer b is free once the epilogue of item t - kBufs has read it
+                if (t >= kBufs && !umma::mbar_wait(smem_u32(&acc_empty[b]), ((t / kBufs) & 1) ^ 1)) {
                     ok = false;
                     break;
                 }
@@ -280,9 +370,17 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                     umma::fence_after_sync();
                     const uint32_t sa = base + (uint32_t)s * kStage, sb = sa + kA;
 #pragma unroll
-                    for (int k = 0; k < kBK / 16; k++)
-                        umma::mma_bf16(acc, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k), idesc,
-                                       (i | k) != 0);
+                    for (int k = 0; k < kBK / 16; k++) {
+                        if constexpr (kMN) {  // 16 K rows = two 8-row swizzle atoms per step
+                            const uint64_t ad = umma::sdesc_sw128_mn(sa + 2048u * k);
+                            umma::mma_bf16(acc, ad, umma::sdesc_sw128_mn(sb + 2048u * k), idesc, (i | k) != 0);
+                            if (bias)
+                                umma::mma_bf16(acc + (uint32_t)BN, ad, umma::sdesc_sw128(ones + 32u * k), idesc_ones,
+                                               (i | k) != 0);
+                        } else  // 16 K elements = 32 bytes of the 128-byte row per step
+                            umma::mma_bf16(acc, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k),
+                                           idesc, (i | k) != 0);
+                    }
                     umma::mma_commit(smem_u32(&empty[s]));  // frees the stage once these MMAs are done
                 }
                 if (ok) umma::mma_commit(smem_u32(&acc_full[b]));  // the item's MMAs have completed
@@ -293,22 +391,29 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
     } else {  // epilogue warps (each wait's outcome made warp-uniform: tcgen05.ld needs the whole warp)
         uint8_t* after_ring = dsm + (base - smem_u32(dsm)) + kGemmRing;
-        __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(after_ring + (warp - 2) * kStageT);
-        uint8_t* box0 = after_ring + kEpiWarps * kStageT + (warp - 2) * 2 * kStageBox;  // 1024-byte aligned
+        uint8_t* box0 = after_ring + (warp - 2) * 2 * kStageBox;  // 1024-byte aligned
         uint8_t* box1 = box0 + kStageBox;
+        DLoad dl{smem_u32(&zbar[warp - 2]), 0u, false};
+        const int q = warp & 3, h = (warp - 2) >> 2;
+        if (EPI == kEpiDgrad && (int)blockIdx.x < n_items)  // the first pair of the first item
+            d_issue(dl, rm, box1, lane, ((blockIdx.x / Mt) % Nt) * BN + h * (BN / 2), (blockIdx.x % Mt) * kBM + q * 32);
         int t = 0;
         for (int w = blockIdx.x; w < n_items; w += gridDim.x, t++) {
             const int mt = w % Mt, nt = (w / Mt) % Nt, z = w / (Mt * Nt);
-            const int b = t & 1;
-            ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full[b]), (t >> 1) & 1));
+            const int b = t % kBufs;
+            ok = __all_sync(0xffffffffu, umma::mbar_wait(smem_u32(&acc_full[b]), (t / kBufs) & 1));
             if (!ok) break;
             umma::fence_after_sync();
-            epilogue<BN, EPI>(p, rm, tmem + (uint32_t)(b * BN), warp, lane, mt * kBM, nt * BN, z, mt, stage, box0,
-                              box1);
+            const int w2 = w + (int)gridDim.x;
+            const bool more = w2 < n_items;
+            ok = epilogue<BN, EPI>(p, rm, tmem + (uint32_t)(b * BN), warp, lane, mt * kBM, nt * BN, z, mt, box0, box1,
+                                   dl, more ? (w2 % Mt) * kBM : -1, more ? ((w2 / Mt) % Nt) * BN : 0);
+            if (!ok) break;
             umma::fence_before_sync();
             __syncwarp();
             if (lane == 0) umma::mbar_arrive(smem_u32(&acc_empty[b]));
         }
+        if (dl.pending && lane == 0) umma::mbar_wait(dl.bar, dl.phase);  // a prefetch still in flight lands
         if (lane == 0) umma::bulk_wait_all();  // this warp's TMA stores have completed
     }
     if (!ok) atomicOr(p.status, kStatusGemmTimeout);
@@ -344,7 +449,9 @@ template <int EPI>
 cudaError_t gemm_bn(int BN, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, const RowMaps& rm,
                     cudaStream_t st) {
     switch (BN) {
-    case 64: return launch_gemm<64, EPI>(a, b, p, rm, st);
+    case 64:  // the data-gradient epilogue stages 64-column boxes per half tile: BN >= 128 only
+        if constexpr (EPI == kEpiDgrad) return cudaErrorInvalidValue;
+        else return launch_gemm<64, EPI>(a, b, p, rm, st);
     case 128: return launch_gemm<128, EPI>(a, b, p, rm, st);
     case 256: return launch_gemm<256, EPI>(a, b, p, rm, st);
     default: return cudaErrorInvalidValue;
@@ -353,7 +460,9 @@ cudaError_t gemm_bn(int BN, const CUtensorMap& a, const CUtensorMap& b, const Ge
 
 template <int EPI>
 cudaError_t setup_epi() {
-    cudaError_t e = cudaFuncSetAttribute(gemm_kernel<64, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    cudaError_t e = cudaSuccess;
+    if constexpr (EPI != kEpiDgrad)
+        e = cudaFuncSetAttribute(gemm_kernel<64, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(gemm_kernel<128, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
     if (e == cudaSuccess)
@@ -371,8 +480,13 @@ cudaError_t gemm_setup() {
 }
 
 cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st,
-                 const CUtensorMap* out_map, const CUtensorMap* out2_map) {
+                 const CUtensorMap* out_map, const CUtensorMap* out2_map, const CUtensorMap* dact_map) {
     if (p.M % kBM || p.N % BN || p.splits < 1 || p.splits > p.k_blocks) return cudaErrorInvalidValue;
+    if (epi == kEpiDgrad && (BN < 128 || !dact_map || !out_map)) return cudaErrorInvalidValue;
+    if (epi == kEpiLoss && !p.colsum) return cudaErrorInvalidValue;
+    if (epi == kEpiPartial && (p.split_stride < (long long)p.M * p.ld_outf + (p.bias_part ? p.M : 0) ||
+                               (p.bias_part && p.ld_outf != p.N)))
+        return cudaErrorInvalidValue;
     RowMaps rm;
     std::memset(&rm, 0, sizeof rm);
     if (BN >= 128 && (epi == kEpiHidden || epi == kEpiDgrad)) {  // these epilogues store through the maps
@@ -380,6 +494,7 @@ cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, co
         if (out_map) rm.out = *out_map;
         if (out2_map) rm.out2 = *out2_map;
     }
+    if (epi == kEpiDgrad) rm.dact = *dact_map;
     switch (epi) {
     case kEpiPartial: return gemm_bn<kEpiPartial>(BN, a, b, p, rm, st);
     case kEpiHidden: return gemm_bn<kEpiHidden>(BN, a, b, p, rm, st);
@@ -391,27 +506,27 @@ cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, co
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients).
 // Weight-gradient partials summed over the K splits in a fixed order (deterministic gradients): a block
 // covers 32 groups of four consecutive outputs (16-byte loads) with eight threads per group, thread g
 // summing splits g, g + 8, ... in order; the eight sums are then added in g order. Many threads per
-// output keep enough loads in flight: the partials are L2-resident and the sum is latency-bound.
+// output keep enough loads in flight: the partials are L2-resident and the sum is latency-bound. The
+// outputs of one split are its M x N weight partials, then (nb > 0) its nb bias partials.
 constexpr int kRedOut4 = 32, kRedGroups = 8;
 __global__ void __launch_bounds__(kRedOut4 * kRedGroups)
-    reduce_partials_kernel(const float* __restrict__ ws, int splits, int M, int N, int transpose,
-                           float* __restrict__ grad) {
+    reduce_partials_kernel(const float* __restrict__ ws, int splits, long long stride4, int M, int N, int transpose,
+                           float* __restrict__ grad_w, int nb, float* __restrict__ grad_b) {
     __shared__ float4 part[kRedGroups][kRedOut4];
-    const size_t MN4 = (size_t)M * N / 4;
+    const size_t MN = (size_t)M * N, n4 = (MN + nb) / 4;
     const int o = threadIdx.x % kRedOut4, g = threadIdx.x / kRedOut4;
     const size_t i = (size_t)blockIdx.x * kRedOut4 + o;
     const float4* w4 = reinterpret_cast<const float4*>(ws);
     float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (i < MN4) {
+    if (i < n4) {
         int z = g;
         for (; z + 3 * kRedGroups < splits; z += 4 * kRedGroups) {
             float4 v[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) v[u] = w4[(size_t)(z + u * kRedGroups) * MN4 + i];
+            for (int u = 0; u < 4; u++) v[u] = w4[(size_t)(z + u * kRedGroups) * stride4 + i];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 s.x += v[u].x;
@@ -421,7 +536,7 @@ __global__ void __launch_bounds__(kRedOut4 * kRedGroups)
             }
         }
         for (; z < splits; z += kRedGroups) {
-            const float4 v = w4[(size_t)z * MN4 + i];
+            const float4 v = w4[(size_t)z * stride4 + i];
             s.x += v.x;
             s.y += v.y;
             s.z += v.z;
@@ -430,7 +545,7 @@ __global__ void __launch_bounds__(kRedOut4 * kRedGroups)
     }
     part[g][o] = s;
     __syncthreads();
-    if (g == 0 && i < MN4) {
+    if (g == 0 && i < n4) {
         float4 t = part[0][o];
         for (int k = 1; k < kRedGroups; k++) {
             t.x += part[k][o].x;
@@ -441,57 +556,64 @@ __global__ void __launch_bounds__(kRedOut4 * kRedGroups)
         const float r[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-            const size_t e = 4 * i + h, m = e / N, n = e % N;
-            grad[transpose ? n * M + m : e] = r[h];
-        }
-    }
-}
-
-cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st) {
-    const size_t MN = (size_t)M * N;
-    if (MN % 4) return cudaErrorInvalidValue;
-    const size_t blocks = (MN / 4 + kRedOut4 - 1) / kRedOut4;
-    reduce_partials_kernel<<<(unsigned)blocks, kRedOut4 * kRedGroups, 0, st>>>(ws, splits, M, N, transpose ? 1 : 0,
-                                                                             grad);
-    return cudaGetLastError();
-}
-
-// out[r] = sum of row r of a BF16 matrix (bias gradients from the transposed output gradients), one
-// block of 1024 threads per row (eight 16-byte loads in flight per thread), fixed reduction order.
-__global__ void __launch_bounds__(1024) row_sums_kernel(const __nv_bfloat16* __restrict__ T, int cols, int ld,
-                                                        float* __restrict__ out) {
-    __shared__ float part[1024];
-    const __nv_bfloat16* r = T + (size_t)blockIdx.x * ld;
-    float s = 0.f;
-    for (int c0 = threadIdx.x * 8; c0 < cols; c0 += 1024 * 8 * 4) {
-        uint4 w[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int c = c0 + u * 1024 * 8;
-            w[u] = c < cols ? *reinterpret_cast<const uint4*>(r + c) : make_uint4(0, 0, 0, 0);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const uint32_t ws[4] = {w[u].x, w[u].y, w[u].z, w[u].w};
-#pragma unroll
-            for (int h = 0; h < 4; h++) {
-                const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&ws[h]);
-                s += __low2float(b) + __high2float(b);
+            const size_t e = 4 * i + h;
+            if (e >= MN) {
+                grad_b[e - MN] = r[h];
+            } else {
+                const size_t m = e / N, n = e % N;
+                grad_w[transpose ? n * M + m : e] = r[h];
             }
         }
     }
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 512; o > 0; o >>= 1) {
-        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[blockIdx.x] = part[0];
 }
 
-cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st) {
-    if (cols % 8 || ld % 8) return cudaErrorInvalidValue;
-    row_sums_kernel<<<rows, 1024, 0, st>>>(T, cols, ld, out);
+cudaError_t reduce_partials(const float* ws, int splits, long long stride, int M, int N, bool transpose, float* grad_w,
+                            int nb, float* grad_b, cudaStream_t st) {
+    const size_t MN = (size_t)M * N;
+    if (MN % 4 || nb % 4 || stride % 4 || stride < (long long)(MN + nb) || (nb && !grad_b)) return cudaErrorInvalidValue;
+    const size_t blocks = ((MN + nb) / 4 + kRedOut4 - 1) / kRedOut4;
+    reduce_partials_kernel<<<(unsigned)blocks, kRedOut4 * kRedGroups, 0, st>>>(ws, splits, stride / 4, M, N,
+                                                                             transpose ? 1 : 0, grad_w, nb, grad_b);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Bias gradients from column sums: out_l[c] = sum over g of part_l[g][c], the sums that the loss epilogue
+// leaves per 32 rows (the output layer's bias; the hidden layers' come from the weight-gradient GEMMs).
+// One block of 32 warps per 32 columns of a layer (lane = column, coalesced 128-byte loads); warp w sums
+// groups w, w + 32, ... in order, eight loads in flight, and the 32 warp sums are added in warp order
+// (deterministic).
+__global__ void __launch_bounds__(1024) column_reduce_kernel(const ColumnReduceArgs a) {
+    __shared__ float part[32][33];
+    int l = 0;
+    while (l + 1 < a.n_layers && (int)blockIdx.x >= a.block0[l + 1]) l++;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int cols = a.cols[l], c = ((int)blockIdx.x - a.block0[l]) * 32 + lane;
+    const float* src = a.part[l] + c;
+    float s = 0.f;
+    int g = w;
+    for (; g + 7 * 32 < a.groups; g += 8 * 32) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = src[(size_t)(g + 32 * u) * cols];
+#pragma unroll
+        for (int u = 0; u < 8; u++) s += v[u];
+    }
+    for (; g < a.groups; g += 32) s += src[(size_t)g * cols];
+    part[w][lane] = s;
+    __syncthreads();
+    if (w == 0) {
+        float t = part[0][lane];
+        for (int k = 1; k < 32; k++) t += part[k][lane];
+        a.out[l][c] = t;
+    }
+}
+
+cudaError_t column_reduce(const ColumnReduceArgs& a, cudaStream_t st) {
+    if (a.n_layers < 1 || a.n_layers > kMaxLayers) return cudaErrorInvalidValue;
+    for (int l = 0; l < a.n_layers; l++)
+        if (a.cols[l] % 32 || a.block0[l + 1] - a.block0[l] != a.cols[l] / 32) return cudaErrorInvalidValue;
+    column_reduce_kernel<<<a.block0[a.n_layers], 1024, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -676,8 +798,6 @@ __global__ void features_kernel(const FeatureArgs a) {
         __nv_bfloat16* xr = a.X + (a.row0 + c) * a.n_in;
         if (c >= a.n) {  // padding row
             for (int j = 0; j < a.n_in; j += 8) *reinterpret_cast<uint4*>(xr + j) = make_uint4(0, 0, 0, 0);
-            if (a.XT)
-                for (int j = 0; j < a.n_in; j++) a.XT[(size_t)j * a.ldXT + a.row0 + c] = __float2bfloat16_rn(0.f);
             continue;
         }
         const float pR = dbl_to_flt(a.uniform_pressure ? a.in[0][0] : a.in[0][c]);
@@ -706,9 +826,6 @@ __global__ void features_kernel(const FeatureArgs a) {
             }
             *reinterpret_cast<uint4*>(xr + j0) =
                 make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
-            if (a.XT)
-#pragma unroll
-                for (int h = 0; h < 8; h++) a.XT[(size_t)(j0 + h) * a.ldXT + a.row0 + c] = __float2bfloat16_rn(x[h]);
         }
         if (a.outside) a.outside[a.idx_base + c] = inside ? 0 : 1;
         if (a.fail_idx) {

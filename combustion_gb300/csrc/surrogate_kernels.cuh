@@ -17,19 +17,22 @@ constexpr int kEpiWarps = 8;       // loss partials per 128-row tile: one per ep
 constexpr int kBM = 128;           // rows per tile (one M = 128 MMA, one TMEM lane per row)
 constexpr int kBK = 64;            // K per pipeline stage: one 128-byte swizzle row of BF16
 constexpr int kGemmRing = 144 * 1024;  // operand ring: stages x (A + B tile)
-// Shared memory after the ring, per epilogue warp: 2 KB for transposed stores, then two 4 KB boxes
-// (32 rows x 64 BF16, 128-byte swizzle) for the TMA stores of row-major outputs.
-constexpr int kStageT = 2048, kStageBox = 4096;
-constexpr int kGemmSmem = kGemmRing + 8 * (kStageT + 2 * kStageBox) + 1024;  // + alignment; one block per SM
+// Shared memory after the ring: per epilogue warp two 4 KB boxes (32 rows x 64 BF16, 128-byte swizzle)
+// for the TMA stores of row-major outputs and the TMA loads of SiLU derivatives; then a 16 x 64 BF16 tile
+// of ones (the B operand of the bias-gradient MMAs).
+constexpr int kStageBox = 4096, kOnesTile = 16 * 128;
+constexpr int kGemmSmem = kGemmRing + 8 * 2 * kStageBox + kOnesTile + 1024;  // + alignment; one block per SM
 constexpr int kMaxIn = 259;        // rates-layout inputs for up to 256 species
 constexpr int kMaxOut = 258;       // transport outputs for up to 256 species
 constexpr int kMaxLayers = 8;
 
 enum Epilogue : int {
-    kEpiPartial = 0,  // FP32 accumulator tile to ws[split][M][N] (weight-gradient partials)
-    kEpiHidden = 1,   // z = acc + bias: Z (optional), silu(z) row-major, silu(z) transposed (optional)
-    kEpiLoss = 2,     // y = acc + bias: d = y - target (valid columns), loss partial, d * scale row-major + transposed
-    kEpiDgrad = 3,    // dz = acc * silu'(z_in): row-major + transposed
+    kEpiPartial = 0,  // FP32 accumulator tile to ws[split] (weight-gradient partials; A and B MN-major), and
+                      // with bias_part the row sums of A (A times a ones tile: the bias-gradient partials)
+    kEpiHidden = 1,   // z = acc + bias: silu(z) row-major, silu'(z) row-major (optional, for the backward)
+    kEpiLoss = 2,     // y = acc + bias: d = y - target (valid columns), loss partial, d * scale row-major,
+                      // column sums of each 32 rows
+    kEpiDgrad = 3,    // dz = acc * silu'(z) row-major
     kEpiLinear = 4,   // y = acc + bias to FP32 row-major
 };
 
@@ -38,24 +41,25 @@ enum DynOffset : int { kDynAy = 1, kDynBx = 2, kDynTarget = 4 };
 struct GemmParams {
     int M, N;               // output tile grid: M / 128 by N / BN blocks
     int k_blocks, splits;   // 64-wide K blocks in total; split z takes [z KB / S, (z + 1) KB / S)
-    int a_x0, a_y0, b_x0, b_y0;  // TMA coordinate offsets (K, row) of A and B
-    const int* row0;        // device row offset added where `dyn` says (training batch position)
-    int dyn;
+    const int* row0;        // device row offset added where `dyn` says (training batch position): to the
+    int dyn;                // rows of A (kDynAy) or to the K rows of the MN-major B (kDynBx)
     const float* bias;
     __nv_bfloat16* out;  int ld_out;   // row-major BF16 [M][ld]
     __nv_bfloat16* out2; int ld_out2;  // row-major BF16 [M][ld]
-    __nv_bfloat16* outT; int ld_outT;  // transposed BF16 [N][ld]
-    const __nv_bfloat16* zin; int ld_zin;  // pre-activations for the SiLU backward
+    float* colsum; int ld_colsum;      // [M / 32][ld]: column sums of the BF16 output over each 32 rows
+    long long split_stride;            // partials: floats from one split's [M][ld] block to the next
+    int bias_part;                     // partials: also the row sums of A, at ws[split][M][ld] + row
     const float* target; int ld_target; int n_valid; float grad_scale;
     float* loss;            // one partial per epilogue warp: [row tile][kEpiWarps]
     float* outf; int ld_outf;  // FP32 output
     int* status;
 };
 
-// TMA store maps of the row-major BF16 outputs out and out2 (boxes of 64 columns x 32 rows, 128-byte
-// swizzle): the hidden-layer (Z, silu(Z)) and data-gradient (dZ) epilogues write through them.
+// TMA maps of the epilogues' row-major BF16 matrices (boxes of 64 columns x 32 rows, 128-byte swizzle):
+// the hidden-layer (silu'(Z), silu(Z)) and data-gradient (dZ) epilogues store through out / out2; the
+// data-gradient epilogue loads the SiLU derivatives through dact.
 struct RowMaps {
-    CUtensorMap out, out2;
+    CUtensorMap out, out2, dact;
 };
 
 enum SurStatus : int { kStatusGemmTimeout = 2 };
@@ -76,7 +80,6 @@ struct FeatureArgs {
     double T0, R_over_P0;
     const float* mean; const float* rstd;  // normalisation of the raw features
     __nv_bfloat16* X; size_t row0;          // row-major [.][n_in], rows from row0
-    __nv_bfloat16* XT; size_t ldXT;         // transposed [n_in][ldXT] (optional)
     float* raw;                             // raw features [n][n_feat] (optional, statistics)
     int* hull_lo; int* hull_hi;             // order-preserving integer min / max of raw features (optional)
     const float* lo; const float* hi;       // trust region (inference gate, optional)
@@ -165,11 +168,24 @@ cudaError_t mlp_infer(const CUtensorMap& tx, const FusedMaps& maps, const FusedP
 // device; it runs before the first GEMM (and outside any stream capture).
 cudaError_t gemm_setup();
 // out_map / out2_map: store maps of p.out / p.out2 (required where the epilogue writes them: hidden layers
-// and data gradients, whose width is a multiple of 256).
+// and data gradients, whose width is a multiple of 256); dact_map: the data gradient's SiLU derivatives.
 cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, const GemmParams& p, cudaStream_t st,
-                 const CUtensorMap* out_map = nullptr, const CUtensorMap* out2_map = nullptr);
-cudaError_t reduce_partials(const float* ws, int splits, int M, int N, bool transpose, float* grad, cudaStream_t st);
-cudaError_t row_sums(const __nv_bfloat16* T, int rows, int cols, int ld, float* out, cudaStream_t st);
+                 const CUtensorMap* out_map = nullptr, const CUtensorMap* out2_map = nullptr,
+                 const CUtensorMap* dact_map = nullptr);
+// grad_w[m][n] (or [n][m] with transpose) = sum over z of ws[z * stride + m N + n]; with nb > 0 also
+// grad_b[m] = sum over z of ws[z * stride + M N + m], m < nb. Fixed order.
+cudaError_t reduce_partials(const float* ws, int splits, long long stride, int M, int N, bool transpose, float* grad_w,
+                            int nb, float* grad_b, cudaStream_t st);
+// Bias gradients from column sums, several layers in one launch: out[l][c] = sum over g < groups of
+// part[l][g][c] (fixed order), c < cols[l] (a multiple of 32); block0[l] = sum of cols[j] / 32 over j < l.
+struct ColumnReduceArgs {
+    int n_layers, groups;
+    const float* part[kMaxLayers];
+    int cols[kMaxLayers];
+    float* out[kMaxLayers];
+    int block0[kMaxLayers + 1];
+};
+cudaError_t column_reduce(const ColumnReduceArgs& a, cudaStream_t st);
 cudaError_t adam(const AdamArgs& a, cudaStream_t st);
 cudaError_t finish_step(const float* loss_part, int n_part, float norm, float* losses, int* step, int* row0,
                         int batch, int n_batches, cudaStream_t st);

@@ -1,6 +1,6 @@
 // Blackwell (sm_103a) tensor-core primitives in inline PTX: mbarriers, 2-D TMA tile loads and stores, TMEM
 // allocation, tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in TMEM), tcgen05.commit and
-// tcgen05.ld. Operand tiles are K-major with the 128-byte swizzle that TMA writes.
+// tcgen05.ld. Operand tiles are K-major or MN-major, with the 128-byte swizzle that TMA writes.
 //
 // Shared-memory operand tile (one "K block" of 64 BF16 = 128 bytes per row):
 //   row r of the tile at byte r * 128; its eight 16-byte chunks j stored at chunk j ^ (r % 8)
@@ -10,8 +10,14 @@
 // (1024: the distance between 8-row groups), the fixed version value 1 in bits 46-47, base offset 0,
 // layout type in bits 61-63 (2 = 128-byte swizzle). A K step of 16 elements inside the 128-byte row
 // advances the start address by 32 bytes; the hardware applies the swizzle to the final address.
+// MN-major operand tile (the weight-gradient GEMM reads row-major activations with the batch as K): TMA
+// boxes of 64 MN elements (128 bytes, the same swizzle) by 64 K rows, box j of the tile holding MN
+// elements [64 j, 64 j + 64) at byte 8192 j. Descriptor: leading byte offset = the distance between
+// 64-element MN blocks (8192), stride byte offset = the distance between 8-row K groups (1024); a K step
+// of 16 rows advances the start address by 2048 bytes (whole swizzle atoms).
 // Instruction descriptor (kind::f16): D format in bits 4-5 (1 = F32), A and B formats in bits 7-9 and
-// 10-12 (1 = BF16), K-major A and B (bits 15, 16 clear), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+// 10-12 (1 = BF16), A and B major in bits 15 and 16 (0 = K-major, 1 = MN-major), N >> 3 in bits 17-22,
+// M >> 4 in bits 24-28.
 // TMEM accumulator of an M = 128 MMA: row m in lane m, column n in column n (32-bit cells). A warp reads
 // the 32 lanes [32 (w % 4), 32 (w % 4) + 32) only, w its index in the block.
 #pragma once
@@ -92,8 +98,20 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
     return d;
 }
 
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+constexpr uint32_t kMnBlockBytes = 64 * 64 * 2;  // one MN-major box: 64 K rows x 128 bytes
+
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(kMnBlockBytes >> 4) << 16;  // leading byte offset: next 64-element MN block
+    d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset: next 8 K rows
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N, bool a_mn = false, bool b_mn = false) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, one elected thread.
@@ -108,6 +126,18 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
 // Arrives on the mbarrier once every MMA this thread issued before has completed.
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// One 32-bit column of this thread's TMEM lane, waited for before returning.
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
+    uint32_t r;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r)
+        : "r"(taddr)
+        : "memory");
+    return __uint_as_float(r);
 }
 
 // 32 consecutive 32-bit columns of this thread's TMEM lane, waited for before returning.

@@ -4,8 +4,9 @@ GPU forward and backward kernels; the product library never uses it).
 The surrogate has no reference counterpart. Network: layers l = 0 .. L-1, Z_l = A_l W_l^T + b_l,
 A_{l+1} = silu(Z_l) for hidden layers, the last layer linear; loss = mean over rows and valid output
 columns of (y - t)^2. With ``bf16=True`` the values the GPU stores in BF16 are rounded the same way
-(features, weights, hidden activations, the loss gradient and the back-propagated pre-activation
-gradients, round-to-nearest-even), so that the remaining difference is FP32 accumulation only.
+(features, weights, hidden activations, the SiLU derivatives at the pre-activations, the loss gradient
+and the back-propagated pre-activation gradients, round-to-nearest-even), so that the remaining
+difference is FP32 accumulation (and the GPU's approximate tanh) only.
 """
 from __future__ import annotations
 
@@ -61,5 +62,5 @@ def loss_and_grads(layers, X, T, n_valid, bf=False):
         if l == 0:
             break
         dA = G @ r(layers[l][0])
-        G = r(dA * dsilu(r(Zs[l - 1]) if bf else Zs[l - 1]))
+        G = r(dA * r(dsilu(Zs[l - 1])))
     return loss, grads, Y
