@@ -106,8 +106,7 @@ struct cb_surrogate {
     long long w_off[kMaxLayers] = {}, b_off[kMaxLayers] = {};
     float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
     bf16* W[kMaxLayers] = {};
-    bf16* WT[kMaxLayers] = {};
-    CUtensorMap mW[kMaxLayers], mWT[kMaxLayers];
+    CUtensorMap mW[kMaxLayers], mW_K[kMaxLayers];  // K-major B of the forward; MN-major B of the data gradient
     // normalisation (n_out floats each, zero beyond n_feat): in_mean, in_rstd, out_mean, out_rstd, out_std, lo, hi
     float* norm = nullptr;
     std::vector<float> h_norm;
@@ -123,7 +122,6 @@ struct cb_surrogate {
     CUtensorMap mAct_A[kMaxLayers], mdY_A, mdZ_A[2];         // K-major A operands (128-row boxes)
     CUtensorMap mAct_K[kMaxLayers], mdY_K, mdZ_K[2];         // MN-major weight-gradient operands (64-row boxes)
     CUtensorMap mSd_S[kMaxLayers], mAct_S[kMaxLayers], mdZ_S[2];  // TMA maps (32-row boxes) of the epilogues
-    float* colsum = nullptr;  // column sums of the output gradient dY per 32 rows [batch / 32][n_out]
     float* ws = nullptr;
     float* loss_part = nullptr;
     float* losses = nullptr;  // mean squared error of every step since the parameters were set
@@ -162,7 +160,7 @@ AdamArgs adam_args(cb_surrogate* s, int total_steps) {
     AdamArgs a;
     std::memset(&a, 0, sizeof a);
     a.n_layers = s->L;
-    for (int l = 0; l < s->L; l++) a.L[l] = AdamLayer{s->w_off[l], s->dims[l + 1], s->dims[l], s->W[l], s->WT[l]};
+    for (int l = 0; l < s->L; l++) a.L[l] = AdamLayer{s->w_off[l], s->dims[l + 1], s->dims[l], s->W[l]};
     a.n_weights = s->n_weights;
     a.n_params = s->n_params;
     a.lr = s->lr;
@@ -218,8 +216,6 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
             p.grad_scale = 2.0f / ((float)rows * (float)s->n_feat);
             p.out = s->dY;
             p.ld_out = s->n_out;
-            p.colsum = s->colsum;
-            p.ld_colsum = s->n_out;
             p.loss = s->loss_part;
             if (dyn) {
                 p.row0 = s->counters + 1;
@@ -238,9 +234,9 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
     }
     if (!backward) return CB_OK;
     for (int l = L - 1; l >= 0; l--) {
-        // weight gradient (split K over the rows, operands MN-major from the row-major activations) and,
-        // for the hidden layers, the bias gradient (row sums of dZ_l^T by the tensor core), reduced in a
-        // fixed order
+        // weight gradient (split K over the rows, operands MN-major from the row-major activations) and
+        // bias gradient (sums of the output gradient over the rows, by the tensor core), reduced in a fixed
+        // order
         GemmParams p = base_params(s);
         const CUtensorMap *ma, *mb;
         bool transpose;
@@ -250,13 +246,14 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
             ma = &s->mAct_K[l - 1];
             mb = &s->mdY_K;
             transpose = true;
+            p.bias_part = kBiasCols;
         } else {  // W_l = dZ_l^T A_{l-1}: M = dims[l+1], N = dims[l]
             p.M = s->dims[l + 1];
             p.N = s->dims[l];
             ma = &s->mdZ_K[l % 2];
             mb = l == 0 ? &mX_K : &s->mAct_K[l - 1];
             transpose = false;
-            p.bias_part = 1;
+            p.bias_part = kBiasRows;
             if (l == 0 && dyn) {
                 p.row0 = s->counters + 1;
                 p.dyn = kDynBx;
@@ -267,7 +264,7 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         p.splits = wgrad_splits(p.M, p.N, BN, p.k_blocks);
         p.outf = s->ws;
         p.ld_outf = p.N;
-        const int nb = p.bias_part ? p.M : 0;
+        const int nb = p.bias_part == kBiasRows ? p.M : p.N;
         p.split_stride = (long long)p.M * p.N + nb;
         SUR_CUDA(gemm(BN, kEpiPartial, *ma, *mb, p, st));
         SUR_CUDA(reduce_partials(s->ws, p.splits, p.split_stride, p.M, p.N, transpose, s->g + s->w_off[l], nb,
@@ -281,18 +278,8 @@ int run_pass(cb_surrogate* s, int rows, const CUtensorMap& mX, const CUtensorMap
         q.out = s->dZ[(l - 1) % 2];
         q.ld_out = s->width;
         const CUtensorMap& a = l == L - 1 ? s->mdY_A : s->mdZ_A[l % 2];
-        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mWT[l], q, st, &s->mdZ_S[(l - 1) % 2], nullptr, &s->mSd_S[l - 1]));
+        SUR_CUDA(gemm(bn_for(q.N), kEpiDgrad, a, s->mW_K[l], q, st, &s->mdZ_S[(l - 1) % 2], nullptr, &s->mSd_S[l - 1]));
     }
-    // the output layer's bias gradient from the loss epilogue's column sums
-    ColumnReduceArgs cr;
-    std::memset(&cr, 0, sizeof cr);
-    cr.n_layers = 1;
-    cr.groups = rows / 32;
-    cr.part[0] = s->colsum;
-    cr.cols[0] = s->n_out;
-    cr.out[0] = s->g + s->b_off[L - 1];
-    cr.block0[1] = s->n_out / 32;
-    SUR_CUDA(column_reduce(cr, st));
     if (update) {
         SUR_CUDA(adam(adam_args(s, total_steps), st));
         const int n_batches = (int)(s->n_train / s->batch);
@@ -310,11 +297,9 @@ int free_all(cb_surrogate* s) {
     for (void* q : ptrs) cudaFree(q);
     for (int l = 0; l < kMaxLayers; l++) {
         cudaFree(s->W[l]);
-        cudaFree(s->WT[l]);
         cudaFree(s->Sd[l]);
         cudaFree(s->Act[l]);
     }
-    cudaFree(s->colsum);
     if (s->stream) cudaStreamDestroy(s->stream);
     return CB_OK;
 }
@@ -490,20 +475,18 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     rc = rc ? rc : dalloc(&s->norm, (size_t)kNormRows * s->n_out);
     for (int l = 0; l < s->L && !rc; l++) {
         rc = dalloc(&s->W[l], (size_t)s->dims[l] * s->dims[l + 1]);
-        rc = rc ? rc : dalloc(&s->WT[l], (size_t)s->dims[l] * s->dims[l + 1]);
     }
     for (int l = 0; l < s->hidden && !rc; l++) {
         rc = dalloc(&s->Sd[l], B * Wd);
         rc = rc ? rc : dalloc(&s->Act[l], B * Wd);
     }
-    rc = rc ? rc : dalloc(&s->colsum, B / 32 * s->n_out);
     rc = rc ? rc : dalloc(&s->dY, B * s->n_out);
     for (int h = 0; h < 2 && !rc; h++) rc = dalloc(&s->dZ[h], B * Wd);
     // weight-gradient partials: the largest splits x M x N of any layer
     size_t ws = 0;
     for (int l = 0; l < s->L; l++) {
         const int M = l == s->L - 1 ? s->dims[l] : s->dims[l + 1], N = l == s->L - 1 ? s->dims[l + 1] : s->dims[l];
-        ws = std::max(ws, (size_t)wgrad_splits(M, N, bn_for(N), s->batch / kBK) * (M * N + M));
+        ws = std::max(ws, (size_t)wgrad_splits(M, N, bn_for(N), s->batch / kBK) * (M * N + std::max(M, N)));
     }
     rc = rc ? rc : dalloc(&s->ws, ws);
     rc = rc ? rc : dalloc(&s->losses, kMaxSteps);
@@ -517,7 +500,7 @@ int cb_surrogate_create(cb_mech* mech, const cb_surrogate_desc* d, cb_surrogate*
     const int L = s->L;
     for (int l = 0; l < L && !rc; l++) {
         rc = make_map(&s->mW[l], s->W[l], s->dims[l], s->dims[l + 1], bn_for(s->dims[l + 1]));
-        rc = rc ? rc : make_map(&s->mWT[l], s->WT[l], s->dims[l + 1], s->dims[l], bn_for(s->dims[l]));
+        rc = rc ? rc : make_map(&s->mW_K[l], s->W[l], s->dims[l], s->dims[l + 1], kBK);
     }
     for (int l = 0; l < s->hidden && !rc; l++) {
         rc = make_map(&s->mAct_A[l], s->Act[l], Wd, B, kBM);

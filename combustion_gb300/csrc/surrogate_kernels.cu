@@ -53,38 +53,6 @@ __device__ __forceinline__ void store_row_bf16(__nv_bfloat16* base, int ld, int 
                             pack_bf16(a[8 * j + 4], a[8 * j + 5]), pack_bf16(a[8 * j + 6], a[8 * j + 7]));
 }
 
-// Column sums of a warp's 32 x 32 chunk (lane = row, a[j] = column j): returns to lane j the sum of
-// column j over the 32 rows. Five exchange rounds halve the columns each lane carries (16 + 8 + 4 + 2 + 1
-// shuffles); the order of the additions is fixed.
-__device__ __forceinline__ float column_sums32(const float* a, int lane) {
-    float b[16];
-    {
-        const bool up = lane & 16;
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-            const float keep = up ? a[j + 16] : a[j], send = up ? a[j] : a[j + 16];
-            b[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-        }
-    }
-#pragma unroll
-    for (int w = 8; w >= 1; w >>= 1) {
-        const bool up = lane & w;
-#pragma unroll
-        for (int j = 0; j < w; j++) {
-            const float keep = up ? b[j + w] : b[j], send = up ? b[j] : b[j + w];
-            b[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
-        }
-    }
-    return b[0];
-}
-
-// Rounds to the nearest BF16 value in place (the value that is stored), so that sums over the stored
-// matrix are formed from the same numbers.
-__device__ __forceinline__ void round_bf16(float* a) {
-#pragma unroll
-    for (int j = 0; j < 32; j++) a[j] = __bfloat162float(__float2bfloat16_rn(a[j]));
-}
-
 // Row r (this lane) of a 32 x 64 BF16 box in the 128-byte swizzle of its TMA store map: columns
 // [32 half, 32 half + 32) are the 16-byte chunks 4 half .. 4 half + 3, chunk c of row r stored at
 // chunk position c ^ (r % 8) (eight consecutive rows hit eight different bank groups).
@@ -117,8 +85,7 @@ __device__ __forceinline__ void d_issue(DLoad& dl, const RowMaps& rm, uint8_t* b
 // The epilogue of one tile for one warp: its 32 rows (TMEM lane quarter q) and its half h of the columns,
 // 32 columns per TMEM load. The hidden-layer and data-gradient epilogues (tiles at least 128 wide) put
 // their row-major BF16 outputs into 32 x 64 boxes in shared memory and store each box with one TMA store
-// (lane 0); the other outputs are written directly. The loss and data-gradient epilogues also leave the
-// column sums of their 32 rows (the bias gradient, reduced over the row groups by column_reduce).
+// (lane 0); the other outputs are written directly.
 // (nm0, nn0): the origin of the warp's next item (nm0 < 0: none), where the data-gradient epilogue's
 // SiLU-derivative prefetch goes after the item's last pair. False when a wait ran out.
 template <int BN, int EPI>
@@ -189,9 +156,7 @@ __device__ __forceinline__ bool epilogue(const GemmParams& p, const RowMaps& rm,
                     a[k] = d * p.grad_scale;
                 }
             }
-            round_bf16(a);
             store_row_bf16(p.out, p.ld_out, row, n, a);
-            p.colsum[(size_t)((m0 + q * 32) >> 5) * p.ld_colsum + n + lane] = column_sums32(a, lane);
         } else if constexpr (EPI == kEpiDgrad) {
             static_assert(BN >= 128, "data gradients stage through 64-column boxes");
             if (half == 0) {  // this pair's SiLU derivatives have landed: into registers, then the next pair's load
@@ -238,10 +203,22 @@ __device__ __forceinline__ bool epilogue(const GemmParams& p, const RowMaps& rm,
             }
         }
     }
-    if constexpr (EPI == kEpiPartial) {  // row sums of A (bias-gradient partial): one TMEM column, first half
-        if (p.bias_part && h == 0 && n0 == 0)
-            p.outf[(size_t)z * p.split_stride + (size_t)p.M * p.ld_outf + row] =
-                umma::tmem_ld1(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)BN);
+    if constexpr (EPI == kEpiPartial) {  // bias-gradient partials, after the split's weight partials
+        float* bp = p.outf + (size_t)z * p.split_stride + (size_t)p.M * p.ld_outf;
+        if (p.bias_part == kBiasRows && h == 0 && n0 == 0)  // every column is the row sum: read one
+            bp[row] = umma::tmem_ld1(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)BN);
+        if (p.bias_part == kBiasCols && q == 0 && m0 == 0) {  // every row is the column sums: row 0 (lane 0)
+#pragma unroll 1
+            for (int c = h * (BN / 2); c < (h + 1) * (BN / 2); c += 32) {
+                float v[32];
+                umma::tmem_ld32(tmem + (uint32_t)(BN + c), v);
+                if (lane == 0) {
+                    float4* dst = reinterpret_cast<float4*>(bp + n0 + c);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                }
+            }
+        }
     }
     if constexpr (EPI == kEpiLoss) {  // one partial per warp: no barrier among the epilogue warps
 #pragma unroll
@@ -257,20 +234,21 @@ __device__ __forceinline__ bool epilogue(const GemmParams& p, const RowMaps& rm,
 // warps drain the last one (acc_full[b]: MMAs of buffer b done; acc_empty[b]: its epilogue done).
 // The weight-gradient items (kEpiPartial) read both operands MN-major: A = dZ^T and B = A_in^T straight
 // from the row-major activations [rows][width] (the batch is K), 64 x 64 boxes (2 for A, BN / 64 for B).
-// With bias_part, each K step also multiplies A by a 16-column tile of ones (N = 16, B K-major) into the
-// TMEM columns after the accumulator: every column of that product is the row sum of A over the split,
-// the bias-gradient partial. These items use one accumulator (a block takes one item on a full GPU).
+// With bias_part, each K step also multiplies by a tile of ones into the TMEM columns after the
+// accumulator: kBiasRows A times 16 columns of ones (N = 16, B K-major), each column of the product the
+// row sums of A over the split; kBiasCols 128 rows of ones (A K-major) times B, each row the column sums
+// of B^T. These items use one accumulator (a block takes one item on a full GPU).
 template <int BN, int EPI>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, const GemmParams p,
                 const __grid_constant__ RowMaps rm) {
-    constexpr bool kMN = EPI == kEpiPartial;
+    constexpr bool kMN = EPI == kEpiPartial;                  // A and B MN-major
+    constexpr bool kBMN = kMN || EPI == kEpiDgrad;            // B MN-major (data gradients: B = W row-major)
     constexpr uint32_t kA = kBM * 128, kB = BN * 128, kStage = kA + kB;
     constexpr int STAGES = kGemmRing / (int)kStage;
     static_assert(STAGES >= 2, "operand ring needs two stages");
     constexpr int kBufs = kMN ? 1 : 2;  // accumulators in TMEM
-    // TMEM columns (a power of two >= 32): two accumulators, or one plus the 16 bias columns
-    constexpr uint32_t kCols = kMN ? (BN == 64 ? 128u : BN == 128 ? 256u : 512u) : 2u * BN;
+    constexpr uint32_t kCols = 2u * BN;  // two accumulators, or one and the bias product (at most BN columns)
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], mma_done, zbar[kEpiWarps];
     __shared__ uint32_t tmem_s;
@@ -295,7 +273,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         umma::tmem_alloc(smem_u32(&tmem_s), kCols);
         umma::tmem_relinquish();
     }
-    const uint32_t ones = base + kGemmRing + kEpiWarps * 2 * kStageBox;  // 16 x 64 BF16 ones, K-major
+    const uint32_t ones = base + kGemmRing;  // weight-gradient items: 128 x 64 BF16 ones, K-major
     if (kMN && p.bias_part && warp >= 2) {
         uint4* o = reinterpret_cast<uint4*>(dsm + (ones - smem_u32(dsm)));
         for (int i = threadIdx.x - 64; i < kOnesTile / 16; i += kGemmThreads - 64)
@@ -325,16 +303,20 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                     const uint32_t bar = smem_u32(&full[s]), sa = base + (uint32_t)s * kStage;
                     const int kx = (kb0 + i) * kBK;
                     umma::mbar_expect_tx(bar, kStage);
-                    if constexpr (kMN) {  // x: MN element (multiple of 64), y: K row
+                    // MN-major: x = MN element (a multiple of 64), y = K row; K-major: x = K element, y = row
+                    if constexpr (kMN) {
 #pragma unroll
                         for (int j = 0; j < kBM / 64; j++)
                             umma::tma_load_2d(sa + j * umma::kMnBlockBytes, &ta, bar, mt * kBM + 64 * j, kx + a_off);
+                    } else {
+                        umma::tma_load_2d(sa, &ta, bar, kx, mt * kBM + a_off);
+                    }
+                    if constexpr (kBMN) {
 #pragma unroll
                         for (int j = 0; j < BN / 64; j++)
                             umma::tma_load_2d(sa + kA + j * umma::kMnBlockBytes, &tb, bar, nt * BN + 64 * j,
                                               kx + b_off);
-                    } else {  // x: K element (multiple of 64), y: row
-                        umma::tma_load_2d(sa, &ta, bar, kx, mt * kBM + a_off);
+                    } else {
                         umma::tma_load_2d(sa + kA, &tb, bar, kx, nt * BN);
                     }
                 }
@@ -345,9 +327,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
-            constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN, kMN, kMN);
-            constexpr uint32_t idesc_ones = umma::idesc_bf16_f32(kBM, 16, true, false);
-            const bool bias = kMN && p.bias_part;
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(kBM, BN, kMN, kBMN);
+            constexpr uint32_t idesc_rows = umma::idesc_bf16_f32(kBM, 16, true, false);  // A (MN) x ones
+            constexpr uint32_t idesc_cols = umma::idesc_bf16_f32(kBM, BN, false, true);  // ones x B (MN)
+            const int bias = kMN ? p.bias_part : kBiasNone;
             int it = 0, t = 0;
             for (int w = blockIdx.x; w < n_items && ok; w += gridDim.x, t++) {
                 const int z = w / (Mt * Nt);
@@ -373,13 +356,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                     for (int k = 0; k < kBK / 16; k++) {
                         if constexpr (kMN) {  // 16 K rows = two 8-row swizzle atoms per step
                             const uint64_t ad = umma::sdesc_sw128_mn(sa + 2048u * k);
-                            umma::mma_bf16(acc, ad, umma::sdesc_sw128_mn(sb + 2048u * k), idesc, (i | k) != 0);
-                            if (bias)
-                                umma::mma_bf16(acc + (uint32_t)BN, ad, umma::sdesc_sw128(ones + 32u * k), idesc_ones,
+                            const uint64_t bd = umma::sdesc_sw128_mn(sb + 2048u * k);
+                            umma::mma_bf16(acc, ad, bd, idesc, (i | k) != 0);
+                            if (bias == kBiasRows)
+                                umma::mma_bf16(acc + (uint32_t)BN, ad, umma::sdesc_sw128(ones + 32u * k), idesc_rows,
                                                (i | k) != 0);
-                        } else  // 16 K elements = 32 bytes of the 128-byte row per step
+                            else if (bias == kBiasCols)
+                                umma::mma_bf16(acc + (uint32_t)BN, umma::sdesc_sw128(ones + 32u * k), bd, idesc_cols,
+                                               (i | k) != 0);
+                        } else if constexpr (kBMN) {  // A: 32 bytes of the row per step; B: two atoms
+                            umma::mma_bf16(acc, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128_mn(sb + 2048u * k),
+                                           idesc, (i | k) != 0);
+                        } else {  // 16 K elements = 32 bytes of the 128-byte row per step
                             umma::mma_bf16(acc, umma::sdesc_sw128(sa + 32u * k), umma::sdesc_sw128(sb + 32u * k),
                                            idesc, (i | k) != 0);
+                        }
                     }
                     umma::mma_commit(smem_u32(&empty[s]));  // frees the stage once these MMAs are done
                 }
@@ -483,10 +474,12 @@ cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, co
                  const CUtensorMap* out_map, const CUtensorMap* out2_map, const CUtensorMap* dact_map) {
     if (p.M % kBM || p.N % BN || p.splits < 1 || p.splits > p.k_blocks) return cudaErrorInvalidValue;
     if (epi == kEpiDgrad && (BN < 128 || !dact_map || !out_map)) return cudaErrorInvalidValue;
-    if (epi == kEpiLoss && !p.colsum) return cudaErrorInvalidValue;
-    if (epi == kEpiPartial && (p.split_stride < (long long)p.M * p.ld_outf + (p.bias_part ? p.M : 0) ||
-                               (p.bias_part && p.ld_outf != p.N)))
-        return cudaErrorInvalidValue;
+    if (epi == kEpiPartial) {
+        const long long nb = p.bias_part == kBiasRows ? p.M : p.bias_part == kBiasCols ? p.N : 0;
+        if (p.split_stride < (long long)p.M * p.ld_outf + nb || (p.bias_part && p.ld_outf != p.N) ||
+            p.bias_part < kBiasNone || p.bias_part > kBiasCols)
+            return cudaErrorInvalidValue;
+    }
     RowMaps rm;
     std::memset(&rm, 0, sizeof rm);
     if (BN >= 128 && (epi == kEpiHidden || epi == kEpiDgrad)) {  // these epilogues store through the maps
@@ -578,57 +571,13 @@ cudaError_t reduce_partials(const float* ws, int splits, long long stride, int M
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Bias gradients from column sums: out_l[c] = sum over g of part_l[g][c], the sums that the loss epilogue
-// leaves per 32 rows (the output layer's bias; the hidden layers' come from the weight-gradient GEMMs).
-// One block of 32 warps per 32 columns of a layer (lane = column, coalesced 128-byte loads); warp w sums
-// groups w, w + 32, ... in order, eight loads in flight, and the 32 warp sums are added in warp order
-// (deterministic).
-__global__ void __launch_bounds__(1024) column_reduce_kernel(const ColumnReduceArgs a) {
-    __shared__ float part[32][33];
-    int l = 0;
-    while (l + 1 < a.n_layers && (int)blockIdx.x >= a.block0[l + 1]) l++;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int cols = a.cols[l], c = ((int)blockIdx.x - a.block0[l]) * 32 + lane;
-    const float* src = a.part[l] + c;
-    float s = 0.f;
-    int g = w;
-    for (; g + 7 * 32 < a.groups; g += 8 * 32) {
-        float v[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) v[u] = src[(size_t)(g + 32 * u) * cols];
-#pragma unroll
-        for (int u = 0; u < 8; u++) s += v[u];
-    }
-    for (; g < a.groups; g += 32) s += src[(size_t)g * cols];
-    part[w][lane] = s;
-    __syncthreads();
-    if (w == 0) {
-        float t = part[0][lane];
-        for (int k = 1; k < 32; k++) t += part[k][lane];
-        a.out[l][c] = t;
-    }
-}
-
-cudaError_t column_reduce(const ColumnReduceArgs& a, cudaStream_t st) {
-    if (a.n_layers < 1 || a.n_layers > kMaxLayers) return cudaErrorInvalidValue;
-    for (int l = 0; l < a.n_layers; l++)
-        if (a.cols[l] % 32 || a.block0[l + 1] - a.block0[l] != a.cols[l] / 32) return cudaErrorInvalidValue;
-    column_reduce_kernel<<<a.block0[a.n_layers], 1024, 0, st>>>(a);
-    return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------------------------------
-// Adam on the FP32 master parameters (weights of every layer, then biases), writing the BF16 weights and
-// their transposes that the GEMMs read. The step counter lives on the device (CUDA-graph replays).
+// Adam on the FP32 master parameters (weights of every layer, then biases), writing the BF16 weights that
+// the GEMMs read (row-major [out][in]: the forward's K-major B, the data gradient's MN-major B). The step counter lives on the device (CUDA-graph replays).
 __device__ __forceinline__ void write_bf16_weight(const AdamArgs& a, long long i, float w) {
     int l = 0;
     while (l + 1 < a.n_layers && i >= a.L[l + 1].w_off) l++;
     const AdamLayer& L = a.L[l];
-    const long long r = i - L.w_off;
-    const int o = (int)(r / L.n_in), c = (int)(r % L.n_in);
-    const __nv_bfloat16 b = __float2bfloat16_rn(w);
-    L.W[(size_t)o * L.n_in + c] = b;
-    L.WT[(size_t)c * L.n_out + o] = b;
+    L.W[i - L.w_off] = __float2bfloat16_rn(w);
 }
 
 __global__ void adam_kernel(const AdamArgs a) {

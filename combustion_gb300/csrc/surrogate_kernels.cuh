@@ -18,25 +18,30 @@ constexpr int kBM = 128;           // rows per tile (one M = 128 MMA, one TMEM l
 constexpr int kBK = 64;            // K per pipeline stage: one 128-byte swizzle row of BF16
 constexpr int kGemmRing = 144 * 1024;  // operand ring: stages x (A + B tile)
 // Shared memory after the ring: per epilogue warp two 4 KB boxes (32 rows x 64 BF16, 128-byte swizzle)
-// for the TMA stores of row-major outputs and the TMA loads of SiLU derivatives; then a 16 x 64 BF16 tile
-// of ones (the B operand of the bias-gradient MMAs).
-constexpr int kStageBox = 4096, kOnesTile = 16 * 128;
-constexpr int kGemmSmem = kGemmRing + 8 * 2 * kStageBox + kOnesTile + 1024;  // + alignment; one block per SM
+// for the TMA stores of row-major outputs and the TMA loads of SiLU derivatives. The weight-gradient
+// items, whose epilogue writes straight to global memory, keep a 128 x 64 BF16 tile of ones there instead
+// (the extra operand of the bias-gradient MMAs).
+constexpr int kStageBox = 4096, kOnesTile = 128 * 128;
+constexpr int kGemmSmem = kGemmRing + 8 * 2 * kStageBox + 1024;  // + alignment; one block per SM
 constexpr int kMaxIn = 259;        // rates-layout inputs for up to 256 species
 constexpr int kMaxOut = 258;       // transport outputs for up to 256 species
 constexpr int kMaxLayers = 8;
 
 enum Epilogue : int {
     kEpiPartial = 0,  // FP32 accumulator tile to ws[split] (weight-gradient partials; A and B MN-major), and
-                      // with bias_part the row sums of A (A times a ones tile: the bias-gradient partials)
+                      // with bias_part the bias-gradient partials (row sums of A or column sums of B, by
+                      // MMAs with a tile of ones)
     kEpiHidden = 1,   // z = acc + bias: silu(z) row-major, silu'(z) row-major (optional, for the backward)
-    kEpiLoss = 2,     // y = acc + bias: d = y - target (valid columns), loss partial, d * scale row-major,
-                      // column sums of each 32 rows
+    kEpiLoss = 2,     // y = acc + bias: d = y - target (valid columns), loss partial, d * scale row-major
     kEpiDgrad = 3,    // dz = acc * silu'(z) row-major
     kEpiLinear = 4,   // y = acc + bias to FP32 row-major
 };
 
 enum DynOffset : int { kDynAy = 1, kDynBx = 2, kDynTarget = 4 };
+// Bias-gradient partials of a weight-gradient GEMM D = A B^T (A = dZ^T of a hidden layer, or A_in^T of the
+// output layer with B = dY^T): kBiasRows = the row sums of A (M values, A times 16 columns of ones),
+// kBiasCols = the column sums of B^T (N values, 128 rows of ones times B^T).
+enum BiasPart : int { kBiasNone = 0, kBiasRows = 1, kBiasCols = 2 };
 
 struct GemmParams {
     int M, N;               // output tile grid: M / 128 by N / BN blocks
@@ -46,9 +51,8 @@ struct GemmParams {
     const float* bias;
     __nv_bfloat16* out;  int ld_out;   // row-major BF16 [M][ld]
     __nv_bfloat16* out2; int ld_out2;  // row-major BF16 [M][ld]
-    float* colsum; int ld_colsum;      // [M / 32][ld]: column sums of the BF16 output over each 32 rows
     long long split_stride;            // partials: floats from one split's [M][ld] block to the next
-    int bias_part;                     // partials: also the row sums of A, at ws[split][M][ld] + row
+    int bias_part;                     // partials: kBiasRows / kBiasCols, after the split's [M][ld] block
     const float* target; int ld_target; int n_valid; float grad_scale;
     float* loss;            // one partial per epilogue warp: [row tile][kEpiWarps]
     float* outf; int ld_outf;  // FP32 output
@@ -137,7 +141,6 @@ struct AdamLayer {
     long long w_off;
     int n_out, n_in;
     __nv_bfloat16* W;
-    __nv_bfloat16* WT;
 };
 struct AdamArgs {
     AdamLayer L[kMaxLayers];
@@ -176,16 +179,7 @@ cudaError_t gemm(int BN, int epi, const CUtensorMap& a, const CUtensorMap& b, co
 // grad_b[m] = sum over z of ws[z * stride + M N + m], m < nb. Fixed order.
 cudaError_t reduce_partials(const float* ws, int splits, long long stride, int M, int N, bool transpose, float* grad_w,
                             int nb, float* grad_b, cudaStream_t st);
-// Bias gradients from column sums, several layers in one launch: out[l][c] = sum over g < groups of
-// part[l][g][c] (fixed order), c < cols[l] (a multiple of 32); block0[l] = sum of cols[j] / 32 over j < l.
-struct ColumnReduceArgs {
-    int n_layers, groups;
-    const float* part[kMaxLayers];
-    int cols[kMaxLayers];
-    float* out[kMaxLayers];
-    int block0[kMaxLayers + 1];
-};
-cudaError_t column_reduce(const ColumnReduceArgs& a, cudaStream_t st);
+
 cudaError_t adam(const AdamArgs& a, cudaStream_t st);
 cudaError_t finish_step(const float* loss_part, int n_part, float norm, float* losses, int* step, int* row0,
                         int batch, int n_batches, cudaStream_t st);
