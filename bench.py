@@ -150,6 +150,38 @@ def measured_bf16_peak():
     return 1900.0, "fallback 1.9 PFLOP/s bf16, of fallback"
 
 
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        v = json.load(open(path)).get("hbm_gbs")
+        if v:
+            return float(v), "MEASURED_PEAKS.json hbm_gbs (copy), of measured"
+    return 6800.0, "fallback 6.8 TB/s, of fallback"
+
+
+def train_step_bytes(batch, n_in, width, hidden, n_out, n_params):
+    """Algorithmic HBM bytes of one training step as the kernels move them: every BF16 activation matrix
+    written once by its forward epilogue (silu(Z), silu'(Z)) and read by the GEMMs that consume it, the
+    FP32 targets, the output gradient and the pre-activation gradients, the split-K weight-gradient
+    partials written and read back, and Adam's FP32 state (p, g, m, v read; p, m, v and the BF16 weights
+    written). Weight reads (L2-resident) are left out."""
+    B = batch
+
+    def splits(M, N):
+        bn = 256 if N % 256 == 0 else 128 if N % 128 == 0 else 64
+        return min(max(1, 148 // ((M // 128) * (N // bn))), B // 64)
+
+    act = B * width * 2
+    fwd = B * n_in * 2 + 2 * act                              # layer 0: X in, silu and silu' out
+    fwd += (hidden - 1) * (act + 2 * act)                     # hidden layers 1 .. H-1
+    fwd += act + B * n_out * 4 + B * n_out * 2                # output layer: targets in, dY out
+    bwd = act + B * n_out * 2 + 2 * 4 * splits(width, n_out) * (width * n_out + n_out)   # output wgrad
+    bwd += B * n_out * 2 + act + act                          # output dgrad: dY, silu' in, dZ out
+    bwd += (hidden - 1) * (2 * act + 2 * 4 * splits(width, width) * (width * width + width) + 3 * act)
+    bwd += act + B * n_in * 2 + 2 * 4 * splits(width, n_in) * (width * n_in + width)     # first-layer wgrad
+    return fwd + bwd + n_params * (4 * 4 + 3 * 4 + 2)
+
+
 RATES_GROUPS = (("dTdt", slice(0, 1)), ("dVdt", slice(1, 2)), ("species", slice(2, None)))
 TRANSPORT_GROUPS = (("conductivity", slice(0, 1)), ("viscosity", slice(1, 2)), ("diffusion", slice(2, None)))
 
@@ -267,6 +299,16 @@ def run_surrogate(args, mech, d_in, r_out, t_out, n, world, stream, mixed_ms):
     best = max((p for p in points if p["measured_max_rel_err"] <= p["stated_max_rel_err"]),
                key=lambda p: p["cells_per_s"], default=None)
     at_bar = next(p for p in points if p["stated_max_rel_err"] == 1e-4)
+    # the training step is bound by HBM traffic (each layer's GEMM is 4-8 us of tensor work against
+    # 15-20 us of activation reads and writes): its roofline is bytes per step over the copy bandwidth
+    hbm, hbm_src = measured_hbm_peak()
+    step_s = train_s / (2 * args.sur_steps)
+    tb = train_step_bytes(info.batch, info.n_in, info.width, info.hidden_layers, info.n_out, int(info.n_params))
+    train_roofline = {"bound": "hbm", "bytes_per_step": tb, "achieved": tb / step_s / 1e9, "peak": hbm,
+                      "unit": "GB/s", "frac": tb / step_s / 1e9 / hbm, "peak_source": hbm_src,
+                      "tensor_frac_sustained": 2 * train_flops * args.sur_steps / train_s / 1e12 /
+                      float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops_sustained", 1700.0))
+                      if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None}
     beats_mixed = [p["stated_max_rel_err"] for p in points if p["ms_per_step"] < mixed_ms and p["fallback_rate"] < 1.0]
     # the network alone (no gate): mixed rates + one network's transport, timed the same way
     def ungated():
@@ -304,7 +346,8 @@ def run_surrogate(args, mech, d_in, r_out, t_out, n, world, stream, mixed_ms):
                      "optimizer": "Adam lr 1e-3, cosine decay to 1e-5", "loss_first": float(losses[0][0]),
                      "loss_last": float(np.mean(losses[0][-20:])), "generate_s": gen_s, "train_s": train_s,
                      "ms_per_step": 1e3 * train_s / (2 * args.sur_steps),
-                     "tflops": 2 * train_flops * args.sur_steps / train_s / 1e12},
+                     "tflops": 2 * train_flops * args.sur_steps / train_s / 1e12,
+                     "roofline": train_roofline},
         "calibration": {"cells": n_cal, "seed": 5, "median_max_rel_err": float(err_cal.median()),
                         "fraction_within_1e-4": float((err_cal <= 1e-4).double().mean()),
                         "fraction_within_1e-2": float((err_cal <= 1e-2).double().mean())},
