@@ -34,9 +34,14 @@ __device__ __forceinline__ void accumulate_group_m(const RatesMixedTables& tb, c
     for (int r = MODEL ? tb.H->group_end[MODEL - 1] : 0; r < tb.H->group_end[MODEL]; r++) {
         const ReactionF& x = tb.reactions[r];
         const double cR = reaction_rate_m<MODEL>(tb, x, c, MODEL >= 2 ? c.Mf[x.eff_row] : 0.f);
+        // read-modify-writes in pairs, the two reads issued together (net species are distinct)
 #pragma unroll 1
-        for (int q = 0; q < x.n_net; q++)
-            wdot[x.net_k[q]] = fma(int_to_double_small(x.net_n[q]), cR, wdot[x.net_k[q]]);
+        for (int q = 0; q < x.n_net; q += 2) {
+            const int k0 = x.net_k[q], k1 = x.net_k[q + 1 < x.n_net ? q + 1 : q];
+            const double w0 = wdot[k0], w1 = wdot[k1];
+            wdot[k0] = fma(int_to_double_small(x.net_n[q]), cR, w0);
+            if (q + 1 < x.n_net) wdot[k1] = fma(int_to_double_small(x.net_n[q + 1]), cR, w1);
+        }
     }
 }
 
@@ -122,7 +127,7 @@ __device__ void rates_mixed_cell(const RatesMixedTables& tb, const RatesArgs<KMA
 }
 
 template <int KMAX, bool SMEM>
-__global__ void __launch_bounds__(kBlock) rates_mixed_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
+__global__ void __launch_bounds__(kBlock, 2) rates_mixed_kernel(const uint8_t* __restrict__ gtab, uint32_t tab_bytes,
                                                             const __grid_constant__ RatesArgs<KMAX> io, size_t n,
                                                             int* status) {
     __shared__ uint64_t bar;

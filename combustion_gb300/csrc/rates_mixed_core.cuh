@@ -36,14 +36,57 @@ __device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, fl
     return min_pos(kF32Max, exp_f32x(fmaf(a.b, lnT, fmaf(a.mEa, rcpT, a.lnA))));
 }
 
+// Product of the side's concentrations with multiplicities (reaction.rs:53-63), species order. The loads
+// (kMaxSide slots, absent ones skipped) are issued together before the first multiply, so that a cell's
+// thread-local reads overlap instead of each waiting for the previous factor.
 __device__ __forceinline__ double conc_product_m(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
-    double p = C[ks[0]];
+    double v[kMaxSide];
+#pragma unroll
+    for (int q = 0; q < kMaxSide; q++) v[q] = q < n ? C[ks[q]] : 1.0;
+    double p = v[0];
 #pragma unroll 1
-    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+    for (int m = 1; m < ns[0]; m++) p *= v[0];
+#pragma unroll
+    for (int q = 1; q < kMaxSide; q++) {
+        if (q < n) {
 #pragma unroll 1
-    for (int q = 1; q < n; q++)
+            for (int m = 0; m < ns[q]; m++) p *= v[q];
+        }
+    }
+    return p;
+}
+
+// Product of the net species' cached Gibbs exponentials, |nu| times each, species order: four loads
+// issued together per batch, as in conc_product_m.
+template <class CellT>
+__device__ __forceinline__ double gibbs_product_m(const ReactionF& x, const CellT& c) {
+    double p = 1.0;
+#pragma unroll
+    for (int q0 = 0; q0 < kMaxNet; q0 += 4) {
+        if (q0 >= x.n_net) break;
+        double v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int q = q0 + j;
+            v[j] = q < x.n_net ? (x.net_n[q] > 0 ? c.ex[x.net_k[q]] : c.exn[x.net_k[q]]) : 1.0;
+        }
+        int j0 = 0;
+        if (q0 == 0) {  // seeded with the first factor
+            p = v[0];
+            const int nu0 = x.net_n[0];
 #pragma unroll 1
-        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
+            for (int m = 1; m < (nu0 > 0 ? nu0 : -nu0); m++) p *= v[0];
+            j0 = 1;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j >= j0 && q0 + j < x.n_net) {
+                const int nu = x.net_n[q0 + j];
+#pragma unroll 1
+                for (int m = 0; m < (nu > 0 ? nu : -nu); m++) p *= v[j];
+            }
+        }
+    }
     return p;
 }
 
@@ -56,20 +99,43 @@ __device__ __forceinline__ double int_to_double_small(int v) {
     return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
 }
 
-// cR of one reaction. MODEL is a compile-time constant (reactions are grouped by model), so no
-// predicated FP64 instruction of another model's branch is executed.
+// e^x and e^-x of an FP64 argument to FP32 relative accuracy (a few 1e-8) over the FP64 range: x = n ln2
+// + r with n = rint(x / ln2) and r formed in FP64 (three FP64 instructions; the reduction error is
+// below 1e-13 for |x| < 708), e^r and e^-r in FP32 (exp2f of r log2(e)), then 2^n and 2^-n added to the
+// exponent fields with integer instructions (|n| <= 1021 keeps both results normal). Beyond |x| = 708,
+// infinities and NaN: the FP64 exponential and its reciprocal.
+__device__ __forceinline__ void exp_pair_mixed(double x, double& ep, double& em) {
+    const int hi = __double2hiint(x);
+    if ((hi & 0x7fffffff) >= 0x40862000) {
+        ep = exp64(x);
+        em = rcp64(ep);
+        return;
+    }
+    const double t = fma(x, 0x1.71547652b82fep+0, 0x1.8p52);  // x / ln2 + 1.5 * 2^52: n in the low word
+    const int n = __double2loint(t);
+    const double r = fma(t - 0x1.8p52, -0x1.62e42fefa39efp-1, x);
+    const float rl = dbl_to_flt(r) * 0x1.715476p+0f;  // r log2(e), |r| <= ln2 / 2
+    const long long bp = __double_as_longlong(flt_to_dbl(exp2f(rl)));
+    const long long bm = __double_as_longlong(flt_to_dbl(exp2f(-rl)));
+    ep = __longlong_as_double(bp + ((long long)n << 52));
+    em = __longlong_as_double(bm - ((long long)n << 52));
+}
+
 // The cached Gibbs exponentials of the mixed program for exponent x (reaction.rs:234-263), with the
 // standard-state factor of the equilibrium constant folded in: ex = min(M3, e^x) RT/P0 and
 // exn = min(cbrt(f32::MAX), e^-x) P0/RT, so that a reaction's product of |nu| factors per net species
-// carries (P0/RT)^(-sum nu) without a multiply per reaction; e^-x is the FP64 reciprocal of e^x (3 FP64
-// operations instead of an exponential's 9; its zero and infinity meet the same clamps).
+// carries (P0/RT)^(-sum nu) without a multiply per reaction. Both exponentials to FP32 relative accuracy
+// (exp_pair_mixed: 3 FP64 operations where an FP64 exponential and reciprocal take 12).
 __device__ __forceinline__ void gibbs_exps(double x, bool need_exp, bool need_exp_neg, double M3, double cbrt_max,
                                            double C0, double rcpC0, double& ex, double& exn) {
-    const double e = exp64(x);
-    if (need_exp) ex = min_pos(M3, e) * rcpC0;
-    if (need_exp_neg) exn = min_pos(cbrt_max, rcp64(e)) * C0;
+    double ep, em;
+    exp_pair_mixed(x, ep, em);
+    if (need_exp) ex = min_pos(M3, ep) * rcpC0;
+    if (need_exp_neg) exn = min_pos(cbrt_max, em) * C0;
 }
 
+// cR of one reaction. MODEL is a compile-time constant (reactions are grouped by model), so no
+// predicated FP64 instruction of another model's branch is executed.
 // CellT: any cell view with C, ex, exn (FP64, indexable, from gibbs_exps), C0, rcpC0, rcpC0sq and the FP32
 // temperatures Ctotf, Tf, lnTf, rcpTf (one thread's cell here, one warp's cell in the batched reactors).
 // Mf: the reaction's FP32 third-body concentration (unused by models 0 and 1).
@@ -134,19 +200,8 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
     const double Rf = conc_product_m(c.C, x.r_k, x.r_n, x.n_r);
     double Rnet = Rf;
     if constexpr (MODEL != 1) {
-        const int nu0 = x.net_n[0];
-        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
-        double p = t0;
-#pragma unroll 1
-        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
-#pragma unroll 1
-        for (int q = 1; q < x.n_net; q++) {
-            const int nu = x.net_n[q], k = x.net_k[q];
-            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
-#pragma unroll 1
-            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
-        }
         // (P0/RT)^(-sum nu) is folded into the cell's exponentials (gibbs_exps), one factor per use
+        const double p = gibbs_product_m(x, c);
         Rnet = fma(-p, conc_product_m(c.C, x.p_k, x.p_n, x.n_p), Rf);
     }
     return kf * Rnet;
