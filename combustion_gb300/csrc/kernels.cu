@@ -114,10 +114,15 @@ __device__ void rates_cell(const RatesTables& tb, const RatesArgs<KMAX>& io, siz
     double wdot[KMAX];
     for (int k = 0; k < A; k++) wdot[k] = 0.0;
     // species_rates (reaction.rs:312-327), reactions grouped by model
+    // read-modify-writes in pairs, the two reads issued together (net species are distinct)
     auto accumulate = [&](const Reaction& x, double cR) {
 #pragma unroll 1
-        for (int q = 0; q < x.n_net; q++)
-            wdot[x.net_k[q]] = fma(small_int_to_double(x.net_n[q]), cR, wdot[x.net_k[q]]);
+        for (int q = 0; q < x.n_net; q += 2) {
+            const int k0 = x.net_k[q], k1 = x.net_k[q + 1 < x.n_net ? q + 1 : q];
+            const double w0 = wdot[k0], w1 = wdot[k1];
+            wdot[k0] = fma(small_int_to_double(x.net_n[q]), cR, w0);
+            if (q + 1 < x.n_net) wdot[k1] = fma(small_int_to_double(x.net_n[q + 1]), cR, w1);
+        }
     };
     plain_group<KMAX, 0>(tb, c, accumulate);
     plain_group<KMAX, 1>(tb, c, accumulate);

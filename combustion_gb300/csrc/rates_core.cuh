@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "device_common.cuh"
 #include "device_math.cuh"
 #include "tables.h"
@@ -70,17 +72,92 @@ __device__ __forceinline__ double small_int_to_double(int v) {
 }
 
 // Product of concentrations with multiplicities (product_of_exponentiations, reaction.rs:53-63),
-// seeded with the first factor.
+// seeded with the first factor. BATCH (a thread's own cell, arrays in thread-local memory): the loads
+// (kMaxSide slots, absent ones skipped) are issued together before the first multiply, so that the reads
+// overlap instead of each waiting for the previous factor. Otherwise (a warp's cell in shared memory,
+// one reaction per lane) one load per factor, fewer registers. The multiplication order is the same.
+template <bool BATCH>
 __device__ __forceinline__ double conc_product(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
-    double p = C[ks[0]];
+    if constexpr (BATCH) {
+        double v[kMaxSide];
+#pragma unroll
+        for (int q = 0; q < kMaxSide; q++) v[q] = q < n ? C[ks[q]] : 1.0;
+        double p = v[0];
 #pragma unroll 1
-    for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+        for (int m = 1; m < ns[0]; m++) p *= v[0];
+#pragma unroll
+        for (int q = 1; q < kMaxSide; q++) {
+            if (q < n) {
 #pragma unroll 1
-    for (int q = 1; q < n; q++)
+                for (int m = 0; m < ns[q]; m++) p *= v[q];
+            }
+        }
+        return p;
+    } else {
+        double p = C[ks[0]];
 #pragma unroll 1
-        for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
-    return p;
+        for (int m = 1; m < ns[0]; m++) p *= C[ks[0]];
+#pragma unroll 1
+        for (int q = 1; q < n; q++)
+#pragma unroll 1
+            for (int m = 0; m < ns[q]; m++) p *= C[ks[q]];
+        return p;
+    }
 }
+
+// 1/Kc without its standard-state factor: the cached Gibbs exponentials of the net species, |nu| times
+// each, in species order; with BATCH four loads issued together per batch, as in conc_product.
+template <bool BATCH, class Rx, class CellT>
+__device__ __forceinline__ double gibbs_product(const Rx& x, const CellT& c) {
+    if constexpr (BATCH) {
+        double p = 1.0;
+#pragma unroll
+        for (int q0 = 0; q0 < kMaxNet; q0 += 4) {
+            if (q0 >= x.n_net) break;
+            double v[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int q = q0 + j;
+                v[j] = q < x.n_net ? (x.net_n[q] > 0 ? c.ex[x.net_k[q]] : c.exn[x.net_k[q]]) : 1.0;
+            }
+            int j0 = 0;
+            if (q0 == 0) {  // seeded with the first factor
+                p = v[0];
+                const int nu0 = x.net_n[0];
+#pragma unroll 1
+                for (int m = 1; m < (nu0 > 0 ? nu0 : -nu0); m++) p *= v[0];
+                j0 = 1;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (j >= j0 && q0 + j < x.n_net) {
+                    const int nu = x.net_n[q0 + j];
+#pragma unroll 1
+                    for (int m = 0; m < (nu > 0 ? nu : -nu); m++) p *= v[j];
+                }
+            }
+        }
+        return p;
+    } else {
+        const int nu0 = x.net_n[0];
+        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
+        double p = t0;
+#pragma unroll 1
+        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
+#pragma unroll 1
+        for (int q = 1; q < x.n_net; q++) {
+            const int nu = x.net_n[q], k = x.net_k[q];
+            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
+#pragma unroll 1
+            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
+        }
+        return p;
+    }
+}
+
+// Cells whose arrays are the thread's own (thread-local memory) batch their loads.
+template <class CellT>
+constexpr bool kBatchLoads = std::is_array<decltype(CellT::C)>::value;
 
 // Pieces of one reaction's rate of progress, for the analytic Jacobian: cR = kf * Rnet with
 // Rnet = Rf - pK * Pp, and dkf/dM the forward coefficient's derivative in the third-body concentration.
@@ -169,7 +246,8 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
         if constexpr (PARTS) parts->dkf_dM = 0.0;
     }
     // Rate of progress (reaction.rs:269-306).
-    const double Rf = conc_product(c.C, x.r_k, x.r_n, x.n_r);
+    constexpr bool B = kBatchLoads<CellT>;
+    const double Rf = conc_product<B>(c.C, x.r_k, x.r_n, x.n_r);
     double Rnet = Rf;
     if constexpr (PARTS) {
         parts->kf = kf;
@@ -179,23 +257,12 @@ __device__ __forceinline__ double reaction_eval(const RatesTables& tb, const Rea
     }
     if constexpr (MODEL != 1) {
         // 1/Kc: product of the cached Gibbs exponentials, repeated |nu| times, in species order.
-        const int nu0 = x.net_n[0];
-        const double t0 = nu0 > 0 ? c.ex[x.net_k[0]] : c.exn[x.net_k[0]];
-        double p = t0;
-#pragma unroll 1
-        for (int n = 1; n < (nu0 > 0 ? nu0 : -nu0); n++) p *= t0;
-#pragma unroll 1
-        for (int q = 1; q < x.n_net; q++) {
-            const int nu = x.net_n[q], k = x.net_k[q];
-            const double tt = nu > 0 ? c.ex[k] : c.exn[k];
-#pragma unroll 1
-            for (int n = 0; n < (nu > 0 ? nu : -nu); n++) p *= tt;
-        }
+        double p = gibbs_product<B>(x, c);
         // (P0/RT)^(-sum nu): the factor chosen with integer selects, one multiply for every reaction.
         const int msn = x.minus_sigma_net;
         const double cfac = msn == 1 ? c.C0 : msn == -1 ? c.rcpC0 : msn == -2 ? c.rcpC0sq : 1.0;
         p *= cfac;
-        const double Pp = conc_product(c.C, x.p_k, x.p_n, x.n_p);
+        const double Pp = conc_product<B>(c.C, x.p_k, x.p_n, x.n_p);
         Rnet = fma(-p, Pp, Rf);
         if constexpr (PARTS) {
             parts->pK = p;

@@ -8,6 +8,7 @@
 
 #include "device_common.cuh"
 #include "device_math.cuh"
+#include "rates_core.cuh"
 #include "tables_mixed.h"
 
 namespace cbg {
@@ -36,59 +37,7 @@ __device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, fl
     return min_pos(kF32Max, exp_f32x(fmaf(a.b, lnT, fmaf(a.mEa, rcpT, a.lnA))));
 }
 
-// Product of the side's concentrations with multiplicities (reaction.rs:53-63), species order. The loads
-// (kMaxSide slots, absent ones skipped) are issued together before the first multiply, so that a cell's
-// thread-local reads overlap instead of each waiting for the previous factor.
-__device__ __forceinline__ double conc_product_m(const double* C, const uint16_t* ks, const int8_t* ns, int n) {
-    double v[kMaxSide];
-#pragma unroll
-    for (int q = 0; q < kMaxSide; q++) v[q] = q < n ? C[ks[q]] : 1.0;
-    double p = v[0];
-#pragma unroll 1
-    for (int m = 1; m < ns[0]; m++) p *= v[0];
-#pragma unroll
-    for (int q = 1; q < kMaxSide; q++) {
-        if (q < n) {
-#pragma unroll 1
-            for (int m = 0; m < ns[q]; m++) p *= v[q];
-        }
-    }
-    return p;
-}
-
-// Product of the net species' cached Gibbs exponentials, |nu| times each, species order: four loads
-// issued together per batch, as in conc_product_m.
-template <class CellT>
-__device__ __forceinline__ double gibbs_product_m(const ReactionF& x, const CellT& c) {
-    double p = 1.0;
-#pragma unroll
-    for (int q0 = 0; q0 < kMaxNet; q0 += 4) {
-        if (q0 >= x.n_net) break;
-        double v[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int q = q0 + j;
-            v[j] = q < x.n_net ? (x.net_n[q] > 0 ? c.ex[x.net_k[q]] : c.exn[x.net_k[q]]) : 1.0;
-        }
-        int j0 = 0;
-        if (q0 == 0) {  // seeded with the first factor
-            p = v[0];
-            const int nu0 = x.net_n[0];
-#pragma unroll 1
-            for (int m = 1; m < (nu0 > 0 ? nu0 : -nu0); m++) p *= v[0];
-            j0 = 1;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            if (j >= j0 && q0 + j < x.n_net) {
-                const int nu = x.net_n[q0 + j];
-#pragma unroll 1
-                for (int m = 0; m < (nu > 0 ? nu : -nu); m++) p *= v[j];
-            }
-        }
-    }
-    return p;
-}
+// The products of the rate of progress are the FP64 path's (rates_core.cuh: conc_product, gibbs_product).
 
 __device__ __forceinline__ double int_to_double_small(int v) {
     if (v == 0) return 0.0;
@@ -197,12 +146,13 @@ __device__ __forceinline__ double reaction_rate_m(const RatesMixedTables& tb, co
         kf = arrhenius_f(x.k, c.lnTf, c.rcpTf);
     }
     // FP64 rate of progress (reaction.rs:269-306).
-    const double Rf = conc_product_m(c.C, x.r_k, x.r_n, x.n_r);
+    constexpr bool B = kBatchLoads<CellT>;
+    const double Rf = conc_product<B>(c.C, x.r_k, x.r_n, x.n_r);
     double Rnet = Rf;
     if constexpr (MODEL != 1) {
         // (P0/RT)^(-sum nu) is folded into the cell's exponentials (gibbs_exps), one factor per use
-        const double p = gibbs_product_m(x, c);
-        Rnet = fma(-p, conc_product_m(c.C, x.p_k, x.p_n, x.n_p), Rf);
+        const double p = gibbs_product<B>(x, c);
+        Rnet = fma(-p, conc_product<B>(c.C, x.p_k, x.p_n, x.n_p), Rf);
     }
     return kf * Rnet;
 }
