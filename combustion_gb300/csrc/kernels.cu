@@ -221,6 +221,36 @@ __device__ __forceinline__ double diffusion_of(double MVTN, double VT, double W,
     return div64(__dsub_rn(MVTN, __dmul_rn(__dmul_rn(VT, W), X)), S);
 }
 
+// Rows k0 .. k0 + Q - 1 of Wilke's mixing sums (transport.rs:148-158, the square expanded), each summed
+// over j in order, and their terms of mu added in row order.
+template <int Q>
+__device__ __forceinline__ double wilke_rows(const double* A2, const double* AB, const double* B2, int K, int k0,
+                                             const double* X, const double* Y, const double* Z, const double* v,
+                                             double mu) {
+    const double* a2 = A2 + (size_t)k0 * K;
+    const double* ab = AB + (size_t)k0 * K;
+    const double* b2 = B2 + (size_t)k0 * K;
+    double s1[Q], s2[Q], s3[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) s1[q] = s2[q] = s3[q] = 0.0;
+    for (int j = 0; j < K; j++) {
+        const double xj = X[j], yj = Y[j], zj = Z[j];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            s1[q] = fma(a2[q * K + j], xj, s1[q]);
+            s2[q] = fma(ab[q * K + j], yj, s2[q]);
+            s3[q] = fma(b2[q * K + j], zj, s3[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int k = k0 + q;
+        const double den = fma(v[k], fma(v[k], s3[q], s2[q]), s1[q]);
+        mu = fma(X[k] * (v[k] * v[k]), rcp64(den), mu);
+    }
+    return mu;
+}
+
 template <int KMAX>
 __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io, size_t i, size_t o) {
     // i: the cell's index in the inputs, o: in the outputs (they differ for gathered cells)
@@ -267,32 +297,16 @@ __device__ void transport_cell(const uint8_t* tab, const TransportArgs<KMAX>& io
         Y[k] = X[k] * r;
         Z[k] = Y[k] * r;
     }
-    // Four rows per pass over j (rows padded with zeros to a multiple of 4): 12 independent FMA chains
-    // per thread and one load of X_j, Y_j, Z_j per 12 FMAs.
+    // Four rows per pass over j: 12 independent FMA chains per thread and one load of X_j, Y_j, Z_j per
+    // 12 FMAs; the last K % 4 rows in a pass of their own size (no FMAs on padding rows).
     double mu = 0.0;
-    for (int k0 = 0; k0 < K; k0 += 4) {
-        const double* a2 = A2 + (size_t)k0 * K;
-        const double* ab = AB + (size_t)k0 * K;
-        const double* b2 = B2 + (size_t)k0 * K;
-        double s1[4] = {0.0, 0.0, 0.0, 0.0}, s2[4] = {0.0, 0.0, 0.0, 0.0}, s3[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int j = 0; j < K; j++) {
-            const double xj = X[j], yj = Y[j], zj = Z[j];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                s1[q] = fma(a2[q * K + j], xj, s1[q]);
-                s2[q] = fma(ab[q * K + j], yj, s2[q]);
-                s3[q] = fma(b2[q * K + j], zj, s3[q]);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int k = k0 + q;
-            if (k < K) {
-                const double den = fma(v[k], fma(v[k], s3[q], s2[q]), s1[q]);
-                mu = fma(X[k] * (v[k] * v[k]), rcp64(den), mu);
-            }
-        }
+    int k0 = 0;
+    for (; k0 + 4 <= K; k0 += 4) mu = wilke_rows<4>(A2, AB, B2, K, k0, X, Y, Z, v, mu);
+    if (K - k0 >= 2) {
+        mu = wilke_rows<2>(A2, AB, B2, K, k0, X, Y, Z, v, mu);
+        k0 += 2;
     }
+    if (K - k0 == 1) mu = wilke_rows<1>(A2, AB, B2, K, k0, X, Y, Z, v, mu);
     io.out[1][o] = VT * mu;
 
     // Mixture-averaged diffusion (transport.rs:162-177); S reuses Y.
