@@ -211,7 +211,9 @@ cudaError_t copy_rows(double* stage, size_t chunk, const double* const* rows, in
 // Host arrays: chunks through two device staging slots. Copies run on their own streams and kernels on
 // one compute stream (one chunk's kernels at a time: the kernels use persistent grids), so that the
 // copies of neighbouring chunks overlap the kernels: H2D(c+1) and D2H(c-1) run while chunk c computes.
-// One cudaMemcpyAsync per array per chunk.
+// Only the first chunk's upload and the last chunk's download are exposed, so those two chunks are one
+// wave of the path's kernels; the others are the standard chunk, one of them taking the remainder.
+// One cudaMemcpyAsync per array per chunk (one 2-D copy per run of equally spaced host rows).
 int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* const* out, uint32_t flags) {
     const int ni = n_inputs(m, path), no = n_outputs(m, path);
     const bool uniform = rates_layout(path) && (flags & CB_UNIFORM_PRESSURE);
@@ -242,9 +244,20 @@ int call_host(cb_mech* m, Path path, size_t n, const double* const* in, double* 
     cudaStream_t h2d = m->copy_stream[0], comp = m->copy_stream[1], d2h = m->copy_stream[2];
     std::vector<const double*> din(ni);
     std::vector<double*> dout(no);
-    size_t c = 0;
-    for (size_t lo = 0; lo < n; lo += chunk, c++) {
-        const size_t len = n - lo < chunk ? n - lo : chunk;
+    std::vector<size_t> sizes;  // chunk lengths, in order
+    const size_t edge = wave && wave < chunk ? wave : chunk;
+    if (n <= 2 * edge) {
+        for (size_t lo = 0; lo < n; lo += chunk) sizes.push_back(std::min(chunk, n - lo));
+    } else {
+        sizes.push_back(edge);
+        size_t mid = n - 2 * edge;
+        for (; mid >= chunk; mid -= chunk) sizes.push_back(chunk);
+        if (mid) sizes.push_back(mid);
+        sizes.push_back(edge);
+    }
+    size_t lo = 0;
+    for (size_t c = 0; c < sizes.size(); lo += sizes[c], c++) {
+        const size_t len = sizes[c];
         const int s = (int)(c & 1);
         cudaEvent_t* ev = m->slot_event[s];
         double* base = m->d_stage + s * per_slot;

@@ -154,7 +154,8 @@ def test_ragged_sizes(n):
 
 
 def test_host_memory_path_and_uniform_pressure():
-    """CB_HOST_MEMORY with more cells than one staging chunk, and the uniform-pressure constants."""
+    """CB_HOST_MEMORY with more cells than one staging chunk (first and last chunks of one wave, standard
+    chunks between, one of them the remainder), and the uniform-pressure constants."""
     from combustion_gb300 import synthetic
     m = util.mechanism("k10")
     mech = _mech(m)
@@ -176,6 +177,17 @@ def test_host_memory_path_and_uniform_pressure():
     mech.transport(np.array(tin), tout)
     tref, tscale = o.transport(tin, nthreads=NTHREADS, scale=True)
     assert util.cond_err(tout, tref, tscale).max() <= util.PLAIN_TOL
+    # the fused call on host arrays equals the device call bit for bit
+    torch = _torch()
+    ro = torch.empty((mech.A + 2, n), dtype=torch.float64, device="cuda")
+    to = torch.empty((mech.K + 2, n), dtype=torch.float64, device="cuda")
+    mech.rates_transport(_dev(ins), ro, to)
+    torch.cuda.synchronize()
+    mech.synchronize()
+    hro, hto = np.zeros((mech.A + 2, n)), np.zeros((mech.K + 2, n))
+    mech.rates_transport(np.array(ins), hro, hto)
+    assert np.array_equal(hro, ro.cpu().numpy()) and np.array_equal(hto, to.cpu().numpy())
+    assert np.array_equal(hro, out)
 
 
 def test_errors_are_reported_not_raised_on_device():
