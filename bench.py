@@ -607,8 +607,15 @@ def run_ours(args):
     m_r_out = torch.empty_like(r_out)
     m_t_out = torch.empty_like(t_out)
 
-    def step_mixed():
+    mix_mid = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    mix_bound = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+
+    def step_mixed(s=None):
+        if s is not None:
+            mix_bound[s].record(stream)
         mech.rates(d_in, m_r_out, mixed=True)
+        if s is not None:
+            mix_mid[s].record(stream)
         mech.transport(t_in, m_t_out, mixed=True)
 
     for _ in range(args.warmup):
@@ -624,11 +631,28 @@ def run_ours(args):
         torch.cuda.synchronize()
         mix_start.record(stream)
         for s in range(args.steps):
-            step_mixed()
+            step_mixed(s)
         mix_end.record(stream)
+        mix_bound[args.steps].record(stream)
         torch.cuda.synchronize()
     mech.synchronize()
     mixed_ms = mix_start.elapsed_time(mix_end) / args.steps
+    mixed_rates_ms = float(np.mean([mix_bound[s].elapsed_time(mix_mid[s]) for s in range(args.steps)]))
+    mixed_transport_ms = float(np.mean([mix_mid[s].elapsed_time(mix_bound[s + 1]) for s in range(args.steps)]))
+    # The mixed rates kernel is bound by the FP64 pipe (the steps the form keeps in FP64): its roofline is
+    # FP64 instructions per cell (ncu count, profiles/ncu_traffic.json) over the measured FP64 issue rate.
+    mixed_roofline = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        rm = json.load(open(tpath)).get("rates_mixed", {})
+        if rm.get("fp64_inst_per_cell"):
+            fp64_rate = cb.device_fp64_peak()  # FP64 instructions (FMA, MUL, ADD alike) per second
+            achieved_inst = rm["fp64_inst_per_cell"] * n / (mixed_rates_ms * 1e-3)
+            mixed_roofline = {"bound": "fp64", "kernel": "rates_mixed", "achieved": achieved_inst / 1e12,
+                              "peak": fp64_rate / 1e12, "unit": "T FP64 instructions/s",
+                              "frac": achieved_inst / fp64_rate, "fp64_inst_per_cell": rm["fp64_inst_per_cell"],
+                              "traffic": rm.get("dram_bytes_per_cell", 0) * n,
+                              "source": "FP64 instruction count of one ncu capture (" + rm.get("source", "") + ")"}
     rates_ms = [a.elapsed_time(b) for a, b in zip(ev_start, ev_mid)]
     transport_ms = [a.elapsed_time(b) for a, b in zip(ev_mid, ev_end)]
     total_ms = ev_start[0].elapsed_time(ev_end[-1])
@@ -772,7 +796,9 @@ def run_ours(args):
                 "plain_f64": {"cells_per_s": value, "ms_per_step": ms_per_step,
                               "max_err": None if parity is None else max(parity["rates_max_err"], parity["transport_max_err"])},
                 "mixed": {"cells_per_s": world * n / (mixed_ms * 1e-3), "ms_per_step": mixed_ms, "error": mixed_err,
-                          "api": "cb_rates_mixed + cb_transport_mixed"},
+                          "api": "cb_rates_mixed + cb_transport_mixed",
+                          "kernels_ms": {"rates_mixed": mixed_rates_ms, "transport_mixed": mixed_transport_ms},
+                          "roofline": mixed_roofline},
                 "mixed_surrogate": surrogate_form,
             },
             "reactors": reactors_form,
