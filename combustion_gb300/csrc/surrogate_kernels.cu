@@ -942,8 +942,11 @@ cudaError_t audit(const AuditArgs& a, size_t cap, cudaStream_t st) {
 // the MMAs of the other. Shape: 64 inputs, hidden width 256, 64 outputs (up to 62 species).
 //   warp 0: TMA producer (input tiles, weight chunks in the MMAs' order)
 //   warp 1: TMEM owner and MMA issuer
-//   warps 2-9: epilogue, two warps per TMEM lane quarter (columns 0-127 and 128-255)
-constexpr int kFusedThreads = 320;
+//   warps 2-17: epilogue, four warps per TMEM lane quarter (64 columns each; the 64-wide output layer
+//   takes two, 32 columns each): sixteen warps keep enough instructions in flight for a tile's epilogue
+//   to take about as long as the other tile's MMAs
+constexpr int kFusedEpiWarps = 16;
+constexpr int kFusedThreads = 64 + 32 * kFusedEpiWarps;
 constexpr int kFusedWidth = 256;
 constexpr uint32_t kActChunk = kBM * 128;              // 16 KB: 128 rows x 64 BF16
 constexpr uint32_t kActBytes = 4 * kActChunk;           // one tile's activations (256 columns)
@@ -970,10 +973,16 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     extern __shared__ uint8_t dsm[];
     __shared__ uint64_t w_full[kWStages], w_empty[kWStages], x_full[2], acc_full[2], act_ready[2], act_free[2], fin;
     __shared__ uint32_t tmem_s;
+    // biases of every layer, the hidden layers' halved: silu(z) = h (1 + tanh h) with h = z / 2 = fma(1/2,
+    // acc, b / 2), one FMA where z = acc + b and h = z / 2 took two (the same h: halving is exact)
+    __shared__ __align__(16) float sbias[kMaxLayers * kFusedWidth];
     const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
     const uint32_t act0 = base, wring = base + 2 * kActBytes;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int L = p.L;
+    for (int l = 0; l < L; l++)
+        for (int c = threadIdx.x; c < p.dims[l + 1]; c += blockDim.x)
+            sbias[l * kFusedWidth + c] = (l < L - 1 ? 0.5f : 1.0f) * p.bias[l][c];
     const int tiles = p.rows / kBM;
     const int pairs = (tiles + 1) / 2;
     if (threadIdx.x == 0) {
@@ -984,7 +993,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         for (int t = 0; t < 2; t++) {
             umma::mbar_init(smem_u32(&x_full[t]), 1);
             umma::mbar_init(smem_u32(&acc_full[t]), 1);
-            umma::mbar_init(smem_u32(&act_ready[t]), 8);
+            umma::mbar_init(smem_u32(&act_ready[t]), kFusedEpiWarps);
             umma::mbar_init(smem_u32(&act_free[t]), 1);
         }
         umma::mbar_init(smem_u32(&fin), 1);
@@ -1072,17 +1081,19 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
             umma::mma_commit(smem_u32(&fin));  // every MMA issued here has completed before TMEM is freed
             umma::mbar_wait(smem_u32(&fin), 0);
         }
-    } else {  // epilogue warps 2..9
+    } else {  // epilogue warps 2..17
         const int e = warp - 2;
         const int q = warp & 3;          // TMEM lane quarter
-        const int half = e >> 2;         // column half
+        const int quarter = e >> 2;      // column quarter
         const int r = q * 32 + lane;     // row within the tile
         int pi = 0;
         for (int pr = blockIdx.x; pr < pairs && ok; pr += gridDim.x, pi++) {
             for (int l = 0; l < L && ok; l++) {
                 const int N = p.dims[l + 1];
-                const int cols = N / 2;  // this warp's columns: [half * cols, half * cols + cols)
-                const float* bias = p.bias[l];
+                // this warp's columns: a quarter of N in chunks of 32 (N = 64: the first two quarters only)
+                const int cols = N >= 128 ? N / 4 : 32;
+                const int c_begin = quarter * cols < N ? quarter * cols : N;
+                const float* bias = sbias + l * kFusedWidth;  // halved for the hidden layers
                 for (int t = 0; t < 2 && ok; t++) {
                     const int tile = 2 * pr + t;
                     if (tile >= tiles) break;
@@ -1095,19 +1106,29 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
                     const uint32_t acc = tmem + (uint32_t)(t * 256) + ((uint32_t)(q * 32) << 16);
                     const uint32_t a_base = act0 + t * kActBytes;
 #pragma unroll 1
-                    for (int c = half * cols; c < half * cols + cols; c += 32) {
+                    for (int c = c_begin; c < c_begin + cols && c < N; c += 32) {
                         float v[32];
                         umma::tmem_ld32(acc + (uint32_t)c, v);
+                        const float4* b4 = reinterpret_cast<const float4*>(bias + c);  // broadcast reads
                         if (l < L - 1) {
 #pragma unroll
-                            for (int j = 0; j < 32; j++) v[j] = siluf_(v[j] + bias[c + j]);
+                            for (int j = 0; j < 8; j++) {
+                                const float4 hb = b4[j];
+                                const float hbb[4] = {hb.x, hb.y, hb.z, hb.w};
+#pragma unroll
+                                for (int e = 0; e < 4; e++) {
+                                    const float h = fmaf(0.5f, v[4 * j + e], hbb[e]);
+                                    v[4 * j + e] = fmaf(h, tanh_approx(h), h);
+                                }
+                            }
                             store_act_bf16(a_base + (uint32_t)(c >> 6) * kActChunk, r, c, v);
                         } else {
                             float4* dst = reinterpret_cast<float4*>(p.Y + ((size_t)tile * kBM + r) * p.ldY + c);
 #pragma unroll
-                            for (int j = 0; j < 8; j++)
-                                dst[j] = make_float4(v[4 * j] + bias[c + 4 * j], v[4 * j + 1] + bias[c + 4 * j + 1],
-                                                     v[4 * j + 2] + bias[c + 4 * j + 2], v[4 * j + 3] + bias[c + 4 * j + 3]);
+                            for (int j = 0; j < 8; j++) {
+                                const float4 b = b4[j];
+                                dst[j] = make_float4(v[4 * j] + b.x, v[4 * j + 1] + b.y, v[4 * j + 2] + b.z, v[4 * j + 3] + b.w);
+                            }
                         }
                     }
                     // activations visible to the tensor core, accumulator reads complete: the MMAs of the
