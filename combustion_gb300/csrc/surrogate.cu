@@ -4,11 +4,12 @@
 //
 // Network: dims[0] = n_in (K + 2 features padded to 64) -> hidden layers of `width` (SiLU) -> dims[L] =
 // n_out (K + 2 outputs padded to 64). Layer l computes Z = A_{l-1} W_l^T + b_l with W_l [dims[l+1]][dims[l]].
-// Training step (one CUDA graph): forward GEMMs keep Z, silu(Z) and its transpose per hidden layer, the
-// output GEMM's epilogue forms the MSE gradient; backward runs per layer a split-K weight-gradient GEMM
-// (transposed activations as K-major operands), a deterministic reduction of the partials and the bias
-// row sums, and the data-gradient GEMM whose epilogue applies the SiLU derivative; Adam updates the FP32
-// master weights and rewrites the BF16 weights and their transposes.
+// Training step (one CUDA graph): forward GEMMs keep silu(Z) and silu'(Z) per hidden layer (row-major),
+// the output GEMM's epilogue forms the MSE gradient; backward runs per layer a split-K weight-gradient
+// GEMM that reads the row-major activations and gradients as MN-major operands and adds the bias-gradient
+// partials (MMAs against a tile of ones), a deterministic reduction of both partials, and the
+// data-gradient GEMM (row-major W as its MN-major B) whose epilogue multiplies by silu'(Z); Adam updates
+// the FP32 master weights and rewrites the BF16 weights.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -2,8 +2,10 @@
 //
 // The GEMM is D[M][N] = A[M][K] B[N][K]^T over BF16 operands with an FP32 accumulator in tensor memory:
 // 128 x BN output tiles taken in turn by a persistent block per SM (two accumulators in tensor memory,
-// so that one tile's epilogue runs under the next tile's MMAs), operands streamed through a ring of shared-memory stages by TMA
-// (128-byte swizzle, K-major), tcgen05.mma issued by one thread, the accumulator read back by eight
+// so that one tile's epilogue runs under the next tile's MMAs), operands streamed through a ring of
+// shared-memory stages by TMA (128-byte swizzle, K-major or MN-major per GEMM: the weight gradients read
+// both operands MN-major, the data gradients B), tcgen05.mma issued by one thread, the accumulator read
+// back by eight
 // epilogue warps (one TMEM lane, i.e. one output row, per thread; two warps per lane quarter, each on
 // half of the columns) which apply the layer's element-wise work before anything is written to global
 // memory. Every mbarrier wait is bounded: a wait that runs
