@@ -110,6 +110,21 @@ def test_transport_parity(config, n):
     assert ce.max() <= util.PLAIN_TOL
 
 
+@pytest.mark.parametrize("K", [11, 15])
+def test_transport_species_count_3_mod_4(K, monkeypatch):
+    """Wilke's mixing rows run in passes of 4, then one of 2 and one of 1: a species count of 3 mod 4 takes
+    both remainder passes (10 and 250 take the 2-row pass, 53 the 1-row pass)."""
+    from combustion_gb300 import synthetic
+    monkeypatch.setitem(synthetic.CONFIGS, f"k{K}", dict(K=K, elementary=2 * K, three_body=4, troe=2))
+    m = synthetic.generate_mechanism(f"k{K}")
+    assert m.K == K
+    mech = _mech(m)
+    o = _oracle_for(m, mech)
+    cells = synthetic.generate_cells(K, 4096, "k10")
+    x, ref, scale = _run_transport(mech, o, cells)
+    assert _report(f"transport k{K}", x, ref, scale).max() <= util.PLAIN_TOL
+
+
 def test_branch_mechanism_parity():
     m = branch_mechanism()
     mech = _mech(m)
