@@ -39,8 +39,8 @@ __device__ __forceinline__ void accumulate_group_m(const RatesMixedTables& tb, c
         for (int q = 0; q < x.n_net; q += 2) {
             const int k0 = x.net_k[q], k1 = x.net_k[q + 1 < x.n_net ? q + 1 : q];
             const double w0 = wdot[k0], w1 = wdot[k1];
-            wdot[k0] = fma(int_to_double_small(x.net_n[q]), cR, w0);
-            if (q + 1 < x.n_net) wdot[k1] = fma(int_to_double_small(x.net_n[q + 1]), cR, w1);
+            wdot[k0] = fma(small_int_to_double(x.net_n[q]), cR, w0);
+            if (q + 1 < x.n_net) wdot[k1] = fma(small_int_to_double(x.net_n[q + 1]), cR, w1);
         }
     }
 }

@@ -39,15 +39,6 @@ __device__ __forceinline__ double arrhenius_f(const ArrheniusF& a, float lnT, fl
 
 // The products of the rate of progress are the FP64 path's (rates_core.cuh: conc_product, gibbs_product).
 
-__device__ __forceinline__ double int_to_double_small(int v) {
-    if (v == 0) return 0.0;
-    const unsigned a = v < 0 ? (unsigned)(-v) : (unsigned)v;
-    const int e = 31 - __clz(a);
-    const unsigned long long mant = (unsigned long long)(a ^ (1u << e)) << (52 - e);
-    const unsigned long long sign = v < 0 ? (1ull << 63) : 0ull;
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(1023 + e) << 52) | mant));
-}
-
 // e^x and e^-x of an FP64 argument to FP32 relative accuracy (a few 1e-8) over the FP64 range: x = n ln2
 // + r with n = rint(x / ln2) and r formed in FP64 (three FP64 instructions; the reduction error is
 // below 1e-13 for |x| < 708), e^r and e^-r in FP32 (exp2f of r log2(e)), then 2^n and 2^-n added to the

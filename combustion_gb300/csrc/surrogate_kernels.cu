@@ -29,10 +29,6 @@ __device__ __forceinline__ float tanh_approx(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float siluf_(float z) {
-    const float h = 0.5f * z;
-    return fmaf(h, tanh_approx(h), h);
-}
 // silu(z) and silu'(z) from one tanh: with h = z / 2 and t = tanh(h), sigmoid(z) = (1 + t) / 2, so
 // silu(z) = h (1 + t) and silu'(z) = sigmoid(z) (1 + z (1 - sigmoid(z))) = (1 + t + h (1 - t^2)) / 2.
 __device__ __forceinline__ void silu_and_derivative(float z, float& s, float& d) {
